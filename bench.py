@@ -1,0 +1,500 @@
+#!/usr/bin/env python3
+"""Benchmark: frame-pairs/s for SSIMULACRA2 at 1080p (headline) and Butteraugli at 4K.
+
+Workloads (seeded synthetic frames, vship_gb300.synth; no dataset is available offline):
+  * ssimu2_1080p : 240 pairs of 1920x1080 YUV420P10 (BT.709, limited range; 8x8 block-DCT
+                   distortion, step U[4, 32], chroma x2), converted to float32 R'G'B' planes.
+  * butter_4k    : 60 pairs of 3840x2160 YUV420P10, Gaussian blur sigma U[0.5, 2] + noise sigma
+                   U[1, 6], float32 R'G'B' planes, intensity 203, Qnorm 2.
+
+A step scores every pair of the workload once.
+  value : inputs resident in HBM, batched device entry points (Vship_*ComputeDeviceAsync), CUDA
+          events on the launching stream around the K timed steps. Inputs (12 GB per workload)
+          are far larger than L2, so no flush is needed between steps.
+  e2e   : the reference-facing C ABI (Vship_ComputeSSIMU2Float / Vship_ComputeButteraugliFloatv3)
+          from pinned host buffers, one handler per host thread; every call copies its planes
+          host->device and reads its score back.
+
+--impl reference runs the reference's math on the host cores instead (the reference has no CPU
+implementation and its CUDA build cannot run on this machine, so this is the FP32 CPU
+restatement in oracle/, threaded over all host cores), one bounded sample per step.
+
+Multi-GPU: every rank runs the full workload on its own GPU (frame pairs are independent,
+replicas only); value = pairs over all ranks / max over ranks of the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W1080, H1080 = 1920, 1080
+W4K, H4K = 3840, 2160
+
+
+def total_scale_pixels(w: int, h: int) -> int:
+    t = 0
+    for _ in range(6):
+        t += w * h
+        w, h = (w - 1) // 2 + 1, (h - 1) // 2 + 1
+    return t
+
+
+# Algorithmic bytes of the dominant kernels, per frame pair (FP32 planes):
+#   ssimu2_stats reads both XYB pyramids once: 2 images x 3 channels x 4 B x T pixels.
+#   butter_diff reads the 20 band planes (LF vals, MF, HF, UHF of both images) once and writes
+#   4 planes (AC sum, DC sum, two mask precomputes) at each of the two scales.
+def ssimu2_stats_bytes(w, h):
+    return 2 * 3 * 4 * total_scale_pixels(w, h)
+
+
+def butter_diff_bytes(w, h):
+    n = w * h
+    nh = ((w - 1) // 2 + 1) * ((h - 1) // 2 + 1)
+    return 24 * 4 * (n + nh)
+
+
+# Whole-pipeline algorithmic bytes per pair (b_in = 3 B/px for 16-bit 4:2:0 input; FP32 planes).
+def ssimu2_pair_bytes(w, h):
+    return 2 * 3 * w * h + 2 * 12 * total_scale_pixels(w, h) * 2
+
+
+def butter_pair_bytes(w, h):
+    n = w * h
+    nh = ((w - 1) // 2 + 1) * ((h - 1) // 2 + 1)
+    return 2 * 3 * n + 272 * (n + nh) + 8 * n + 4 * nh
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str):
+    """DRAM bytes per launch for `kernel` from the committed ncu summary, if one exists."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(kernel)
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for ln in f:
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+# distributed helpers (replicas only)
+
+def dist_setup(args):
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------
+# workloads
+
+def make_inputs(kind: str, npairs: int, device):
+    """Device-resident float32 R'G'B' planes: (npairs, 3, H, W) for reference and distorted."""
+    import torch
+    from vship_gb300 import synth
+    if kind == "ssimu2":
+        h, w, dist = H1080, W1080, "dct"
+    else:
+        h, w, dist = H4K, W4K, "blur_noise"
+    ref = torch.empty((npairs, 3, h, w), dtype=torch.float32, device=device)
+    dst = torch.empty_like(ref)
+    for t in range(npairs):
+        r, d = synth.yuv420p10_frames(h, w, t, seed=7 if kind == "ssimu2" else 11, distortion=dist, device=device)
+        ref[t] = synth.yuv420p10_to_rgb(r)
+        dst[t] = synth.yuv420p10_to_rgb(d)
+    return ref, dst
+
+
+def frames_table(v, ref, dst, start, count):
+    frames = []
+    for t in range(start, start + count):
+        for x in (ref, dst):
+            frames.append(([x[t, c].data_ptr() for c in range(3)], x.stride(2) * 4))
+    return v.device_frames_table(frames)
+
+
+def run_device(v, kind, ref, dst, steps, warmup, ws, chunk):
+    """Batched device-resident throughput; returns (seconds for `steps` steps, profile dict, launches)."""
+    import torch
+    npairs, _, h, w = ref.shape
+    if kind == "ssimu2":
+        eng = v.SSIMU2Batch(w, h, chunk)
+        out = torch.zeros(npairs, dtype=torch.float64, device="cuda")
+    else:
+        eng = v.ButteraugliBatch(w, h, chunk, 2, 203.0)
+        out = torch.zeros(npairs * 3, dtype=torch.float64, device="cuda")
+    tables = []
+    for s in range(0, npairs, chunk):
+        c = min(chunk, npairs - s)
+        tables.append((s, c, frames_table(v, ref, dst, s, c)))
+    stream = torch.cuda.current_stream()
+
+    def step():
+        for s, c, tb in tables:
+            if kind == "ssimu2":
+                eng.compute_async(tb.data_ptr(), c, v.IN_FLOAT, out[s:].data_ptr(), stream.cuda_stream)
+            else:
+                eng.compute_async(tb.data_ptr(), c, v.IN_FLOAT, out[3 * s:].data_ptr(), 0, stream.cuda_stream)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    v.profile_report()  # clear
+    v.profile_enable(True)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    v.profile_enable(False)
+    barrier(ws)
+    sec = e0.elapsed_time(e1) / 1e3
+    prof = v.profile_report()
+    launches = sum(n for n, _ in prof.values())
+    result = out.cpu()
+    eng.free()
+    return sec, prof, launches, result
+
+
+def run_e2e(v, kind, ref, dst, steps, warmup, nthreads):
+    """Through the reference-facing C ABI from pinned host memory, one handler per thread."""
+    import ctypes
+    import numpy as np
+    import torch
+    npairs, _, h, w = ref.shape
+    href = ref.cpu().pin_memory()
+    hdst = dst.cpu().pin_memory()
+    L = v.lib()
+    plane_ptrs = []
+    for t in range(npairs):
+        a = (ctypes.c_void_p * 3)(*[href[t, c].data_ptr() for c in range(3)])
+        b = (ctypes.c_void_p * 3)(*[hdst[t, c].data_ptr() for c in range(3)])
+        plane_ptrs.append((a, b))
+    stride = w * 4
+    handlers = []
+    for _ in range(nthreads):
+        hd = v.Handler()
+        if kind == "ssimu2":
+            rc = L.Vship_SSIMU2Init(ctypes.byref(hd), w, h)
+        else:
+            rc = L.Vship_ButteraugliInitv2(ctypes.byref(hd), w, h, 2, ctypes.c_float(203.0))
+        if rc:
+            raise v.VshipError(rc, "init")
+        handlers.append(hd)
+    scores = [None] * npairs
+    errors = []
+
+    def worker(k):
+        hd = handlers[k]
+        sc = ctypes.c_double()
+        norms = (ctypes.c_double * 3)()
+        for i in range(k, npairs, nthreads):
+            a, b = plane_ptrs[i]
+            if kind == "ssimu2":
+                rc = L.Vship_ComputeSSIMU2Float(hd, ctypes.byref(sc), ctypes.cast(a, v._PP), ctypes.cast(b, v._PP),
+                                                stride)
+                scores[i] = sc.value
+            else:
+                rc = L.Vship_ComputeButteraugliFloatv3(hd, norms, None, 0, ctypes.cast(a, v._PP),
+                                                       ctypes.cast(b, v._PP), stride, stride)
+                scores[i] = norms[0]
+            if rc:
+                errors.append(rc)
+
+    def step():
+        th = [threading.Thread(target=worker, args=(k,)) for k in range(nthreads)]
+        [t.start() for t in th]
+        [t.join() for t in th]
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    for hd in handlers:
+        if kind == "ssimu2":
+            L.Vship_SSIMU2Free(hd)
+        else:
+            L.Vship_ButteraugliFree(hd)
+    if errors:
+        raise v.VshipError(errors[0], "e2e compute")
+    h2d = npairs * 2 * 3 * w * h * 4
+    d2h = npairs * (8 if kind == "ssimu2" else 24)
+    return sec, h2d, d2h, np.array(scores)
+
+
+def cpu_baseline(kind, ref, dst, sample_pairs, nthreads):
+    """The reference's math (FP32 restatement in oracle/) on the host cores for a bounded sample."""
+    import numpy as np
+    import oracle
+    t_total = 0.0
+    for t in range(sample_pairs):
+        a = [np.ascontiguousarray(ref[t, c].cpu().numpy()) for c in range(3)]
+        b = [np.ascontiguousarray(dst[t, c].cpu().numpy()) for c in range(3)]
+        t0 = time.perf_counter()
+        if kind == "ssimu2":
+            oracle.ssimu2(a, b, precision=32, nthreads=nthreads)
+        else:
+            oracle.butteraugli(a, b, precision=32, nthreads=nthreads)
+        t_total += time.perf_counter() - t0
+    return sample_pairs / t_total, t_total
+
+
+def bench_workload(v, kind, args, ws, rank):
+    import torch
+    npairs = args.pairs if kind == "ssimu2" else args.butter_pairs
+    chunk = args.chunk if kind == "ssimu2" else args.butter_chunk
+    ref, dst = make_inputs(kind, npairs, "cuda")
+    torch.cuda.synchronize()
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    sec, prof, launches, dev_scores = run_device(v, kind, ref, dst, args.steps, args.warmup, ws, chunk)
+    clocks = sampler.stop()
+    sec = max_over_ranks(sec, ws)
+    value = npairs * ws * args.steps / sec
+    e2e_sec, h2d, d2h, host_scores = run_e2e(v, kind, ref, dst, args.e2e_steps, 1, args.e2e_threads)
+    e2e_sec = max_over_ranks(e2e_sec, ws)
+    e2e_value = npairs * ws * args.e2e_steps / e2e_sec
+    w, h = (W1080, H1080) if kind == "ssimu2" else (W4K, H4K)
+    kname = "ssimu2_stats" if kind == "ssimu2" else "butter_diff"
+    per_pair = ssimu2_stats_bytes(w, h) if kind == "ssimu2" else butter_diff_bytes(w, h)
+    peak, peak_kind = measured_peaks()
+    n_launch, tot_ms = prof.get(kname, (0, 0.0))
+    # algorithmic bytes moved by this kernel over the timed region / its summed launch time
+    # (for Butteraugli the per-pair figure covers both scales, i.e. two launches per batch)
+    total_alg = per_pair * npairs * args.steps
+    alg = total_alg / max(n_launch, 1)
+    avg_s = (tot_ms / 1e3) / max(n_launch, 1)
+    achieved = total_alg / (tot_ms / 1e3) / 1e9 if tot_ms > 0 else 0.0
+    pairs_per_launch = npairs * args.steps / max(n_launch, 1)
+    traffic = ncu_traffic(kname)
+    total_kernel_ms = sum(t for _, t in prof.values())
+    res = {
+        "value": value, "unit": "frame-pairs/s", "ms_per_step": sec / args.steps * 1e3,
+        "pairs_per_step": npairs,
+        "e2e": {"value": e2e_value, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "threads": args.e2e_threads, "steps": args.e2e_steps},
+        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": traffic * pairs_per_launch if traffic is not None else None,
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_s * 1e3},
+        "pipeline_bytes_per_pair": ssimu2_pair_bytes(w, h) if kind == "ssimu2" else butter_pair_bytes(w, h),
+        "kernel_share": {k: round(t / total_kernel_ms, 4) for k, t in sorted(prof.items(), key=lambda x: -x[1][1])}
+        if total_kernel_ms > 0 else {},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "score_check": {"device_vs_e2e_max_abs": float(abs(
+            (dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy()[0::3]) - host_scores).max())},
+    }
+    if rank == 0 and args.cpu_sample > 0:
+        cv, csec = cpu_baseline(kind, ref, dst, args.cpu_sample if kind == "ssimu2" else max(1, args.cpu_sample // 4),
+                                os.cpu_count() or 1)
+        res["cpu_baseline"] = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"{args.cpu_sample if kind == 'ssimu2' else max(1, args.cpu_sample // 4)} "
+                                         f"pairs of the same workload ({csec:.1f} s)"}
+    del ref, dst
+    torch.cuda.empty_cache()
+    return res
+
+
+def main_ours(args):
+    import torch
+    ws, rank, local = dist_setup(args)
+    import vship_gb300 as v
+    if not os.path.exists(v.LIB_PATH):
+        from vship_gb300 import build
+        build.build()
+    v.lib()
+    s2 = bench_workload(v, "ssimu2", args, ws, rank)
+    out = {
+        "metric": "frame-pairs/s (1080p SSIMU2)", "value": s2["value"], "unit": "frame-pairs/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": s2["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ssimu2_1080p: {args.pairs} pairs 1920x1080 YUV420P10 -> float32 RGB planes, "
+                               "8x8 block-DCT distortion", "pairs_per_step": args.pairs,
+                   "parallelism": f"replicas x{ws}", "l2": "inputs 12 GB > L2, no flush",
+                   "launch_chunk_pairs": args.chunk},
+        "e2e": s2["e2e"], "roofline": s2["roofline"], "gpu_launches": s2["gpu_launches"], "clocks": s2["clocks"],
+        "kernel_share": s2["kernel_share"], "pipeline_bytes_per_pair": s2["pipeline_bytes_per_pair"],
+        "score_check": s2["score_check"],
+    }
+    if "cpu_baseline" in s2:
+        out["cpu_baseline"] = s2["cpu_baseline"]
+    if not args.skip_butter:
+        b = bench_workload(v, "butter", args, ws, rank)
+        out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e",
+                                                   "roofline", "gpu_launches", "clocks", "kernel_share",
+                                                   "pipeline_bytes_per_pair", "score_check")
+                                 if k in b}
+        if "cpu_baseline" in b:
+            out["butteraugli_4k"]["cpu_baseline"] = b["cpu_baseline"]
+        out["gpu_launches"] += b["gpu_launches"]
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main_reference(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import torch
+    import numpy as np
+    import oracle
+    from vship_gb300 import synth
+    oracle.lib()
+    nt = os.cpu_count() or 1
+    # each step: one 1080p pair of the same workload through the reference's math on all cores
+    frames = []
+    for t in range(args.warmup + args.steps):
+        r, d = synth.yuv420p10_frames(H1080, W1080, t, seed=7, distortion="dct", device="cpu")
+        a, b = synth.yuv420p10_to_rgb(r).numpy(), synth.yuv420p10_to_rgb(d).numpy()
+        frames.append(([np.ascontiguousarray(a[c]) for c in range(3)], [np.ascontiguousarray(b[c]) for c in range(3)]))
+    for t in range(args.warmup):
+        oracle.ssimu2(*frames[t], precision=32, nthreads=nt)
+    t0 = time.perf_counter()
+    for t in range(args.warmup, args.warmup + args.steps):
+        oracle.ssimu2(*frames[t], precision=32, nthreads=nt)
+    sec = time.perf_counter() - t0
+    value = args.steps / sec
+    out = {
+        "impl": "reference", "metric": "frame-pairs/s (1080p SSIMU2)", "value": value, "unit": "frame-pairs/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ssimu2_1080p: 1 pair per step of the 1920x1080 YUV420P10 block-DCT workload, "
+                               "float32 RGB planes", "pairs_per_step": 1},
+        "cpu_baseline": {"value": value, "unit": "frame-pairs/s", "cores": nt, "kind": "port",
+                         "sample": f"{args.steps} pairs, 1 per step"},
+        "e2e": {"value": value, "unit": "frame-pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference has no CPU implementation and its CUDA build cannot be built for this Arm host "
+                "from its sources here; this is its FP32 math restated in C++ (oracle/), threaded over all cores",
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--pairs", type=int, default=240)
+    ap.add_argument("--chunk", type=int, default=24)
+    ap.add_argument("--butter-pairs", type=int, default=60)
+    ap.add_argument("--butter-chunk", type=int, default=4)
+    ap.add_argument("--e2e-threads", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=4)
+    ap.add_argument("--skip-butter", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        main_reference(args)
+    else:
+        main_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,234 @@
+/* VshipAPI.h -- C ABI of vship_gb300, a GB300 (sm_103a) implementation of Vship's per-frame-pair
+ * SSIMULACRA2 and Butteraugli scoring.
+ *
+ * The first block declares exactly the entry points, types and enum values of the reference's
+ * src/VshipAPI.h (cited per declaration), so a program or FFI binding written against Vship links
+ * against libvship.so unchanged. The second block holds extensions that have no counterpart in
+ * the reference; each says why it exists.
+ *
+ * Threading contract (same as the reference, src/VshipLib.cpp:192-205): handler tables are
+ * thread-safe; a compute call is synchronous (it returns after its result is on the host);
+ * different handlers may be used concurrently from different threads. Unlike the reference, two
+ * threads that share one handler are serialised instead of racing.
+ */
+#ifndef VSHIP_API_HEADER
+#define VSHIP_API_HEADER
+
+#include <stdint.h>
+
+#if defined(_WIN32)
+#if defined(EXPORTVSHIPLIB)
+#define EXPORTPREPROCESS __declspec(dllexport)
+#else
+#define EXPORTPREPROCESS __declspec(dllimport)
+#endif
+#else
+#define EXPORTPREPROCESS __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------------------
+ * Reference-compatible surface (src/VshipAPI.h of Vship 3.1.0)
+ * ------------------------------------------------------------------------------------------- */
+
+/* src/VshipAPI.h:20-23 */
+typedef enum {
+    Vship_HIP = 0,
+    Vship_Cuda = 1,
+} Vship_Backend;
+
+/* src/VshipAPI.h:25-30 */
+typedef struct {
+    int major;
+    int minor;
+    int minorMinor;
+    Vship_Backend backend;
+} Vship_Version;
+
+/* src/VshipAPI.h:32 -- reports 3.1.0, backend Vship_Cuda */
+EXPORTPREPROCESS Vship_Version Vship_GetVersion(void);
+
+/* src/VshipAPI.h:35-58 -- values 0..11 are ABI */
+typedef enum {
+    Vship_NoError = 0,
+    Vship_OutOfVRAM,
+    Vship_OutOfRAM,
+    Vship_DifferingInputType,
+    Vship_NonRGBSInput,
+    Vship_DeviceCountError,
+    Vship_NoDeviceDetected,
+    Vship_BadDeviceArgument,
+    Vship_BadDeviceCode,
+    Vship_BadHandler,
+    Vship_BadPointer,
+    Vship_BadErrorType,
+} Vship_Exception;
+
+/* src/VshipAPI.h:61 */
+EXPORTPREPROCESS Vship_Exception Vship_GetDeviceCount(int* number);
+
+/* src/VshipAPI.h:64 */
+EXPORTPREPROCESS Vship_Exception Vship_SetDevice(int gpu_id);
+
+/* src/VshipAPI.h:67-73 */
+typedef struct {
+    char name[256];
+    uint64_t VRAMSize;
+    int integrated;
+    int MultiProcessorCount;
+    int WarpSize;
+} Vship_DeviceInfo;
+
+/* src/VshipAPI.h:75 */
+EXPORTPREPROCESS Vship_Exception Vship_GetDeviceInfo(Vship_DeviceInfo* device_info, int gpu_id);
+
+/* src/VshipAPI.h:78 -- device count, id range, set device, and a one-thread probe kernel */
+EXPORTPREPROCESS Vship_Exception Vship_GPUFullCheck(int gpu_id);
+
+/* src/VshipAPI.h:82 -- returns the size needed including the terminating NUL; len == 0 only
+ * queries; otherwise copies at most len-1 characters and always NUL-terminates. */
+EXPORTPREPROCESS int Vship_GetErrorMessage(Vship_Exception exception, char* out_message, int len);
+
+/* src/VshipAPI.h:87-89 */
+typedef struct {
+    int id;
+} Vship_SSIMU2Handler;
+
+/* src/VshipAPI.h:91-93 -- page-locked host memory; inputs placed there upload at full speed */
+EXPORTPREPROCESS Vship_Exception Vship_PinnedMalloc(void** ptr, uint64_t size);
+EXPORTPREPROCESS Vship_Exception Vship_PinnedFree(void* ptr);
+
+/* src/VshipAPI.h:96,99 */
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2Init(Vship_SSIMU2Handler* handler, int width, int height);
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2Free(Vship_SSIMU2Handler handler);
+
+/* src/VshipAPI.h:103-111. Inputs: three planar R,G,B planes, BT.709 transfer (gamma-encoded),
+ * full range; float32 or uint16 (0..65535) samples; `stride` is the row pitch in bytes of the
+ * reference frame (and of the distorted one unless the v2 form gives stride2). Frames are not
+ * modified. */
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2Float(Vship_SSIMU2Handler handler, double* score,
+                                                          const uint8_t* srcp1[3], const uint8_t* srcp2[3],
+                                                          int64_t stride);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2Floatv2(Vship_SSIMU2Handler handler, double* score,
+                                                            const uint8_t* srcp1[3], const uint8_t* srcp2[3],
+                                                            int64_t stride, int64_t stride2);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2Uint16(Vship_SSIMU2Handler handler, double* score,
+                                                           const uint8_t* srcp1[3], const uint8_t* srcp2[3],
+                                                           int64_t stride);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2Uint16v2(Vship_SSIMU2Handler handler, double* score,
+                                                             const uint8_t* srcp1[3], const uint8_t* srcp2[3],
+                                                             int64_t stride, int64_t stride2);
+
+/* src/VshipAPI.h:113-115 */
+typedef struct {
+    int id;
+} Vship_ButteraugliHandler;
+
+/* src/VshipAPI.h:117-121. The reference stores its float norms into these int fields (the
+ * value is truncated toward zero); the layout is kept for ABI compatibility. Use the v3 compute
+ * functions below for the exact values. */
+typedef struct {
+    int norm2;
+    int norm3;
+    int norminf;
+} Vship_ButteraugliScore;
+
+/* src/VshipAPI.h:124,127,130 -- Init uses Qnorm = 2 */
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliInit(Vship_ButteraugliHandler* handler, int width, int height,
+                                                       float intensity_multiplier);
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliInitv2(Vship_ButteraugliHandler* handler, int width, int height,
+                                                         int Qnorm, float intensity_multiplier);
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliFree(Vship_ButteraugliHandler handler);
+
+/* src/VshipAPI.h:137-148. dstp is NULL (no distortion map) or points to dststride*height bytes
+ * that receive the float32 distortion map. */
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliFloat(Vship_ButteraugliHandler handler,
+                                                               Vship_ButteraugliScore* score, const uint8_t* dstp,
+                                                               int64_t dststride, const uint8_t* srcp1[3],
+                                                               const uint8_t* srcp2[3], int64_t stride);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliFloatv2(Vship_ButteraugliHandler handler,
+                                                                 Vship_ButteraugliScore* score, const uint8_t* dstp,
+                                                                 int64_t dststride, const uint8_t* srcp1[3],
+                                                                 const uint8_t* srcp2[3], int64_t stride,
+                                                                 int64_t stride2);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliUint16(Vship_ButteraugliHandler handler,
+                                                                Vship_ButteraugliScore* score, const uint8_t* dstp,
+                                                                int64_t dststride, const uint8_t* srcp1[3],
+                                                                const uint8_t* srcp2[3], int64_t stride);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliUint16v2(Vship_ButteraugliHandler handler,
+                                                                  Vship_ButteraugliScore* score, const uint8_t* dstp,
+                                                                  int64_t dststride, const uint8_t* srcp1[3],
+                                                                  const uint8_t* srcp2[3], int64_t stride,
+                                                                  int64_t stride2);
+
+/* ---------------------------------------------------------------------------------------------
+ * Extensions (no counterpart in the reference)
+ * ------------------------------------------------------------------------------------------- */
+
+/* Exact Butteraugli norms {Qnorm, 3-norm, inf-norm} as doubles: the reference's score struct
+ * truncates them to int. Same arguments as the v2 compute functions otherwise. */
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliFloatv3(Vship_ButteraugliHandler handler, double norms[3],
+                                                                 const uint8_t* dstp, int64_t dststride,
+                                                                 const uint8_t* srcp1[3], const uint8_t* srcp2[3],
+                                                                 int64_t stride, int64_t stride2);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliUint16v3(Vship_ButteraugliHandler handler, double norms[3],
+                                                                  const uint8_t* dstp, int64_t dststride,
+                                                                  const uint8_t* srcp1[3], const uint8_t* srcp2[3],
+                                                                  int64_t stride, int64_t stride2);
+
+/* Sample formats of the device-resident entry points (numbered as the reference's InputMemType,
+ * src/util/preprocessor.hpp:94). */
+typedef enum {
+    Vship_InUint8 = 0,
+    Vship_InUint16 = 1,
+    Vship_InHalf = 2,
+    Vship_InFloat = 3,
+} Vship_InputType;
+
+/* One frame resident in device memory: three planes (R, G, B) and the row pitch in bytes. */
+typedef struct {
+    const uint8_t* plane[3];
+    int64_t stride;
+} Vship_DeviceFrame;
+
+/* Batched, device-resident SSIMU2 for callers whose frames already live in GPU memory (decoders,
+ * encoders' candidate buffers): one launch scores up to max_pairs pairs of one resolution.
+ * `frames` is a DEVICE array of 2*npairs frames (pair-major: reference, distorted); scores_dev
+ * receives npairs doubles in device memory; `stream` is a cudaStream_t (NULL = legacy default).
+ * The call only enqueues work; synchronise the stream before reading scores_dev. */
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2BatchInit(Vship_SSIMU2Handler* handler, int width, int height,
+                                                       int max_pairs);
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2ComputeDeviceAsync(Vship_SSIMU2Handler handler,
+                                                                const Vship_DeviceFrame* frames, int npairs,
+                                                                Vship_InputType input_type, double* scores_dev,
+                                                                void* stream);
+
+/* Batched, device-resident Butteraugli (same conventions as the SSIMU2 pair above). norms_dev
+ * receives 3 doubles per pair {Qnorm, 3-norm, inf-norm}; distmaps_dev is NULL or a device
+ * buffer of npairs * width * height floats (dense rows) that receives the distortion maps. */
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliBatchInit(Vship_ButteraugliHandler* handler, int width,
+                                                            int height, int Qnorm, float intensity_multiplier,
+                                                            int max_pairs);
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliComputeDeviceAsync(Vship_ButteraugliHandler handler,
+                                                                     const Vship_DeviceFrame* frames, int npairs,
+                                                                     Vship_InputType input_type, double* norms_dev,
+                                                                     float* distmaps_dev, void* stream);
+EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytes(int width, int height, int max_pairs);
+
+/* Instrumentation: when enabled, every kernel launch is bracketed by CUDA events on its stream.
+ * Vship_ProfileReport synchronises those events and writes a JSON object
+ * {"kernel": [launches, total_ms], ...} (same size/truncation contract as
+ * Vship_GetErrorMessage), then clears the records. Off by default. */
+EXPORTPREPROCESS void Vship_ProfileSetEnabled(int enabled);
+EXPORTPREPROCESS int Vship_ProfileReport(char* out_json, int len);
+
+/* Bytes of device memory one handler holds for a given resolution and batch size. */
+EXPORTPREPROCESS uint64_t Vship_SSIMU2DeviceBytes(int width, int height, int max_pairs);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+#endif /* VSHIP_API_HEADER */

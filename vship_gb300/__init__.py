@@ -1,0 +1,353 @@
+"""vship_gb300: GB300-native SSIMULACRA2 and Butteraugli scoring behind Vship's C ABI.
+
+The product is ``libvship.so`` (hand-written sm_103a CUDA kernels plus the C ABI declared in
+``include/VshipAPI.h``). This module binds it with ctypes and mirrors the reference's interfaces
+for Python callers: handler objects with the semantics of ``Vship_SSIMU2Init`` /
+``Vship_ComputeSSIMU2*`` / ``Vship_ButteraugliInit*`` (src/VshipAPI.h) and, in ``vship_gb300.vs``,
+the ``vship.SSIMULACRA2`` / ``vship.BUTTERAUGLI`` clip functions (src/VshipLib.cpp:58-64).
+
+There is no CPU fallback: if the shared library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libvship.so")
+
+# Vship_Exception (src/VshipAPI.h:35-58)
+NoError, OutOfVRAM, OutOfRAM, DifferingInputType, NonRGBSInput, DeviceCountError, NoDeviceDetected, \
+    BadDeviceArgument, BadDeviceCode, BadHandler, BadPointer, BadErrorType = range(12)
+EXCEPTION_NAMES = ["NoError", "OutOfVRAM", "OutOfRAM", "DifferingInputType", "NonRGBSInput", "DeviceCountError",
+                   "NoDeviceDetected", "BadDeviceArgument", "BadDeviceCode", "BadHandler", "BadPointer",
+                   "BadErrorType"]
+
+# Vship_InputType
+IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT = 0, 1, 2, 3
+
+
+class VshipError(RuntimeError):
+    def __init__(self, code: int, where: str = ""):
+        self.code = int(code)
+        self.name = EXCEPTION_NAMES[self.code] if 0 <= self.code < len(EXCEPTION_NAMES) else "BadErrorType"
+        super().__init__(f"{where}: {error_message(self.code)}" if where else error_message(self.code))
+
+
+class Version(ctypes.Structure):
+    _fields_ = [("major", ctypes.c_int), ("minor", ctypes.c_int), ("minorMinor", ctypes.c_int),
+                ("backend", ctypes.c_int)]
+
+
+class DeviceInfo(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 256), ("VRAMSize", ctypes.c_uint64), ("integrated", ctypes.c_int),
+                ("MultiProcessorCount", ctypes.c_int), ("WarpSize", ctypes.c_int)]
+
+
+class Handler(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int)]
+
+
+class ButteraugliScore(ctypes.Structure):
+    _fields_ = [("norm2", ctypes.c_int), ("norm3", ctypes.c_int), ("norminf", ctypes.c_int)]
+
+
+class DeviceFrame(ctypes.Structure):
+    _fields_ = [("plane", ctypes.c_void_p * 3), ("stride", ctypes.c_int64)]
+
+
+# Every exported entry point: name -> (restype, argtypes). The tests check this list against
+# include/VshipAPI.h and against the library's dynamic symbol table.
+_PP = ctypes.POINTER(ctypes.c_void_p)
+_H = Handler
+_E = ctypes.c_int
+SIGNATURES = {
+    "Vship_GetVersion": (Version, []),
+    "Vship_GetDeviceCount": (_E, [ctypes.POINTER(ctypes.c_int)]),
+    "Vship_SetDevice": (_E, [ctypes.c_int]),
+    "Vship_GetDeviceInfo": (_E, [ctypes.POINTER(DeviceInfo), ctypes.c_int]),
+    "Vship_GPUFullCheck": (_E, [ctypes.c_int]),
+    "Vship_GetErrorMessage": (ctypes.c_int, [ctypes.c_int, ctypes.c_char_p, ctypes.c_int]),
+    "Vship_PinnedMalloc": (_E, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_uint64]),
+    "Vship_PinnedFree": (_E, [ctypes.c_void_p]),
+    "Vship_SSIMU2Init": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int]),
+    "Vship_SSIMU2Free": (_E, [_H]),
+    "Vship_ComputeSSIMU2Float": (_E, [_H, ctypes.POINTER(ctypes.c_double), _PP, _PP, ctypes.c_int64]),
+    "Vship_ComputeSSIMU2Floatv2": (_E, [_H, ctypes.POINTER(ctypes.c_double), _PP, _PP, ctypes.c_int64,
+                                        ctypes.c_int64]),
+    "Vship_ComputeSSIMU2Uint16": (_E, [_H, ctypes.POINTER(ctypes.c_double), _PP, _PP, ctypes.c_int64]),
+    "Vship_ComputeSSIMU2Uint16v2": (_E, [_H, ctypes.POINTER(ctypes.c_double), _PP, _PP, ctypes.c_int64,
+                                         ctypes.c_int64]),
+    "Vship_ButteraugliInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "Vship_ButteraugliInitv2": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "Vship_ButteraugliFree": (_E, [_H]),
+    "Vship_ComputeButteraugliFloat": (_E, [_H, ctypes.POINTER(ButteraugliScore), ctypes.c_void_p, ctypes.c_int64,
+                                           _PP, _PP, ctypes.c_int64]),
+    "Vship_ComputeButteraugliFloatv2": (_E, [_H, ctypes.POINTER(ButteraugliScore), ctypes.c_void_p,
+                                             ctypes.c_int64, _PP, _PP, ctypes.c_int64, ctypes.c_int64]),
+    "Vship_ComputeButteraugliUint16": (_E, [_H, ctypes.POINTER(ButteraugliScore), ctypes.c_void_p, ctypes.c_int64,
+                                            _PP, _PP, ctypes.c_int64]),
+    "Vship_ComputeButteraugliUint16v2": (_E, [_H, ctypes.POINTER(ButteraugliScore), ctypes.c_void_p,
+                                              ctypes.c_int64, _PP, _PP, ctypes.c_int64, ctypes.c_int64]),
+    "Vship_ComputeButteraugliFloatv3": (_E, [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int64,
+                                             _PP, _PP, ctypes.c_int64, ctypes.c_int64]),
+    "Vship_ComputeButteraugliUint16v3": (_E, [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                                              ctypes.c_int64, _PP, _PP, ctypes.c_int64, ctypes.c_int64]),
+    "Vship_SSIMU2BatchInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_SSIMU2ComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_void_p]),
+    "Vship_SSIMU2DeviceBytes": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_ButteraugliBatchInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                        ctypes.c_int]),
+    "Vship_ButteraugliComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                                 ctypes.c_void_p, ctypes.c_void_p]),
+    "Vship_ButteraugliDeviceBytes": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_ProfileSetEnabled": (None, [ctypes.c_int]),
+    "Vship_ProfileReport": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libvship.so (built by ``vship_gb300.build``). Raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run `python -m vship_gb300.build` (needs nvcc)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def error_message(code: int) -> str:
+    L = lib()
+    n = L.Vship_GetErrorMessage(int(code), None, 0)
+    buf = ctypes.create_string_buffer(n)
+    L.Vship_GetErrorMessage(int(code), buf, n)
+    return buf.value.decode()
+
+
+def _check(rc: int, where: str):
+    if rc != NoError:
+        raise VshipError(rc, where)
+
+
+def profile_enable(on: bool = True) -> None:
+    """Bracket every kernel launch with CUDA events (see Vship_ProfileSetEnabled)."""
+    lib().Vship_ProfileSetEnabled(1 if on else 0)
+
+
+def profile_report() -> dict:
+    """{kernel: (launches, total_ms)} since the last report; synchronises the recorded events."""
+    import json
+    L = lib()
+    n = L.Vship_ProfileReport(None, 0)
+    buf = ctypes.create_string_buffer(n + 4096)
+    L.Vship_ProfileReport(buf, len(buf))
+    return {k: (int(v[0]), float(v[1])) for k, v in json.loads(buf.value.decode() or "{}").items()}
+
+
+def version():
+    v = lib().Vship_GetVersion()
+    return (v.major, v.minor, v.minorMinor, "Cuda" if v.backend == 1 else "HIP")
+
+
+def device_count() -> int:
+    n = ctypes.c_int()
+    _check(lib().Vship_GetDeviceCount(ctypes.byref(n)), "Vship_GetDeviceCount")
+    return n.value
+
+
+def device_info(gpu_id: int = 0) -> dict:
+    d = DeviceInfo()
+    _check(lib().Vship_GetDeviceInfo(ctypes.byref(d), gpu_id), "Vship_GetDeviceInfo")
+    return {"name": d.name.decode(errors="replace"), "VRAMSize": d.VRAMSize, "integrated": d.integrated,
+            "MultiProcessorCount": d.MultiProcessorCount, "WarpSize": d.WarpSize}
+
+
+def gpu_full_check(gpu_id: int = 0) -> None:
+    _check(lib().Vship_GPUFullCheck(gpu_id), "Vship_GPUFullCheck")
+
+
+def set_device(gpu_id: int) -> None:
+    _check(lib().Vship_SetDevice(gpu_id), "Vship_SetDevice")
+
+
+# ------------------------------------------------------------------------------------------
+# host planes
+
+def planes_of(frame):
+    """Accept a (3, H, W) array or a sequence of three (H, W) arrays (float32 or uint16, rows
+    contiguous, one shared row stride). Returns (ctypes pointer array, stride, w, h, dtype, keep)."""
+    planes = [np.asarray(p) for p in frame]
+    if len(planes) != 3:
+        raise ValueError("a frame has three planes (R, G, B)")
+    dt = planes[0].dtype
+    if dt not in (np.float32, np.uint16):
+        raise TypeError("planes must be float32 or uint16")
+    h, w = planes[0].shape
+    strides = {p.strides[0] for p in planes}
+    for p in planes:
+        if p.dtype != dt or p.shape != (h, w) or p.strides[1] != dt.itemsize:
+            raise ValueError("planes must share dtype and shape, with contiguous rows")
+    if len(strides) != 1:
+        raise ValueError("the three planes must share one row stride")
+    arr = (ctypes.c_void_p * 3)(*[p.ctypes.data for p in planes])
+    return arr, strides.pop(), w, h, dt, planes
+
+
+class SSIMU2Handler:
+    """One SSIMULACRA2 scorer for a fixed resolution (Vship_SSIMU2Init / Compute / Free)."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = int(width), int(height)
+        self._h = Handler()
+        _check(lib().Vship_SSIMU2Init(ctypes.byref(self._h), self.width, self.height), "Vship_SSIMU2Init")
+
+    def compute(self, reference, distorted) -> float:
+        a1, s1, w, h, dt, k1 = planes_of(reference)
+        a2, s2, w2, h2, dt2, k2 = planes_of(distorted)
+        if (w, h) != (self.width, self.height) or (w2, h2) != (w, h) or dt != dt2:
+            raise VshipError(DifferingInputType, "SSIMU2Handler.compute")
+        out = ctypes.c_double()
+        f = lib().Vship_ComputeSSIMU2Floatv2 if dt == np.float32 else lib().Vship_ComputeSSIMU2Uint16v2
+        _check(f(self._h, ctypes.byref(out), ctypes.cast(a1, _PP), ctypes.cast(a2, _PP), s1, s2),
+               "Vship_ComputeSSIMU2")
+        return out.value
+
+    def free(self):
+        if self._h is not None:
+            _check(lib().Vship_SSIMU2Free(self._h), "Vship_SSIMU2Free")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class ButteraugliHandler:
+    """One Butteraugli scorer (Vship_ButteraugliInitv2 / Compute*v3 / Free)."""
+
+    def __init__(self, width: int, height: int, qnorm: int = 2, intensity_multiplier: float = 203.0):
+        self.width, self.height = int(width), int(height)
+        self.qnorm, self.intensity = int(qnorm), float(intensity_multiplier)
+        self._h = Handler()
+        _check(lib().Vship_ButteraugliInitv2(ctypes.byref(self._h), self.width, self.height, self.qnorm,
+                                             ctypes.c_float(self.intensity)), "Vship_ButteraugliInitv2")
+
+    def compute(self, reference, distorted, distmap: bool = False):
+        """Returns (norm_q, norm_3, norm_inf) and, with distmap=True, the float32 (H, W) map."""
+        a1, s1, w, h, dt, k1 = planes_of(reference)
+        a2, s2, w2, h2, dt2, k2 = planes_of(distorted)
+        if (w, h) != (self.width, self.height) or (w2, h2) != (w, h) or dt != dt2:
+            raise VshipError(DifferingInputType, "ButteraugliHandler.compute")
+        norms = (ctypes.c_double * 3)()
+        dm = np.empty((h, w), np.float32) if distmap else None
+        f = lib().Vship_ComputeButteraugliFloatv3 if dt == np.float32 else lib().Vship_ComputeButteraugliUint16v3
+        _check(f(self._h, norms, dm.ctypes.data if dm is not None else None, w * 4,
+                 ctypes.cast(a1, _PP), ctypes.cast(a2, _PP), s1, s2), "Vship_ComputeButteraugli")
+        res = (norms[0], norms[1], norms[2])
+        return (res, dm) if distmap else res
+
+    def free(self):
+        if self._h is not None:
+            _check(lib().Vship_ButteraugliFree(self._h), "Vship_ButteraugliFree")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.free()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class SSIMU2Batch:
+    """Batched device-resident SSIMU2 (Vship_SSIMU2BatchInit / Vship_SSIMU2ComputeDeviceAsync)."""
+
+    def __init__(self, width: int, height: int, max_pairs: int):
+        self.width, self.height, self.max_pairs = int(width), int(height), int(max_pairs)
+        self._h = Handler()
+        _check(lib().Vship_SSIMU2BatchInit(ctypes.byref(self._h), self.width, self.height, self.max_pairs),
+               "Vship_SSIMU2BatchInit")
+
+    def compute_async(self, frames_dev_ptr: int, npairs: int, input_type: int, scores_dev_ptr: int,
+                      stream_ptr: int = 0) -> None:
+        _check(lib().Vship_SSIMU2ComputeDeviceAsync(self._h, ctypes.c_void_p(frames_dev_ptr), int(npairs),
+                                                    int(input_type), ctypes.c_void_p(scores_dev_ptr),
+                                                    ctypes.c_void_p(stream_ptr)), "Vship_SSIMU2ComputeDeviceAsync")
+
+    def free(self):
+        if self._h is not None:
+            _check(lib().Vship_SSIMU2Free(self._h), "Vship_SSIMU2Free")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class ButteraugliBatch:
+    """Batched device-resident Butteraugli (Vship_ButteraugliBatchInit / ComputeDeviceAsync)."""
+
+    def __init__(self, width: int, height: int, max_pairs: int, qnorm: int = 2, intensity_multiplier: float = 203.0):
+        self.width, self.height, self.max_pairs = int(width), int(height), int(max_pairs)
+        self._h = Handler()
+        _check(lib().Vship_ButteraugliBatchInit(ctypes.byref(self._h), self.width, self.height, int(qnorm),
+                                                ctypes.c_float(intensity_multiplier), self.max_pairs),
+               "Vship_ButteraugliBatchInit")
+
+    def compute_async(self, frames_dev_ptr: int, npairs: int, input_type: int, norms_dev_ptr: int,
+                      distmaps_dev_ptr: int = 0, stream_ptr: int = 0) -> None:
+        _check(lib().Vship_ButteraugliComputeDeviceAsync(self._h, ctypes.c_void_p(frames_dev_ptr), int(npairs),
+                                                         int(input_type), ctypes.c_void_p(norms_dev_ptr),
+                                                         ctypes.c_void_p(distmaps_dev_ptr or None),
+                                                         ctypes.c_void_p(stream_ptr)),
+               "Vship_ButteraugliComputeDeviceAsync")
+
+    def free(self):
+        if self._h is not None:
+            _check(lib().Vship_ButteraugliFree(self._h), "Vship_ButteraugliFree")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def device_frames_table(frames, device="cuda"):
+    """Pack [(planes, stride_bytes), ...] of device pointers into a device array of
+    Vship_DeviceFrame (32 bytes each) held in a torch uint8 tensor."""
+    import torch
+
+    arr = (DeviceFrame * len(frames))()
+    for i, (planes, stride) in enumerate(frames):
+        for c in range(3):
+            arr[i].plane[c] = int(planes[c])
+        arr[i].stride = int(stride)
+    host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
+    return host.to(device)

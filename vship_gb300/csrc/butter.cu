@@ -1,0 +1,1020 @@
+// butter.cu -- Butteraugli scoring on sm_103a.
+//
+// Launch sequence for a batch of frame pairs (reference file:line per step):
+//   decode      : strided input -> linear RGB at full and half resolution
+//                 (butter/Planed.hpp:3-34, colors.hpp:7-23, downupsample.hpp:3-20, main.hpp:116-128)
+//   then for the half scale and the full scale:
+//   opsin       : 17-tap blur (sigma 1.2) of each channel in a 32x48 smem tile + opsin dynamics
+//                 (colors.hpp:25-91)
+//   lf_h, lf_v  : separable 43-tap blur (sigma 7.156); the vertical pass also forms D = XYB - LF
+//                 and the LF "vals" (separatefrequencies.hpp:3-12,160-203)
+//   mf_h, mf_v  : separable 19-tap blur (sigma 3.225) of D; the vertical pass forms MF with its
+//                 range operators and HF_pre = D - MF with X suppressed by Y (:37-99)
+//   hf          : 17-tap tile blur (sigma 1.564) of HF_pre -> HF and UHF (:117-140,189-200)
+//   diff        : the six Malta maps from a register window over a smem tile of the asymmetric
+//                 diffs, the L2 / L2-asymmetric terms and the mask precompute
+//                 (maltaDiff.hpp, simplerdiff.hpp, maskPsycho.hpp:3-40, main.hpp:45-93)
+//   mask_blur   : 17-tap tile blur (sigma 2.7) of both mask planes, adds 10*(B0-B1)^2
+//                 (maskPsycho.hpp:113-135)
+//   diffmap     : fuzzy erosion, MaskY/MaskDcY combine (combineMasks.hpp); at full scale also
+//                 the 2x supersampled add of the half-scale map, the distortion-map store and the
+//                 per-CTA norm partials (downupsample.hpp:287-301, diffnorms.hpp)
+//   finalize    : FP64 p-norm / 3-norm / max combine (diffnorms.hpp:263-306)
+#include "common.cuh"
+#include "butter.h"
+#include "profile.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace vship {
+
+// ------------------------------------------------------------------------------------------
+// Gaussian tables (butter/gaussianblur.hpp:3-14,21-42), built on the host with the reference's
+// float arithmetic: index 0..4 = sigma {1.2, 1.56416327805, 2.7, 3.22489901262, 7.15593339443},
+// radius {8, 8, 8, 9, 21}.
+__constant__ float c_bk[5][43];
+__constant__ float c_bI[5][44];
+
+static int upload_butter_tables() {
+    static const double sig[5] = {1.2, 1.56416327805, 2.7, 3.22489901262, 7.15593339443};
+    float k[5][43] = {}, I[5][44] = {};
+    for (int t = 0; t < 5; t++) {
+        const double sigma = sig[t];
+        const int R = std::max((int)(sigma * 3), 8);
+        const int n = 2 * R + 1;
+        float acc = 0.f;
+        for (int i = 0; i <= n; i++) {
+            double q = (double)std::exp((float)(-(R - i) * (R - i) / (2 * sigma * sigma))) /
+                       std::sqrt(6.28318530718 * sigma * sigma);
+            if (i < n) k[t][i] = (float)q;
+            I[t][i] = acc;
+            acc = (float)((double)acc + q);
+        }
+    }
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bk, k, sizeof(k)));
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bI, I, sizeof(I)));
+    return E_OK;
+}
+
+template <int KI, int R>
+__device__ __forceinline__ float b_inv_mass(int pos, int extent) {
+    const int beg = max(0, pos - R) - (pos - R);
+    const int end = min(extent, pos + R + 1) - (pos - R);
+    return 1.0f / (c_bI[KI][end] - c_bI[KI][beg]);
+}
+
+// ------------------------------------------------------------------------------------------
+// Workspace layout. Per pair and per scale, NPLANES dense planes of pitch p:
+enum : int {
+    P_LIN = 0,    // 0..5   linear RGB (image*3 + c); dead after opsin
+    P_TMP = 0,    // 0..5   horizontal-pass output (reuses LIN)
+    P_SAC = 0,    // 0      sum of AC terms          } written by diff, after the last use of TMP
+    P_SDC = 1,    // 1      sum of DC terms          }
+    P_PRE0 = 2,   // 2      mask precompute, image 0 }
+    P_PRE1 = 3,   // 3      mask precompute, image 1 }
+    P_B0 = 4,     // 4      blurred mask, image 0
+    P_XYB = 6,    // 6..11  XYB, then D = XYB - LF, then HF_pre (X, Y) in place
+    P_LFV = 12,   // 12..17 LF vals
+    P_MF = 18,    // 18..23 MF
+    P_HF = 24,    // 24..27 HF (image*2 + c)
+    P_UHF = 28,   // 28..31 UHF
+    P_DIFF = 32,  // 32     diffmap of this scale
+    NPLANES = 33
+};
+
+struct BScaleDev {
+    int w, h, p;
+    int64_t n;     // p*h
+    int64_t base;  // offset inside the pair's workspace
+};
+struct BGeom {
+    BScaleDev s[2];  // 0 = full, 1 = half
+    int64_t pair_floats;
+    int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x8) at full scale
+};
+
+__device__ __forceinline__ float* bplane(float* work, const BGeom& g, const BScaleDev& S, int pair, int id) {
+    return work + (int64_t)pair * g.pair_floats + S.base + (int64_t)id * S.n;
+}
+// Select a scale with constant indices only, so the parameter struct is never copied to the
+// stack for a dynamic index.
+__device__ __forceinline__ BScaleDev pick_scale(const BGeom& g, int s) { return s == 0 ? g.s[0] : g.s[1]; }
+
+// ------------------------------------------------------------------------------------------
+// Kernel: decode + linearise at full resolution + 2x2 box to half resolution.
+// grid (ceil(w/32), ceil(h/32), 2*npairs), 256 threads.
+template <int IT>
+__global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __restrict__ frames,
+                                                            float* __restrict__ work, BGeom g) {
+    __shared__ float sm[3][32][33];
+    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const FrameDesc fd = frames[blockIdx.z];
+    const BScaleDev F = g.s[0], Hs = g.s[1];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+        const int ly = ty + 8 * r;
+        const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ly;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float v = 0.f;
+            if (gx < F.w && gy < F.h) {
+                v = to_linear(load_sample<IT>(fd.plane[c], fd.stride, gx, gy));
+                bplane(work, g, F, pair, P_LIN + img * 3 + c)[(int64_t)gy * F.p + gx] = v;
+            }
+            sm[c][ly][tx] = v;
+        }
+    }
+    __syncthreads();
+    const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
+    const int gx = blockIdx.x * 16 + lx, gy = blockIdx.y * 16 + ly;
+    if (gx < Hs.w && gy < Hs.h) {
+        const int x0 = 2 * lx, y0 = 2 * ly;
+        const int x1 = min(2 * gx + 1, F.w - 1) - (int)blockIdx.x * 32;
+        const int y1 = min(2 * gy + 1, F.h - 1) - (int)blockIdx.y * 32;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            float s = sm[c][y0][x0];
+            s += sm[c][y1][x0];
+            s += sm[c][y0][x1];
+            s += sm[c][y1][x1];
+            bplane(work, g, Hs, pair, P_LIN + img * 3 + c)[(int64_t)gy * Hs.p + gx] = s * 0.25f;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// 2-D tile blur, radius 8: 32x48 outputs per 256-thread CTA. `in` holds the 64x48 input tile
+// (8-px halo, zero outside the image) with pitch TB_IP; the horizontal pass writes 64x32 values
+// to `hb`; each thread returns the 6 vertical outputs of column (tid & 31), rows 6*(tid>>5)+o.
+constexpr int TB_TW = 32, TB_TH = 48, TB_R = 8;
+constexpr int TB_IW = TB_TW + 2 * TB_R, TB_IH = TB_TH + 2 * TB_R;
+constexpr int TB_IP = 49, TB_HP = 33;
+constexpr int TB_SMEM_FLOATS = TB_IH * TB_IP + TB_IH * TB_HP;
+
+__device__ __forceinline__ void tile_load_r8(float* in, const float* __restrict__ plane, int pitch, int w, int h,
+                                             int x0, int y0) {
+    for (int e = threadIdx.x; e < TB_IH * TB_IW; e += 256) {
+        const int r = e / TB_IW, col = e - r * TB_IW;
+        const int gx = x0 - TB_R + col, gy = y0 - TB_R + r;
+        float v = 0.f;
+        if (gx >= 0 && gx < w && gy >= 0 && gy < h) v = __ldg(plane + (int64_t)gy * pitch + gx);
+        in[r * TB_IP + col] = v;
+    }
+}
+
+template <int KI>
+__device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const float rx[8], const float ry[6],
+                                             float out[6]) {
+    const int tid = threadIdx.x;
+    {
+        const int hr = tid >> 2, hg = tid & 3;
+        const float* row = in + hr * TB_IP + 8 * hg;
+        float v[24];
+#pragma unroll
+        for (int j = 0; j < 24; j++) v[j] = row[j];
+        float* dst = hb + hr * TB_HP + 8 * hg;
+#pragma unroll
+        for (int o = 0; o < 8; o++) {
+            float a = 0.f;
+#pragma unroll
+            for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
+            dst[o] = a * rx[o];
+        }
+    }
+    __syncthreads();
+    {
+        const int vc = tid & 31, vg = tid >> 5;
+        const float* col = hb + (6 * vg) * TB_HP + vc;
+        float v[22];
+#pragma unroll
+        for (int j = 0; j < 22; j++) v[j] = col[j * TB_HP];
+#pragma unroll
+        for (int o = 0; o < 6; o++) {
+            float a = 0.f;
+#pragma unroll
+            for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
+            out[o] = a * ry[o];
+        }
+    }
+}
+
+template <int KI>
+__device__ __forceinline__ void tile_masses_r8(int x0, int y0, int w, int h, float rx[8], float ry[6]) {
+    const int tid = threadIdx.x;
+#pragma unroll
+    for (int o = 0; o < 8; o++) rx[o] = b_inv_mass<KI, 8>(x0 + 8 * (tid & 3) + o, w);
+#pragma unroll
+    for (int o = 0; o < 6; o++) ry[o] = b_inv_mass<KI, 8>(y0 + 6 * (tid >> 5) + o, h);
+}
+
+// ------------------------------------------------------------------------------------------
+// opsin dynamics (butter/colors.hpp:3-5,25-79)
+__device__ __forceinline__ void b_opsin(float& x, float& y, float& z, bool clamp) {
+    float ox = fmaf(0.29956550340058319f, x, fmaf(0.63373087833825936f, y, fmaf(0.077705617820981968f, z, 1.7557483643287353f)));
+    float oy = fmaf(0.22158691104574774f, x, fmaf(0.69391388044116142f, y, fmaf(0.0987313588422f, z, 1.7557483643287353f)));
+    float oz = fmaf(0.02f, x, fmaf(0.02f, y, fmaf(0.20480129041026129f, z, 12.226454707163354f)));
+    if (clamp) {
+        ox = fmaxf(ox, 1.7557483643287353f);
+        oy = fmaxf(oy, 1.7557483643287353f);
+        oz = fmaxf(oz, 12.226454707163354f);
+    }
+    x = ox;
+    y = oy;
+    z = oz;
+}
+__device__ __forceinline__ float b_gamma(float v) {
+    constexpr DConst kOff = dconst(9.9710635769299145);
+    return fmaf(19.245013259874995f, logf(add_dc(v, kOff)), -23.16046239805755f);
+}
+
+// grid (ceil(w/32), ceil(h/48), 2*npairs)
+__global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict__ work, BGeom g, int s,
+                                                              float intensity) {
+    extern __shared__ float sm[];
+    float* in = sm;
+    float* hb = sm + TB_IH * TB_IP;
+    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const BScaleDev S = pick_scale(g, s);
+    const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
+    float rx[8], ry[6];
+    tile_masses_r8<0>(x0, y0, S.w, S.h, rx, ry);
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    float src[3][6], blr[3][6];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        tile_load_r8(in, bplane(work, g, S, pair, P_LIN + img * 3 + c), S.p, S.w, S.h, x0, y0);
+        __syncthreads();
+        tile_blur_r8<0>(in, hb, rx, ry, blr[c]);
+#pragma unroll
+        for (int o = 0; o < 6; o++) src[c][o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
+        __syncthreads();
+    }
+    float* ox = bplane(work, g, S, pair, P_XYB + img * 3 + 0);
+    float* oy = bplane(work, g, S, pair, P_XYB + img * 3 + 1);
+    float* oz = bplane(work, g, S, pair, P_XYB + img * 3 + 2);
+#pragma unroll
+    for (int o = 0; o < 6; o++) {
+        const int x = x0 + vc, y = y0 + 6 * vg + o;
+        if (x < S.w && y < S.h) {
+            float sx = src[0][o] * intensity, sy = src[1][o] * intensity, sz = src[2][o] * intensity;
+            float bx = blr[0][o] * intensity, by = blr[1][o] * intensity, bz = blr[2][o] * intensity;
+            b_opsin(bx, by, bz, true);
+            bx = fmaxf(bx, 1e-4f);
+            by = fmaxf(by, 1e-4f);
+            bz = fmaxf(bz, 1e-4f);
+            const float ex = fmaxf(b_gamma(bx) / bx, 1e-4f);
+            const float ey = fmaxf(b_gamma(by) / by, 1e-4f);
+            const float ez = fmaxf(b_gamma(bz) / bz, 1e-4f);
+            b_opsin(sx, sy, sz, false);
+            sx *= ex;
+            sy *= ey;
+            sz *= ez;
+            sx = fmaxf(sx, 1.7557483643287353f);
+            sy = fmaxf(sy, 1.7557483643287353f);
+            sz = fmaxf(sz, 12.226454707163354f);
+            const int64_t i = (int64_t)y * S.p + x;
+            ox[i] = sx - sy;
+            oy[i] = sx + sy;
+            oz[i] = sz;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Separable horizontal pass, radius R (21 or 9): 128x16 tile per CTA; each thread makes 8
+// consecutive outputs from 8+2R registers. Warp w covers rows (w>>2)*8..+7 and columns
+// (w&3)*32..+31; the smem pitch is 17 mod 32 so the 8 rows of a warp hit distinct banks.
+// grid (ceil(w/128), ceil(h/16), 6*npairs): z -> pair = z/6, plane = src_id + z%6.
+constexpr int HB_TW = 128, HB_TH = 16, HB_P = 177;
+
+template <int KI, int R>
+__global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ work, BGeom g, int s, int src_id,
+                                                           int dst_id) {
+    __shared__ float in[HB_TH * HB_P];
+    const int pair = blockIdx.z / 6, pl = blockIdx.z % 6;
+    const BScaleDev S = pick_scale(g, s);
+    const float* src = bplane(work, g, S, pair, src_id + pl);
+    float* dst = bplane(work, g, S, pair, dst_id + pl);
+    const int x0 = blockIdx.x * HB_TW, y0 = blockIdx.y * HB_TH;
+    constexpr int IW = HB_TW + 2 * R;
+    for (int e = threadIdx.x; e < HB_TH * IW; e += 256) {
+        const int r = e / IW, col = e - r * IW;
+        const int gx = x0 - R + col, gy = y0 + r;
+        float v = 0.f;
+        if (gx >= 0 && gx < S.w && gy < S.h) v = __ldg(src + (int64_t)gy * S.p + gx);
+        in[r * HB_P + col] = v;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = (warp >> 2) * 8 + (lane >> 2);
+    const int col0 = (warp & 3) * 32 + 8 * (lane & 3);
+    const int gy = y0 + row;
+    if (gy >= S.h) return;
+    float v[8 + 2 * R];
+#pragma unroll
+    for (int j = 0; j < 8 + 2 * R; j++) v[j] = in[row * HB_P + col0 + j];
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+        const int x = x0 + col0 + o;
+        float a = 0.f;
+#pragma unroll
+        for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
+        if (x < S.w) dst[(int64_t)gy * S.p + x] = a * b_inv_mass<KI, R>(x, S.w);
+    }
+}
+
+// Separable vertical pass over the three channels of one image: 32x64 tile, each thread makes
+// 8 consecutive rows of one column for every channel, then runs the fused epilogue.
+// grid (ceil(w/32), ceil(h/64), 2*npairs).
+constexpr int VB_TW = 32, VB_TH = 64;
+
+template <int KI, int R>
+__device__ __forceinline__ void vblur3(float* in, float* __restrict__ work, const BGeom& g, int pair, int s, int src_id,
+                                       float out[3][8]) {
+    const BScaleDev S = pick_scale(g, s);
+    const int x0 = blockIdx.x * VB_TW, y0 = blockIdx.y * VB_TH;
+    constexpr int IH = VB_TH + 2 * R;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float* src = bplane(work, g, S, pair, src_id + c);
+        for (int e = threadIdx.x; e < IH * VB_TW; e += 256) {
+            const int r = e >> 5, col = e & 31;
+            const int gx = x0 + col, gy = y0 - R + r;
+            float v = 0.f;
+            if (gx < S.w && gy >= 0 && gy < S.h) v = __ldg(src + (int64_t)gy * S.p + gx);
+            in[c * IH * VB_TW + e] = v;
+        }
+    }
+    __syncthreads();
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    float ry[8];
+#pragma unroll
+    for (int o = 0; o < 8; o++) ry[o] = b_inv_mass<KI, R>(y0 + 8 * vg + o, S.h);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float* col = in + c * IH * VB_TW + (8 * vg) * VB_TW + vc;
+        float v[8 + 2 * R];
+#pragma unroll
+        for (int j = 0; j < 8 + 2 * R; j++) v[j] = col[j * VB_TW];
+#pragma unroll
+        for (int o = 0; o < 8; o++) {
+            float a = 0.f;
+#pragma unroll
+            for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
+            out[c][o] = a * ry[o];
+        }
+    }
+}
+
+// LF vertical pass: D = XYB - LF (in place over XYB) and LF vals (separatefrequencies.hpp:3-12)
+__global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ work, BGeom g, int s) {
+    extern __shared__ float sm[];
+    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    float lf[3][8];
+    vblur3<4, 21>(sm, work, g, pair, s, P_TMP + img * 3, lf);
+    const BScaleDev S = pick_scale(g, s);
+    const int x = blockIdx.x * VB_TW + (threadIdx.x & 31);
+    const int yb = blockIdx.y * VB_TH + 8 * (threadIdx.x >> 5);
+    if (x >= S.w) return;
+    float* xyb[3];
+    float* lfv[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        xyb[c] = bplane(work, g, S, pair, P_XYB + img * 3 + c);
+        lfv[c] = bplane(work, g, S, pair, P_LFV + img * 3 + c);
+    }
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+        const int y = yb + o;
+        if (y >= S.h) break;
+        const int64_t i = (int64_t)y * S.p + x;
+#pragma unroll
+        for (int c = 0; c < 3; c++) xyb[c][i] = xyb[c][i] - lf[c][o];
+        float vx = lf[0][o], vy = lf[1][o], vb = lf[2][o];
+        vb = vb + -0.362267051518f * vy;
+        vb = vb * 49.87984651440f;
+        vx = vx * 33.832837186260f;
+        vy = vy * 14.458268100570f;
+        lfv[0][i] = vx;
+        lfv[1][i] = vy;
+        lfv[2][i] = vb;
+    }
+}
+
+__device__ __forceinline__ float amplify_range(float x, float w) { return x > w ? x + w : x < -w ? x - w : 2.0f * x; }
+__device__ __forceinline__ float remove_range(float x, float w) { return x > w ? x - w : x < -w ? x + w : 0.0f; }
+__device__ __forceinline__ float maximum_clamp(float v, float maxval) {
+    const float kMul = 0.688059627878f;
+    if (v >= maxval) {
+        v -= maxval;
+        v *= kMul;
+        v += maxval;
+    } else if (v < -maxval) {
+        v += maxval;
+        v *= kMul;
+        v -= maxval;
+    }
+    return v;
+}
+
+// MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
+// written over the D planes (separatefrequencies.hpp:37-99,160-187).
+__global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ work, BGeom g, int s) {
+    extern __shared__ float sm[];
+    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    float mf[3][8];
+    vblur3<3, 9>(sm, work, g, pair, s, P_TMP + img * 3, mf);
+    const BScaleDev S = pick_scale(g, s);
+    const int x = blockIdx.x * VB_TW + (threadIdx.x & 31);
+    const int yb = blockIdx.y * VB_TH + 8 * (threadIdx.x >> 5);
+    if (x >= S.w) return;
+    float* d0 = bplane(work, g, S, pair, P_XYB + img * 3 + 0);
+    float* d1 = bplane(work, g, S, pair, P_XYB + img * 3 + 1);
+    float* m0 = bplane(work, g, S, pair, P_MF + img * 3 + 0);
+    float* m1 = bplane(work, g, S, pair, P_MF + img * 3 + 1);
+    float* m2 = bplane(work, g, S, pair, P_MF + img * 3 + 2);
+    const float sx = 0.653020556257f, yw = 46.0f;
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+        const int y = yb + o;
+        if (y >= S.h) break;
+        const int64_t i = (int64_t)y * S.p + x;
+        float hx = d0[i] - mf[0][o];
+        const float hy = d1[i] - mf[1][o];
+        hx *= sx + (yw * (1.0f - sx)) / (yw + hy * hy);
+        d0[i] = hx;
+        d1[i] = hy;
+        m0[i] = remove_range(mf[0][o], 0.29f);
+        m1[i] = amplify_range(mf[1][o], 0.1f);
+        m2[i] = mf[2][o];
+    }
+}
+
+// HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), 2*npairs)
+__global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ work, BGeom g, int s) {
+    extern __shared__ float sm[];
+    float* in = sm;
+    float* hb = sm + TB_IH * TB_IP;
+    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const BScaleDev S = pick_scale(g, s);
+    const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
+    float rx[8], ry[6];
+    tile_masses_r8<1>(x0, y0, S.w, S.h, rx, ry);
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+        tile_load_r8(in, bplane(work, g, S, pair, P_XYB + img * 3 + c), S.p, S.w, S.h, x0, y0);
+        __syncthreads();
+        float blr[6], pre[6];
+        tile_blur_r8<1>(in, hb, rx, ry, blr);
+#pragma unroll
+        for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
+        __syncthreads();
+        float* hfp = bplane(work, g, S, pair, P_HF + img * 2 + c);
+        float* uhfp = bplane(work, g, S, pair, P_UHF + img * 2 + c);
+#pragma unroll
+        for (int o = 0; o < 6; o++) {
+            const int x = x0 + vc, y = y0 + 6 * vg + o;
+            if (x < S.w && y < S.h) {
+                float hf = blr[o], uhf = pre[o];
+                if (c == 0) {
+                    uhf -= hf;
+                    hf = remove_range(hf, 1.5f);
+                    uhf = remove_range(uhf, 0.04f);
+                } else {
+                    hf = maximum_clamp(hf, 28.4691806922f);
+                    uhf -= hf;
+                    uhf = maximum_clamp(uhf, 5.19175294647f);
+                    uhf *= 2.69313763794f;
+                    hf *= 2.155f;
+                    hf = amplify_range(hf, 0.132f);
+                }
+                const int64_t i = (int64_t)y * S.p + x;
+                hfp[i] = hf;
+                uhfp[i] = uhf;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Malta difference (butter/maltaDiff.hpp). Parameters per map, derived on the host in float as
+// MaltaDiffMap[_LF]_Kernel derives them (:528-535).
+struct MaltaMap {
+    float norm1, n2gt, n2lt;
+};
+struct DiffParams {
+    MaltaMap mm[6];
+    float l2asym_gt[2], l2asym_lt[2];  // already including the inner x0.8 (simplerdiff.hpp:297-298)
+    float wmf[3], wlf[3];
+};
+
+__device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) {
+    const float absval = 0.5f * fabsf(a) + 0.5f * fabsf(b);
+    const float diff = a - b;
+    const float scaler = m.n2gt / (m.norm1 + absval);
+    float v = scaler * diff;
+    const float scaler2 = m.n2lt / (m.norm1 + absval);
+    const float fabs0 = fabsf(a);
+    const float too_small = 0.55f * fabs0, too_big = 1.05f * fabs0;
+    float impact = 0.0f;
+    if (a < 0.0f) {
+        if (b > -too_small) impact = b + too_small;
+        else if (b < -too_big) impact = -b - too_big;
+    } else {
+        if (b < too_small) impact = -b + too_small;
+        else if (b > too_big) impact = b - too_big;
+    }
+    impact *= scaler2;
+    return diff < 0.0f ? v - impact : v + impact;
+}
+
+// The 16 line patterns, as (dx, dy) taps in summation order (maltaDiff.hpp:4-512, after google
+// butteraugli). W(dx,dy) reads the register window at output row o.
+#define W(dx, dy) win[(o) + 4 + (dy)][4 + (dx)]
+#define SQ(expr)          \
+    {                     \
+        float s_ = (expr); \
+        ret = fmaf(s_, s_, ret); \
+    }
+#define MALTA_HF_BODY                                                                                       \
+    SQ(W(-4, 0) + W(-3, 0) + W(-2, 0) + W(-1, 0) + W(0, 0) + W(1, 0) + W(2, 0) + W(3, 0) + W(4, 0))        \
+    SQ(W(0, -4) + W(0, -3) + W(0, -2) + W(0, -1) + W(0, 0) + W(0, 1) + W(0, 2) + W(0, 3) + W(0, 4))        \
+    SQ(W(-3, -3) + W(-2, -2) + W(-1, -1) + W(0, 0) + W(1, 1) + W(2, 2) + W(3, 3))                          \
+    SQ(W(3, -3) + W(2, -2) + W(1, -1) + W(0, 0) + W(-1, 1) + W(-2, 2) + W(-3, 3))                          \
+    SQ(W(1, -4) + W(1, -3) + W(1, -2) + W(0, -1) + W(0, 0) + W(0, 1) + W(-1, 2) + W(-1, 3) + W(-1, 4))     \
+    SQ(W(-1, -4) + W(-1, -3) + W(-1, -2) + W(0, -1) + W(0, 0) + W(0, 1) + W(1, 2) + W(1, 3) + W(1, 4))     \
+    SQ(W(-4, -1) + W(-3, -1) + W(-2, -1) + W(-1, 0) + W(0, 0) + W(1, 0) + W(2, 1) + W(3, 1) + W(4, 1))     \
+    SQ(W(-4, 1) + W(-3, 1) + W(-2, 1) + W(-1, 0) + W(0, 0) + W(1, 0) + W(2, -1) + W(3, -1) + W(4, -1))     \
+    SQ(W(-2, -3) + W(-1, -2) + W(-1, -1) + W(0, 0) + W(1, 1) + W(1, 2) + W(2, 3))                          \
+    SQ(W(2, -3) + W(1, -2) + W(1, -1) + W(0, 0) + W(-1, 1) + W(-1, 2) + W(-2, 3))                          \
+    SQ(W(-3, -2) + W(-2, -1) + W(-1, -1) + W(0, 0) + W(1, 1) + W(2, 1) + W(3, 2))                          \
+    SQ(W(3, -2) + W(2, -1) + W(1, -1) + W(0, 0) + W(-1, 1) + W(-2, 1) + W(-3, 2))                          \
+    SQ(W(-4, 2) + W(-3, 2) + W(-2, 1) + W(-1, 1) + W(0, 0) + W(1, 0) + W(2, -1) + W(3, -1))                \
+    SQ(W(-4, -2) + W(-3, -2) + W(-2, -1) + W(-1, -1) + W(0, 0) + W(1, 0) + W(2, 1) + W(3, 1))              \
+    SQ(W(-2, -4) + W(-2, -3) + W(-1, -2) + W(-1, -1) + W(0, 0) + W(0, 1) + W(1, 2) + W(1, 3))              \
+    SQ(W(2, -4) + W(2, -3) + W(1, -2) + W(1, -1) + W(0, 0) + W(0, 1) + W(-1, 2) + W(-1, 3))
+#define MALTA_LF_BODY                                           \
+    SQ(W(-4, 0) + W(-2, 0) + W(0, 0) + W(2, 0) + W(4, 0))       \
+    SQ(W(0, -4) + W(0, -2) + W(0, 0) + W(0, 2) + W(0, 4))       \
+    SQ(W(-3, -3) + W(-2, -2) + W(0, 0) + W(2, 2) + W(3, 3))     \
+    SQ(W(3, -3) + W(2, -2) + W(0, 0) + W(-2, 2) + W(-3, 3))     \
+    SQ(W(1, -4) + W(1, -2) + W(0, 0) + W(-1, 2) + W(-1, 4))     \
+    SQ(W(-1, -4) + W(-1, -2) + W(0, 0) + W(1, 2) + W(1, 4))     \
+    SQ(W(-4, -1) + W(-2, -1) + W(0, 0) + W(2, 1) + W(4, 1))     \
+    SQ(W(-4, 1) + W(-2, 1) + W(0, 0) + W(2, -1) + W(4, -1))     \
+    SQ(W(-2, -3) + W(-1, -2) + W(0, 0) + W(1, 2) + W(2, 3))     \
+    SQ(W(2, -3) + W(1, -2) + W(0, 0) + W(-1, 2) + W(-2, 3))     \
+    SQ(W(-3, -2) + W(-2, -1) + W(0, 0) + W(2, 1) + W(3, 2))     \
+    SQ(W(3, -2) + W(2, -1) + W(0, 0) + W(-2, 1) + W(-3, 2))     \
+    SQ(W(-4, 2) + W(-2, 1) + W(0, 0) + W(2, -1) + W(4, -2))     \
+    SQ(W(-4, -2) + W(-2, -1) + W(0, 0) + W(2, 1) + W(4, 2))     \
+    SQ(W(-2, -4) + W(-1, -2) + W(0, 0) + W(1, 2) + W(2, 4))     \
+    SQ(W(2, -4) + W(1, -2) + W(0, 0) + W(-1, 2) + W(-2, 4))
+
+constexpr int DF_TW = 32, DF_TH = 64, DF_H = 4;
+constexpr int DF_IW = DF_TW + 2 * DF_H, DF_IH = DF_TH + 2 * DF_H;  // 40 x 72
+
+// Sliding 9x9 register window down one column: rows are loaded as they are first needed and
+// die after their last pattern, so about 81 values are live at a time.
+template <bool HF>
+__device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r0, int c, float acc[8]) {
+    float win[16][9];
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+#pragma unroll
+        for (int j = 0; j < 9; j++) win[r][j] = Dt[(r0 + r) * DF_IW + c + j];
+        if (r >= 8) {
+            const int o = r - 8;
+            float ret = 0.0f;
+            if (HF) {
+                MALTA_HF_BODY
+            } else {
+                MALTA_LF_BODY
+            }
+            acc[o] += ret;
+        }
+    }
+}
+#undef W
+#undef SQ
+
+// grid (ceil(w/32), ceil(h/64), npairs), 256 threads; column tid&31, rows 8*(tid>>5)..+7.
+__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__ work, BGeom g, int s, DiffParams P) {
+    __shared__ float Dt[DF_IH * DF_IW];
+    const int pair = blockIdx.z;
+    const BScaleDev S = pick_scale(g, s);
+    const int x0 = blockIdx.x * DF_TW, y0 = blockIdx.y * DF_TH;
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    float acX[8], acY[8];
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+        acX[o] = 0.f;
+        acY[o] = 0.f;
+    }
+    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X
+    const int ids[6] = {P_UHF + 1, P_UHF + 0, P_HF + 1, P_HF + 0, P_MF + 1, P_MF + 0};
+    const int stride_img[6] = {2, 2, 2, 2, 3, 3};
+#pragma unroll
+    for (int m = 0; m < 6; m++) {
+        const float* l0 = bplane(work, g, S, pair, ids[m]);
+        const float* l1 = bplane(work, g, S, pair, ids[m] + stride_img[m]);
+        const MaltaMap mm = P.mm[m];
+        for (int e = threadIdx.x; e < DF_IH * DF_IW; e += 256) {
+            const int r = e / DF_IW, col = e - r * DF_IW;
+            const int gx = x0 - DF_H + col, gy = y0 - DF_H + r;
+            float v = 0.f;
+            if (gx >= 0 && gx < S.w && gy >= 0 && gy < S.h) {
+                const int64_t i = (int64_t)gy * S.p + gx;
+                v = malta_pre(__ldg(l0 + i), __ldg(l1 + i), mm);
+            }
+            Dt[e] = v;
+        }
+        __syncthreads();
+        if (m < 2) malta_column<true>(Dt, 8 * vg, vc, (m & 1) ? acX : acY);
+        else malta_column<false>(Dt, 8 * vg, vc, (m & 1) ? acX : acY);
+        __syncthreads();
+    }
+    const int x = x0 + vc;
+    if (x >= S.w) return;
+    const float mul = 6.19424080439f;
+    const float bias = mul * 12.61050594197f;
+    const float sqb = sqrtf(bias);
+    constexpr DConst k04 = dconst(0.4);
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+        const int y = y0 + 8 * vg + o;
+        if (y >= S.h) break;
+        const int64_t i = (int64_t)y * S.p + x;
+        float ac[3] = {acX[o], acY[o], 0.f};
+        float dc[3] = {0.f, 0.f, 0.f};
+        float hf[2][2], uhf[2][2];
+#pragma unroll
+        for (int m = 0; m < 2; m++)
+#pragma unroll
+            for (int c = 0; c < 2; c++) {
+                hf[m][c] = bplane(work, g, S, pair, P_HF + m * 2 + c)[i];
+                uhf[m][c] = bplane(work, g, S, pair, P_UHF + m * 2 + c)[i];
+            }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            if (c < 2) {  // L2AsymDiff (simplerdiff.hpp:263-293)
+                const float s1 = hf[0][c], s2 = hf[1][c];
+                const float diff = s1 - s2;
+                ac[c] += P.l2asym_gt[c] * diff * diff;
+                const float fabs0 = fabsf(s1);
+                const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
+                const float wl = P.l2asym_lt[c];
+                if (s1 < 0) {
+                    if (s2 > -too_small) { const float v = s2 + too_small; ac[c] += wl * v * v; }
+                    else if (s2 < -too_big) { const float v = -s2 - too_big; ac[c] += wl * v * v; }
+                } else {
+                    if (s2 < too_small) { const float v = too_small - s2; ac[c] += wl * v * v; }
+                    else if (s2 > too_big) { const float v = s2 - too_big; ac[c] += wl * v * v; }
+                }
+            }
+            {
+                const float d = bplane(work, g, S, pair, P_MF + c)[i] - bplane(work, g, S, pair, P_MF + 3 + c)[i];
+                ac[c] += P.wmf[c] * d * d;
+            }
+            {
+                const float d = bplane(work, g, S, pair, P_LFV + c)[i] - bplane(work, g, S, pair, P_LFV + 3 + c)[i];
+                dc[c] += P.wlf[c] * d * d;
+            }
+        }
+        bplane(work, g, S, pair, P_SAC)[i] = ac[0] + ac[1] + ac[2];
+        bplane(work, g, S, pair, P_SDC)[i] = dc[0] + dc[1] + dc[2];
+        // maskinit + diffPrecompute (maskPsycho.hpp:3-40)
+#pragma unroll
+        for (int m = 0; m < 2; m++) {
+            const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
+            const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
+            const float mk = sqrtf(xd * xd + yd * yd);
+            bplane(work, g, S, pair, P_PRE0 + m)[i] = sqrtf(mul * fabsf(mk) + bias) - sqb;
+        }
+    }
+}
+
+// Blur both mask planes (sigma 2.7); store B0 and add 10*(B0-B1)^2 to the AC sum.
+// grid (ceil(w/32), ceil(h/48), npairs)
+__global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restrict__ work, BGeom g, int s) {
+    extern __shared__ float sm[];
+    float* in = sm;
+    float* hb = sm + TB_IH * TB_IP;
+    const int pair = blockIdx.z;
+    const BScaleDev S = pick_scale(g, s);
+    const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
+    float rx[8], ry[6];
+    tile_masses_r8<2>(x0, y0, S.w, S.h, rx, ry);
+    float b[2][6];
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+        tile_load_r8(in, bplane(work, g, S, pair, P_PRE0 + m), S.p, S.w, S.h, x0, y0);
+        __syncthreads();
+        tile_blur_r8<2>(in, hb, rx, ry, b[m]);
+        __syncthreads();
+    }
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    float* b0 = bplane(work, g, S, pair, P_B0);
+    float* sac = bplane(work, g, S, pair, P_SAC);
+#pragma unroll
+    for (int o = 0; o < 6; o++) {
+        const int x = x0 + vc, y = y0 + 6 * vg + o;
+        if (x < S.w && y < S.h) {
+            const int64_t i = (int64_t)y * S.p + x;
+            b0[i] = b[0][o];
+            const float d = b[0][o] - b[1][o];
+            sac[i] += 10.0f * d * d;
+        }
+    }
+}
+
+// combineMasks.hpp:3-19
+__device__ __forceinline__ float mask_common(float c) {
+    constexpr DConst kK = dconst(1.0 / (double)(0.79079917404f * 17.83f));
+    // (float)((1.0 + c) * K) with 1 + c kept exact as a float pair
+    const float s = 1.0f + c;
+    const float bb = s - 1.0f;
+    const float e = (1.0f - (s - bb)) + (c - bb);
+    const float p = s * kK.hi;
+    const float pe = fmaf(s, kK.hi, -p);
+    const float r = p + (pe + fmaf(s, kK.lo, e * kK.hi));
+    return r * r;
+}
+__device__ __forceinline__ float mask_y(float delta) {
+    return mask_common(2.5485944793f / ((0.451936922203f * delta) + 0.829591754942f));
+}
+__device__ __forceinline__ float mask_dc_y(float delta) {
+    return mask_common(0.505054525019f / ((3.87449418804f * delta) + 0.20025578522f));
+}
+// maskPsycho.hpp:42-55
+__device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float& m2) {
+    if (v < m2) {
+        if (v < m0) {
+            m2 = m1;
+            m1 = m0;
+            m0 = v;
+        } else if (v < m1) {
+            m2 = m1;
+            m1 = v;
+        } else {
+            m2 = v;
+        }
+    }
+}
+
+// Fuzzy erosion + diffmap; FINAL also folds in the half-scale map, stores the distortion map
+// and emits norm partials. grid (ceil(w/32), ceil(h/8), npairs), block (32, 8).
+template <bool FINAL>
+__global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__ work, BGeom g, int s,
+                                                             float* __restrict__ distmap, float* __restrict__ partials,
+                                                             float qnorm) {
+    const int pair = blockIdx.z;
+    const BScaleDev S = pick_scale(g, s);
+    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    float sq = 0.f, s3 = 0.f, mx = 0.f;
+    if (x < S.w && y < S.h) {
+        const float* b0 = bplane(work, g, S, pair, P_B0);
+        const int k = 3;
+        const int W = S.w, H = S.h, p = S.p;
+        float m0 = b0[(int64_t)y * p + x], m1 = 2.0f * m0, m2 = m1;
+        if (x >= k) {
+            store_min3(b0[(int64_t)y * p + x - k], m0, m1, m2);
+            if (y >= k) store_min3(b0[(int64_t)(y - k) * p + x - k], m0, m1, m2);
+            if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x - k], m0, m1, m2);
+        }
+        if (x < W - k) {
+            store_min3(b0[(int64_t)y * p + x + k], m0, m1, m2);
+            if (y >= k) store_min3(b0[(int64_t)(y - k) * p + x + k], m0, m1, m2);
+            if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x + k], m0, m1, m2);
+        }
+        if (y >= k) store_min3(b0[(int64_t)(y - k) * p + x], m0, m1, m2);
+        if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x], m0, m1, m2);
+        const float mask = 0.45f * m0 + 0.3f * m1 + 0.25f * m2;
+        const int64_t i = (int64_t)y * p + x;
+        float d = sqrtf(mask_y(mask) * bplane(work, g, S, pair, P_SAC)[i] +
+                        mask_dc_y(mask) * bplane(work, g, S, pair, P_SDC)[i]);
+        if (!FINAL) {
+            bplane(work, g, S, pair, P_DIFF)[i] = d;
+        } else {
+            constexpr DConst k085 = dconst(1.0 - 0.3 * (double)0.5f);
+            const BScaleDev Hs = g.s[1];
+            const float small = bplane(work, g, Hs, pair, P_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
+            d = fmaf(0.5f, small, mul_dc(d, k085));
+            distmap[(int64_t)pair * W * H + (int64_t)y * W + x] = d;
+            sq = powf(d, qnorm);
+            s3 = fabsf(d) * d * d;
+            mx = fabsf(d);
+        }
+    }
+    if (FINAL) {
+        __shared__ float red[3][8];
+        const int lane = threadIdx.x, warp = threadIdx.y;
+        sq = warp_sum(sq);
+        s3 = warp_sum(s3);
+        mx = warp_max(mx);
+        if (lane == 0) {
+            red[0][warp] = sq;
+            red[1][warp] = s3;
+            red[2][warp] = mx;
+        }
+        __syncthreads();
+        if (warp == 0 && lane < 3) {
+            float v = red[lane][0];
+            for (int w = 1; w < 8; w++) v = lane == 2 ? fmaxf(v, red[lane][w]) : v + red[lane][w];
+            const int blk = blockIdx.y * gridDim.x + blockIdx.x;
+            partials[((int64_t)pair * g.norm_tiles + blk) * 3 + lane] = v;
+        }
+    }
+}
+
+// FP64 norm combine, one CTA per pair (diffnorms.hpp:263-306).
+__global__ void __launch_bounds__(256) butter_finalize_kernel(const float* __restrict__ partials,
+                                                              double* __restrict__ norms, BGeom g, int qnorm) {
+    __shared__ double red[3][8];
+    const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double sq = 0.0, s3 = 0.0;
+    float mx = 0.f;
+    for (int t = tid; t < g.norm_tiles; t += 256) {
+        const float* p = partials + ((int64_t)pair * g.norm_tiles + t) * 3;
+        sq += (double)p[0];
+        s3 += (double)p[1];
+        mx = fmaxf(mx, p[2]);
+    }
+    sq = warp_sum(sq);
+    s3 = warp_sum(s3);
+    mx = warp_max(mx);
+    if (lane == 0) {
+        red[0][warp] = sq;
+        red[1][warp] = s3;
+        red[2][warp] = (double)mx;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double a = 0, b = 0, c = 0;
+        for (int w = 0; w < 8; w++) {
+            a += red[0][w];
+            b += red[1][w];
+            c = fmax(c, red[2][w]);
+        }
+        const double n = (double)g.s[0].w * (double)g.s[0].h;
+        norms[pair * 3 + 0] = pow(a / n, 1.0 / (double)qnorm);
+        norms[pair * 3 + 1] = pow(b / n, 1.0 / 3.0);
+        norms[pair * 3 + 2] = c;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+
+static BGeom make_bgeom(int64_t w, int64_t h) {
+    BGeom g{};
+    int64_t off = 0;
+    int64_t cw = w, ch = h;
+    for (int s = 0; s < 2; s++) {
+        BScaleDev& S = g.s[s];
+        S.w = (int)cw;
+        S.h = (int)ch;
+        S.p = (int)round_up(cw, 8);
+        S.n = round_up((int64_t)S.p * ch, 64);
+        S.base = off;
+        off += S.n * NPLANES;
+        cw = half_dim(cw);
+        ch = half_dim(ch);
+    }
+    g.pair_floats = off;
+    g.norm_tiles_x = (int)ceil_div(w, 32);
+    g.norm_tiles = g.norm_tiles_x * (int)ceil_div(h, 8);
+    return g;
+}
+
+static DiffParams make_diff_params() {
+    DiffParams P{};
+    const float hf_asym = 0.8f;
+    const float sq = std::sqrt(hf_asym);
+    struct In {
+        float w_gt, w_lt, norm1;
+        bool hf;
+    };
+    const In in[6] = {
+        {1.10039032555f * hf_asym, 1.10039032555f / hf_asym, 71.7800275169f, true},
+        {173.5f * hf_asym, 173.5f / hf_asym, 5.0f, true},
+        {18.7237414387f * sq, 18.7237414387f / sq, 4498534.45232f, false},
+        {6923.99476109f * sq, 6923.99476109f / sq, 8051.15833247f, false},
+        {37.0819870399f, 37.0819870399f, 130262059.556f, false},
+        {8246.75321353f, 8246.75321353f, 1009002.70582f, false},
+    };
+    for (int m = 0; m < 6; m++) {
+        const float mulli = in[m].hf ? 0.39905817637f : 0.611612573796f;
+        const float len2 = 3.75f * 2.0f + 1.0f;
+        const float wpg = mulli * std::sqrt(0.5f * in[m].w_gt) / len2;
+        const float wpl = mulli * std::sqrt(0.33f * in[m].w_lt) / len2;
+        P.mm[m].norm1 = in[m].norm1;
+        P.mm[m].n2gt = wpg * in[m].norm1;
+        P.mm[m].n2lt = wpl * in[m].norm1;
+    }
+    const float wmul[9] = {400.0f, 1.50815703118f, 0.0f, 2150.0f, 10.6195433239f, 16.2176043152f,
+                           29.2353797994f, 0.844626970982f, 0.703646627719f};
+    for (int c = 0; c < 2; c++) {
+        float gt = wmul[c] * hf_asym, lt = wmul[c] / hf_asym;
+        P.l2asym_gt[c] = (float)((double)gt * 0.8);
+        P.l2asym_lt[c] = (float)((double)lt * 0.8);
+    }
+    for (int c = 0; c < 3; c++) {
+        P.wmf[c] = wmul[3 + c];
+        P.wlf[c] = wmul[6 + c];
+    }
+    return P;
+}
+
+constexpr int kTileSmem = TB_SMEM_FLOATS * 4;
+constexpr int kVLfSmem = 3 * (VB_TH + 42) * VB_TW * 4;
+constexpr int kVMfSmem = 3 * (VB_TH + 18) * VB_TW * 4;
+
+int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensity_, int max_pairs_) {
+    w = width;
+    h = height;
+    qnorm = qnorm_;
+    intensity = intensity_;
+    max_pairs = max_pairs_;
+    BGeom g = make_bgeom(w, h);
+    for (int s = 0; s < 2; s++) {
+        sc[s].w = g.s[s].w;
+        sc[s].h = g.s[s].h;
+        sc[s].n = g.s[s].n;
+    }
+    work_floats = g.pair_floats;
+    norm_blocks = g.norm_tiles;
+    int rc = upload_butter_tables();
+    if (rc) return rc;
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
+    VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * work_floats * max_pairs));
+    VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
+    VSHIP_CUDA_TRY(cudaMalloc(&distmap, sizeof(float) * (size_t)w * h * max_pairs));
+    VSHIP_CUDA_TRY(cudaMalloc(&norms, sizeof(double) * 3 * max_pairs));
+    return E_OK;
+}
+
+void ButterEngine::destroy() {
+    if (work) cudaFree(work);
+    if (partials) cudaFree(partials);
+    if (distmap) cudaFree(distmap);
+    if (norms) cudaFree(norms);
+    work = nullptr;
+    partials = nullptr;
+    distmap = nullptr;
+    norms = nullptr;
+}
+
+size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs) {
+    BGeom g = make_bgeom(w, h);
+    return (sizeof(float) * (size_t)g.pair_floats + sizeof(float) * 3 * (size_t)g.norm_tiles +
+            sizeof(float) * (size_t)w * h + sizeof(double) * 3) *
+           pairs;
+}
+
+int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st) {
+    if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
+    const BGeom g = make_bgeom(w, h);
+    static const DiffParams P = make_diff_params();
+    const unsigned np = (unsigned)npairs;
+    {
+        dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), 2 * np);
+        ProfScope ps_("butter_decode", st);
+        switch (intype) {
+            case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
+            case IN_UINT16: butter_decode_kernel<IN_UINT16><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
+            case IN_HALF: butter_decode_kernel<IN_HALF><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
+            default: butter_decode_kernel<IN_FLOAT><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
+        }
+    }
+    for (int s = 1; s >= 0; s--) {
+        const int64_t sw = g.s[s].w, sh = g.s[s].h;
+        const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), 2 * np);
+        const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 6 * np);
+        const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), 2 * np);
+        { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s, intensity); }
+        { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(work, g, s, P_XYB, P_TMP); }
+        { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(work, g, s); }
+        { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(work, g, s, P_XYB, P_TMP); }
+        { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(work, g, s); }
+        { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s); }
+        const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
+        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, 0, st>>>(work, g, s, P); }
+        const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
+        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(work, g, s); }
+        const dim3 gf((unsigned)ceil_div(sw, 32), (unsigned)ceil_div(sh, 8), np);
+        if (s == 1)
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, dim3(32, 8), 0, st>>>(work, g, s, distmap, partials, (float)qnorm); }
+        else
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, dim3(32, 8), 0, st>>>(work, g, s, distmap, partials, (float)qnorm); }
+    }
+    { ProfScope ps_("butter_finalize", st); butter_finalize_kernel<<<np, 256, 0, st>>>(partials, norms_out ? norms_out : norms, g, qnorm); }
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    return E_OK;
+}
+
+}  // namespace vship

@@ -1,0 +1,93 @@
+// profile.cu -- per-kernel event timing registry (see profile.h).
+#include "profile.h"
+
+#include <atomic>
+#include <cstdio>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+namespace vship {
+
+namespace {
+struct Rec {
+    std::string name;
+    cudaEvent_t a = nullptr, b = nullptr;
+};
+std::atomic<bool> g_on{false};
+std::mutex g_mu;
+std::vector<Rec> g_recs;
+std::vector<cudaEvent_t> g_pool;
+
+cudaEvent_t get_event() {
+    if (!g_pool.empty()) {
+        cudaEvent_t e = g_pool.back();
+        g_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace
+
+bool prof_enabled() { return g_on.load(std::memory_order_relaxed); }
+
+int prof_begin(const char* name, cudaStream_t st) {
+    if (!prof_enabled()) return -1;
+    std::lock_guard<std::mutex> g(g_mu);
+    Rec r;
+    r.name = name;
+    r.a = get_event();
+    r.b = get_event();
+    cudaEventRecord(r.a, st);
+    g_recs.push_back(r);
+    return (int)g_recs.size() - 1;
+}
+
+void prof_end(int token, cudaStream_t st) {
+    if (token < 0) return;
+    std::lock_guard<std::mutex> g(g_mu);
+    if (token < (int)g_recs.size()) cudaEventRecord(g_recs[token].b, st);
+}
+
+// JSON object {"kernel": [launches, total_ms], ...}; clears the records.
+int prof_report(char* buf, int len) {
+    std::map<std::string, std::pair<long, double>> agg;
+    {
+        std::lock_guard<std::mutex> g(g_mu);
+        for (Rec& r : g_recs) {
+            float ms = 0.f;
+            cudaEventSynchronize(r.b);
+            if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+                auto& e = agg[r.name];
+                e.first += 1;
+                e.second += ms;
+            }
+            g_pool.push_back(r.a);
+            g_pool.push_back(r.b);
+        }
+        g_recs.clear();
+    }
+    std::string s = "{";
+    bool first = true;
+    for (auto& kv : agg) {
+        char tmp[256];
+        snprintf(tmp, sizeof(tmp), "%s\"%s\": [%ld, %.6f]", first ? "" : ", ", kv.first.c_str(), kv.second.first,
+                 kv.second.second);
+        s += tmp;
+        first = false;
+    }
+    s += "}";
+    if (buf && len > 0) {
+        int n = (int)s.size() < len - 1 ? (int)s.size() : len - 1;
+        for (int i = 0; i < n; i++) buf[i] = s[i];
+        buf[n] = 0;
+    }
+    return (int)s.size() + 1;
+}
+
+void prof_set(bool on) { g_on.store(on); }
+
+}  // namespace vship

@@ -1,0 +1,449 @@
+// ssimu2.cu -- SSIMULACRA2 scoring on sm_103a.
+//
+// Three kernels per launch, all batched over frame pairs:
+//   1. ssimu2_pyramid  : decode + x^2.4 linearisation + the 6-level 2x2 box pyramid + positive
+//                        XYB, one 32x32 level-0 tile per CTA with every coarser level computed
+//                        from shared memory (the pyramid is tile-local: a 2^k-aligned level-0
+//                        tile maps exactly onto its level-k tile, edge clamp included).
+//                        Reference: ssimu2/main.hpp:15-32, makeXYB.hpp:4-98, downsample.hpp:3-31.
+//   2. ssimu2_stats    : all six scales in one launch. Per 32x48 output tile it stages I1, I2,
+//                        I1^2, I2^2, I1*I2 (8-px halo, zero outside) in shared memory, runs the
+//                        17-tap separable Gaussian (border-renormalised) for the five moments with
+//                        register blocking, forms the SSIM / artifact / detail-loss maps and emits
+//                        18 partial sums (6 pools x 3 channels) per CTA.
+//                        Reference: ssimu2/score.hpp:95-196, gaussianblur.hpp:24-92.
+//   3. ssimu2_finalize : FP64 combine of the partial sums, 4th roots, the 108-feature permutation,
+//                        weighted sum and score mapping (score.hpp:198-401, main.hpp:83-98).
+#include "common.cuh"
+#include "ssimu2.h"
+#include "profile.h"
+
+#include <cmath>
+#include <vector>
+
+namespace vship {
+
+// ------------------------------------------------------------------------------------------
+// Gaussian table (sigma 1.5, radius 8): taps and prefix integral, built on the host exactly as
+// ssimu2/gaussianblur.hpp:7-18 builds them.
+__constant__ float c_s2_k[17];
+__constant__ float c_s2_I[18];
+// SSIMULACRA2 feature weights (ssimu2/score.hpp:272-379), FP64.
+__constant__ double c_s2_w[108];
+
+static const double kSsimu2Weights[108] = {
+    0.0, 0.0007376606707406586, 0.0, 0.0, 0.0007793481682867309, 0.0,
+    0.0, 0.0004371155730107379, 0.0, 1.1041726426657346, 0.00066284834129271, 0.00015231632783718752,
+    0.0, 0.0016406437456599754, 0.0, 1.8422455520539298, 11.441172603757666, 0.0,
+    0.0007989109436015163, 0.000176816438078653, 0.0, 1.8787594979546387, 10.94906990605142, 0.0,
+    0.0007289346991508072, 0.9677937080626833, 0.0, 0.00014003424285435884, 0.9981766977854967, 0.00031949755934435053,
+    0.0004550992113792063, 0.0, 0.0, 0.0013648766163243398, 0.0, 0.0,
+    0.0, 0.0, 0.0, 7.466890328078848, 0.0, 17.445833984131262,
+    0.0006235601634041466, 0.0, 0.0, 6.683678146179332, 0.00037724407979611296, 1.027889937768264,
+    225.20515300849274, 0.0, 0.0, 19.213238186143016, 0.0011401524586618361, 0.001237755635509985,
+    176.39317598450694, 0.0, 0.0, 24.43300999870476, 0.28520802612117757, 0.0004485436923833408,
+    0.0, 0.0, 0.0, 34.77906344483772, 44.835625328877896, 0.0,
+    0.0, 0.0, 0.0, 0.0, 0.0, 0.0,
+    0.0, 0.0008680556573291698, 0.0, 0.0, 0.0, 0.0,
+    0.0, 0.0005313191874358747, 0.0, 0.00016533814161379112, 0.0, 0.0,
+    0.0, 0.0, 0.0, 0.0004179171803251336, 0.0017290828234722833, 0.0,
+    0.0020827005846636437, 0.0, 0.0, 8.826982764996862, 23.19243343998926, 0.0,
+    95.1080498811086, 0.9863978034400682, 0.9834382792465353, 0.0012286405048278493, 171.2667255897307, 0.9807858872435379,
+    0.0, 0.0, 0.0, 0.0005130064588990679, 0.0, 0.00010854057858411537,
+};
+
+static int upload_constants_once() {
+    // Constant memory is per device; the tables are uploaded on every engine init (cheap).
+    float k[17], I[18];
+    const float sigma = 1.5f;
+    I[0] = 0.f;
+    for (int i = 0; i < 17; i++) {
+        float e = std::exp((float)(-(8 - i) * (8 - i)) / (2 * sigma * sigma));
+        k[i] = (float)((double)e / std::sqrt(6.28318530718 * sigma * sigma));
+        I[i + 1] = I[i] + k[i];
+    }
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k, k, sizeof(k)));
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_I, I, sizeof(I)));
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_w, kSsimu2Weights, sizeof(kSsimu2Weights)));
+    return E_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// positive XYB (ssimu2/makeXYB.hpp:4-50)
+__device__ __forceinline__ void positive_xyb(float& r, float& g, float& b) {
+    const float bias = 0.0037930734f;
+    float ox = fmaf(0.30f, r, fmaf(0.622f, g, fmaf(0.078f, b, bias)));
+    float oy = fmaf(0.23f, r, fmaf(0.692f, g, fmaf(0.078f, b, bias)));
+    float oz = fmaf(0.24342269f, r, fmaf(0.20476745f, g, fmaf(0.55180986f, b, bias)));
+    const float abs_bias = -0.1559542025327239f;
+    ox = cbrtf(ox * (float)(ox >= 0.f)) + abs_bias;
+    oy = cbrtf(oy * (float)(oy >= 0.f)) + abs_bias;
+    oz = cbrtf(oz * (float)(oz >= 0.f)) + abs_bias;
+    float X = 0.5f * (ox - oy);
+    float Y = X + oy;
+    float B = oz;
+    constexpr DConst k055 = dconst(0.55), k042 = dconst(0.42), k001 = dconst(0.01);
+    r = add_dc(X * 14.0f, k042);
+    g = add_dc(Y, k001);
+    b = add_dc(B - Y, k055);
+}
+
+// ------------------------------------------------------------------------------------------
+// Kernel 1: decode + linearise + pyramid + XYB. grid (tiles_x0, tiles_y0, 2*npairs), 256 thr.
+template <int IT>
+__global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
+                                                             float* __restrict__ pyr, Ssimu2Geom g) {
+    __shared__ float smA[3 * 32 * 33];
+    __shared__ float smB[3 * 16 * 17];
+    const int img = blockIdx.z;  // pair*2 + image
+    const FrameDesc fd = frames[img];
+    float* base = pyr + (int64_t)img * 3 * g.plane_elems;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int bx = blockIdx.x, by = blockIdx.y;
+    {
+        const Ssimu2Level L = g.lv[0];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int ly = ty + 8 * r;
+            const int gx = bx * 32 + tx, gy = by * 32 + ly;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+            if (gx < L.w && gy < L.h) {
+                v0 = to_linear(load_sample<IT>(fd.plane[0], fd.stride, gx, gy));
+                v1 = to_linear(load_sample<IT>(fd.plane[1], fd.stride, gx, gy));
+                v2 = to_linear(load_sample<IT>(fd.plane[2], fd.stride, gx, gy));
+                float X = v0, Y = v1, B = v2;
+                positive_xyb(X, Y, B);
+                int64_t o = L.off + (int64_t)gy * L.pitch + gx;
+                base[o] = X;
+                base[g.plane_elems + o] = Y;
+                base[2 * g.plane_elems + o] = B;
+            }
+            smA[(0 * 32 + ly) * 33 + tx] = v0;
+            smA[(1 * 32 + ly) * 33 + tx] = v1;
+            smA[(2 * 32 + ly) * 33 + tx] = v2;
+        }
+    }
+    __syncthreads();
+    float* cur = smA;
+    float* nxt = smB;
+    int cside = 32;
+#pragma unroll 1
+    for (int k = 1; k < 6; k++) {
+        const int nside = cside >> 1;
+        const Ssimu2Level L = g.lv[k], P = g.lv[k - 1];
+        const int ox = bx * nside, oy = by * nside;
+        const int pox = bx * cside, poy = by * cside;
+        for (int i = threadIdx.x; i < nside * nside; i += 256) {
+            const int lx = i % nside, ly = i / nside;
+            const int gx = ox + lx, gy = oy + ly;
+            float v[3] = {0.f, 0.f, 0.f};
+            if (gx < L.w && gy < L.h) {
+                const int x0 = 2 * lx, y0 = 2 * ly;
+                const int x1 = min(2 * gx + 1, P.w - 1) - pox;
+                const int y1 = min(2 * gy + 1, P.h - 1) - poy;
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const float* cb = cur + c * cside * (cside + 1);
+                    float s = cb[y0 * (cside + 1) + x0];
+                    s += cb[y1 * (cside + 1) + x0];
+                    s += cb[y0 * (cside + 1) + x1];
+                    s += cb[y1 * (cside + 1) + x1];
+                    v[c] = s * 0.25f;
+                }
+                float X = v[0], Y = v[1], B = v[2];
+                positive_xyb(X, Y, B);
+                int64_t o = L.off + (int64_t)gy * L.pitch + gx;
+                base[o] = X;
+                base[g.plane_elems + o] = Y;
+                base[2 * g.plane_elems + o] = B;
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) nxt[c * nside * (nside + 1) + ly * (nside + 1) + lx] = v[c];
+        }
+        __syncthreads();
+        float* t = cur;
+        cur = nxt;
+        nxt = t;
+        cside = nside;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Kernel 2: fused 5-moment blur + SSIM/edge maps + per-CTA pooling, all scales in one launch.
+// grid (tiles_total, npairs), 256 threads, dynamic smem kStatsSmem.
+constexpr int ST_TW = 32, ST_TH = 48, ST_R = 8;
+constexpr int ST_IW = ST_TW + 2 * ST_R;  // 48 input columns
+constexpr int ST_IH = ST_TH + 2 * ST_R;  // 64 input rows
+constexpr int ST_IP = 49;                // input pitch (== 17 mod 32: conflict-free H-pass reads)
+constexpr int ST_HP = 33;                // H-pass output pitch (conflict-free H-pass stores)
+constexpr int ST_IPLANE = ST_IH * ST_IP;
+constexpr int ST_HPLANE = ST_IH * ST_HP;
+constexpr int kStatsSmem = (5 * ST_IPLANE + 5 * ST_HPLANE) * 4;
+
+__device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
+    // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
+    const int beg = max(0, pos - 8) - (pos - 8);
+    const int end = min(extent, pos + 9) - (pos - 8);
+    return 1.0f / (c_s2_I[end] - c_s2_I[beg]);
+}
+
+__global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __restrict__ pyr,
+                                                              float* __restrict__ partials, Ssimu2Geom g) {
+    extern __shared__ float sm[];
+    float* inq = sm;                   // [5][64][49]: I1, I2, I1^2, I2^2, I1*I2
+    float* hb = sm + 5 * ST_IPLANE;    // [5][64][33]: horizontal pass
+    const int pair = blockIdx.y;
+    const int t = blockIdx.x;
+    int s = 0;
+#pragma unroll
+    for (int k = 1; k < 6; k++) s += (t >= g.tile_begin[k]);
+    const Ssimu2Level L = g.lv[s];
+    const int lt = t - g.tile_begin[s];
+    const int tx0 = (lt % L.tiles_x) * ST_TW;
+    const int ty0 = (lt / L.tiles_x) * ST_TH;
+    const float* im1 = pyr + (int64_t)(pair * 2 + 0) * 3 * g.plane_elems + L.off;
+    const float* im2 = pyr + (int64_t)(pair * 2 + 1) * 3 * g.plane_elems + L.off;
+    const int tid = threadIdx.x;
+
+    // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7
+    const int hr = tid >> 2, hg = tid & 3;
+    float rx[8];
+#pragma unroll
+    for (int o = 0; o < 8; o++) rx[o] = s2_inv_mass(tx0 + 8 * hg + o, L.w);
+    // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5
+    const int vc = tid & 31, vg = tid >> 5;
+    float ry[6];
+#pragma unroll
+    for (int o = 0; o < 6; o++) ry[o] = s2_inv_mass(ty0 + 6 * vg + o, L.h);
+
+    float acc[18];
+#pragma unroll
+    for (int i = 0; i < 18; i++) acc[i] = 0.f;
+
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const float* p1 = im1 + (int64_t)c * g.plane_elems;
+        const float* p2 = im2 + (int64_t)c * g.plane_elems;
+        for (int e = tid; e < ST_IH * ST_IW; e += 256) {
+            const int r = e / ST_IW, col = e - r * ST_IW;
+            const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
+            float a = 0.f, b = 0.f;
+            if (gx >= 0 && gx < L.w && gy >= 0 && gy < L.h) {
+                const int64_t o = (int64_t)gy * L.pitch + gx;
+                a = __ldg(p1 + o);
+                b = __ldg(p2 + o);
+            }
+            const int so = r * ST_IP + col;
+            inq[so] = a;
+            inq[ST_IPLANE + so] = b;
+            inq[2 * ST_IPLANE + so] = a * a;
+            inq[3 * ST_IPLANE + so] = b * b;
+            inq[4 * ST_IPLANE + so] = a * b;
+        }
+        __syncthreads();
+        // horizontal 17-tap pass for the five moments over all 64 rows
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            const float* row = inq + q * ST_IPLANE + hr * ST_IP + 8 * hg;
+            float v[24];
+#pragma unroll
+            for (int j = 0; j < 24; j++) v[j] = row[j];
+            float* dst = hb + q * ST_HPLANE + hr * ST_HP + 8 * hg;
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                float a = 0.f;
+#pragma unroll
+                for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_s2_k[i], a);
+                dst[o] = a * rx[o];
+            }
+        }
+        __syncthreads();
+        // vertical pass + maps
+        float m[5][6];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            const float* col = hb + q * ST_HPLANE + (6 * vg) * ST_HP + vc;
+            float v[22];
+#pragma unroll
+            for (int j = 0; j < 22; j++) v[j] = col[j * ST_HP];
+#pragma unroll
+            for (int o = 0; o < 6; o++) {
+                float a = 0.f;
+#pragma unroll
+                for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_s2_k[i], a);
+                m[q][o] = a * ry[o];
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < 6; o++) {
+            const int y = ty0 + 6 * vg + o, x = tx0 + vc;
+            if (x < L.w && y < L.h) {
+                const int so = (6 * vg + o + ST_R) * ST_IP + vc + ST_R;
+                const float i1 = inq[so], i2 = inq[ST_IPLANE + so];
+                const float m1 = m[0][o], m2 = m[1][o];
+                const float m11 = m1 * m1, m22 = m2 * m2, m12 = m1 * m2, md = m1 - m2;
+                const float num_m = fmaf(md, -md, 1.0f);
+                const float num_s = fmaf(m[4][o] - m12, 2.0f, 0.0009f);
+                const float denom = (m[2][o] - m11) + (m[3][o] - m22) + 0.0009f;
+                const float d0 = fmaxf(1.0f - (num_m * num_s) / denom, 0.0f);
+                const float v1 = (fabsf(i2 - m2) + 1.0f) / (fabsf(i1 - m1) + 1.0f) - 1.0f;
+                const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
+                const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
+                acc[0 * 3 + c] += d0;
+                acc[1 * 3 + c] += q0 * q0;
+                acc[2 * 3 + c] += d1;
+                acc[3 * 3 + c] += q1 * q1;
+                acc[4 * 3 + c] += d2;
+                acc[5 * 3 + c] += q2 * q2;
+            }
+        }
+        __syncthreads();
+    }
+    // block reduction of the 18 pools
+    float* red = sm;  // reuse: [8 warps][18]
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int i = 0; i < 18; i++) {
+        float v = warp_sum(acc[i]);
+        if (lane == 0) red[warp * 18 + i] = v;
+    }
+    __syncthreads();
+    if (tid < 18) {
+        float v = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; w++) v += red[w * 18 + tid];
+        partials[((int64_t)pair * g.tiles_total + t) * 18 + tid] = v;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Kernel 3: FP64 finalisation, one CTA per pair.
+__global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __restrict__ partials,
+                                                              double* __restrict__ scores, Ssimu2Geom g) {
+    __shared__ double red[8][18];
+    __shared__ double pooled[6][18];
+    const int pair = blockIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int s = 0; s < 6; s++) {
+        double acc[18];
+#pragma unroll
+        for (int i = 0; i < 18; i++) acc[i] = 0.0;
+        for (int t = g.tile_begin[s] + tid; t < g.tile_begin[s + 1]; t += 256) {
+            const float* p = partials + ((int64_t)pair * g.tiles_total + t) * 18;
+#pragma unroll
+            for (int i = 0; i < 18; i++) acc[i] += (double)p[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 18; i++) {
+            double v = warp_sum(acc[i]);
+            if (lane == 0) red[warp][i] = v;
+        }
+        __syncthreads();
+        if (tid < 18) {
+            double v = 0.0;
+            for (int w = 0; w < 8; w++) v += red[w][tid];
+            pooled[s][tid] = v / ((double)g.lv[s].w * (double)g.lv[s].h);
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        // pooled[s][pool*3 + channel], pool = map*2 + norm (map: ssim, artifact, detail)
+        double ssim = 0.0;
+        for (int plane = 0; plane < 3; plane++)
+            for (int s = 0; s < 6; s++)
+                for (int n = 0; n < 2; n++)
+                    for (int i = 0; i < 3; i++) {
+                        double v = pooled[s][(i * 2 + n) * 3 + plane];
+                        if (n == 1) v = sqrt(sqrt(v));
+                        ssim = fma(c_s2_w[plane * 36 + s * 6 + n * 3 + i], v, ssim);
+                    }
+        ssim *= 0.9562382616834844;
+        ssim = (6.248496625763138e-5 * ssim * ssim) * ssim + 2.326765642916932 * ssim -
+               0.020884521182843837 * ssim * ssim;
+        scores[pair] = ssim > 0.0 ? pow(ssim, 0.6276336467831387) * -10.0 + 100.0 : 100.0;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host side
+
+Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h) {
+    Ssimu2Geom g{};
+    int64_t off = 0;
+    int tiles = 0;
+    int64_t cw = w, ch = h;
+    for (int s = 0; s < 6; s++) {
+        Ssimu2Level& L = g.lv[s];
+        L.w = (int)cw;
+        L.h = (int)ch;
+        L.pitch = (int)round_up(cw, 8);
+        L.off = off;
+        off += round_up((int64_t)L.pitch * ch, 64);
+        L.tiles_x = (int)ceil_div(cw, ST_TW);
+        L.tiles_y = (int)ceil_div(ch, ST_TH);
+        g.tile_begin[s] = tiles;
+        tiles += L.tiles_x * L.tiles_y;
+        cw = half_dim(cw);
+        ch = half_dim(ch);
+    }
+    g.tile_begin[6] = tiles;
+    g.tiles_total = tiles;
+    g.plane_elems = off;
+    return g;
+}
+
+int Ssimu2Engine::init(int64_t width, int64_t height, int max_pairs_) {
+    w = width;
+    h = height;
+    max_pairs = max_pairs_;
+    geom = make_ssimu2_geom(w, h);
+    int rc = upload_constants_once();
+    if (rc) return rc;
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStatsSmem));
+    VSHIP_CUDA_TRY(cudaMalloc(&pyr, sizeof(float) * (size_t)geom.plane_elems * 3 * 2 * max_pairs));
+    VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * (size_t)geom.tiles_total * 18 * max_pairs));
+    VSHIP_CUDA_TRY(cudaMalloc(&scores, sizeof(double) * max_pairs));
+    return E_OK;
+}
+
+void Ssimu2Engine::destroy() {
+    if (pyr) cudaFree(pyr);
+    if (partials) cudaFree(partials);
+    if (scores) cudaFree(scores);
+    pyr = nullptr;
+    partials = nullptr;
+    scores = nullptr;
+}
+
+size_t Ssimu2Engine::device_bytes(int64_t w, int64_t h, int pairs) {
+    Ssimu2Geom g = make_ssimu2_geom(w, h);
+    return sizeof(float) * (size_t)g.plane_elems * 6 * pairs + sizeof(float) * (size_t)g.tiles_total * 18 * pairs +
+           sizeof(double) * pairs;
+}
+
+int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st) {
+    if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
+    dim3 g1((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), (unsigned)(2 * npairs));
+    {
+    ProfScope ps("ssimu2_pyramid", st);
+    switch (intype) {
+        case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
+        case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
+        case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
+        default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
+    }
+    }
+    dim3 g2((unsigned)geom.tiles_total, (unsigned)npairs);
+    {
+        ProfScope ps("ssimu2_stats", st);
+        ssimu2_stats_kernel<<<g2, 256, kStatsSmem, st>>>(pyr, partials, geom);
+    }
+    {
+        ProfScope ps("ssimu2_finalize", st);
+        ssimu2_finalize_kernel<<<npairs, 256, 0, st>>>(partials, out_scores ? out_scores : scores, geom);
+    }
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    return E_OK;
+}
+
+}  // namespace vship

@@ -1,0 +1,48 @@
+// ssimu2.h -- SSIMULACRA2 engine (host interface of ssimu2.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace vship {
+
+struct FrameDesc;
+
+// One pyramid level in device memory: planar FP32, rows padded to `pitch` floats.
+struct Ssimu2Level {
+    int w, h, pitch;
+    int tiles_x, tiles_y;
+    int64_t off;  // element offset of the level inside one channel plane
+};
+
+// Geometry of the 6-scale pyramid and of the stats-kernel tiling (32x48 output tiles).
+struct Ssimu2Geom {
+    Ssimu2Level lv[6];
+    int tile_begin[7];
+    int tiles_total;
+    int64_t plane_elems;  // elements of one channel's whole pyramid
+};
+
+Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h);
+
+// Device workspace and launch sequence for up to `max_pairs` frame pairs of one resolution.
+// Layout: pyr[pair][image][channel][plane_elems], partials[pair][tile][18], scores[pair].
+class Ssimu2Engine {
+public:
+    int64_t w = 0, h = 0;
+    int max_pairs = 0;
+    Ssimu2Geom geom{};
+    float* pyr = nullptr;
+    float* partials = nullptr;
+    double* scores = nullptr;
+
+    int init(int64_t width, int64_t height, int max_pairs);
+    void destroy();
+    // frames_dev: 2*npairs FrameDesc in device memory (pair-major: reference, distorted).
+    // Scores land in out_scores (device) or in this->scores when out_scores is null.
+    int launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st);
+    static size_t device_bytes(int64_t w, int64_t h, int pairs);
+};
+
+}  // namespace vship

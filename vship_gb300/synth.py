@@ -1,0 +1,184 @@
+"""Seeded synthetic frame pairs for the parity tests and the benchmark.
+
+No dataset is available offline, so these stand in for real video with the shapes and value
+distributions of the benchmark configurations:
+
+* ``rgb24_pair``       -- 8-bit RGB: per channel a sum of 8 sinusoidal gratings (orientation
+                          U[0, pi), period U[4, 64] px, amplitude U[10, 40]) plus U[-8, 8] noise,
+                          centred at 128, clipped and rounded; distorted = reference + N(0, 4).
+* ``yuv420p10_frames`` -- 10-bit 4:2:0 limited-range Y'CbCr built from the same grating model
+                          (luma x4 for 10 bits, chroma at half resolution), with a per-frame phase
+                          drift of 0.05 rad; distortions are 8x8 block-DCT quantisation (step
+                          U[4, 32], chroma step x2) or a Gaussian blur (sigma U[0.5, 2]) followed by
+                          Gaussian noise (sigma U[1, 6]).
+* ``yuv420p10_to_rgb`` -- the BT.709 conversion used to feed RGB planes to the scorers: limited ->
+                          full range, bilinear chroma upsampling with MPEG-2 (left) siting, BT.709
+                          matrix, gamma-encoded R'G'B' in [0, 1].
+
+Scalar draws come from numpy's seeded generator (identical on every host); per-pixel noise comes
+from a torch generator on the requested device, so CPU and GPU draws differ. Every consumer that
+compares two implementations hands both the same arrays.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+
+def _gratings(h: int, w: int, rs: np.random.Generator, n: int, amp_scale: float, phase: float,
+              device, out: torch.Tensor | None = None) -> torch.Tensor:
+    """Sum of n sinusoidal gratings evaluated with separable outer products (float64)."""
+    xs = torch.arange(w, device=device, dtype=torch.float64)
+    ys = torch.arange(h, device=device, dtype=torch.float64)
+    acc = torch.zeros((h, w), device=device, dtype=torch.float64) if out is None else out
+    for _ in range(n):
+        theta = rs.uniform(0.0, math.pi)
+        period = rs.uniform(4.0, 64.0)
+        amp = rs.uniform(10.0, 40.0) * amp_scale
+        phi = rs.uniform(0.0, 2 * math.pi) + phase
+        k = 2 * math.pi / period
+        ax = k * math.cos(theta) * xs
+        by = k * math.sin(theta) * ys + phi
+        acc += amp * (torch.outer(torch.cos(by), torch.sin(ax)) + torch.outer(torch.sin(by), torch.cos(ax)))
+    return acc
+
+
+def rgb24_pair(h: int = 256, w: int = 256, seed: int = 1, device="cpu"):
+    """One 8-bit RGB reference/distorted pair, each a (3, h, w) uint8 tensor."""
+    rs = np.random.default_rng(seed)
+    gen = torch.Generator(device=device).manual_seed(seed)
+    ref = torch.empty((3, h, w), dtype=torch.uint8, device=device)
+    dist = torch.empty_like(ref)
+    for c in range(3):
+        v = _gratings(h, w, rs, 8, 1.0, 0.0, device)
+        v += (torch.rand((h, w), generator=gen, device=device, dtype=torch.float64) * 16.0 - 8.0)
+        r = torch.clamp(torch.round(v + 128.0), 0, 255)
+        ref[c] = r.to(torch.uint8)
+        d = torch.clamp(torch.round(r + 4.0 * torch.randn((h, w), generator=gen, device=device, dtype=torch.float64)),
+                        0, 255)
+        dist[c] = d.to(torch.uint8)
+    return ref, dist
+
+
+# ------------------------------------------------------------------------------------------
+# YUV 4:2:0, 10-bit
+
+def _dct_matrix(n: int = 8, device="cpu") -> torch.Tensor:
+    k = torch.arange(n, dtype=torch.float64, device=device)
+    m = torch.cos(math.pi * (2 * k[None, :] + 1) * k[:, None] / (2 * n)) * math.sqrt(2.0 / n)
+    m[0] /= math.sqrt(2.0)
+    return m  # orthonormal DCT-II rows
+
+
+def block_dct_quantise(plane: torch.Tensor, step: float, lo: int, hi: int) -> torch.Tensor:
+    """8x8 block DCT, uniform quantisation of every coefficient with `step`, inverse DCT,
+    rounding and clipping to [lo, hi]. Edges are padded by replication to a multiple of 8."""
+    h, w = plane.shape
+    ph, pw = (-h) % 8, (-w) % 8
+    x = plane.to(torch.float64)
+    if ph or pw:
+        x = torch.nn.functional.pad(x[None, None], (0, pw, 0, ph), mode="replicate")[0, 0]
+    H, W = x.shape
+    D = _dct_matrix(8, x.device)
+    blocks = x.reshape(H // 8, 8, W // 8, 8).permute(0, 2, 1, 3)
+    coef = D @ blocks @ D.T
+    coef = torch.round(coef / step) * step
+    rec = (D.T @ coef @ D).permute(0, 2, 1, 3).reshape(H, W)[:h, :w]
+    return torch.clamp(torch.round(rec), lo, hi).to(torch.int32)
+
+
+def gaussian_blur_noise(plane: torch.Tensor, sigma: float, noise_sigma: float, lo: int, hi: int,
+                        gen: torch.Generator) -> torch.Tensor:
+    """Separable Gaussian blur (radius ceil(3 sigma), edge replication) then N(0, noise_sigma)."""
+    x = plane.to(torch.float64)[None, None]
+    r = max(1, int(math.ceil(3 * sigma)))
+    t = torch.arange(-r, r + 1, dtype=torch.float64, device=x.device)
+    k = torch.exp(-t * t / (2 * sigma * sigma))
+    k /= k.sum()
+    x = torch.nn.functional.pad(x, (r, r, 0, 0), mode="replicate")
+    x = torch.nn.functional.conv2d(x, k.view(1, 1, 1, -1))
+    x = torch.nn.functional.pad(x, (0, 0, r, r), mode="replicate")
+    x = torch.nn.functional.conv2d(x, k.view(1, 1, -1, 1))[0, 0]
+    x = x + noise_sigma * torch.randn(x.shape, generator=gen, device=x.device, dtype=torch.float64)
+    return torch.clamp(torch.round(x), lo, hi).to(torch.int32)
+
+
+def yuv420p10_source(h: int, w: int, t: int, seed: int, device="cpu"):
+    """Reference frame t of a sequence: (Y, Cb, Cr) int32 tensors, limited range."""
+    rs = np.random.default_rng(seed)  # same gratings for every frame; only the phase drifts
+    gen = torch.Generator(device=device).manual_seed(seed * 100003 + t)
+    phase = 0.05 * t
+    y = _gratings(h, w, rs, 8, 4.0, phase, device)
+    y += torch.rand((h, w), generator=gen, device=device, dtype=torch.float64) * 64.0 - 32.0
+    Y = torch.clamp(torch.round(y + 502.0), 64, 940).to(torch.int32)
+    ch, cw = (h + 1) // 2, (w + 1) // 2
+    out = [Y]
+    for _ in range(2):
+        c = _gratings(ch, cw, rs, 8, 2.0, phase, device)
+        c += torch.rand((ch, cw), generator=gen, device=device, dtype=torch.float64) * 32.0 - 16.0
+        out.append(torch.clamp(torch.round(c + 512.0), 64, 960).to(torch.int32))
+    return tuple(out)
+
+
+def yuv420p10_frames(h: int, w: int, t: int, seed: int = 7, distortion: str = "dct", device="cpu"):
+    """(reference, distorted) YUV 4:2:0 10-bit frames for pair t of a sequence."""
+    src = yuv420p10_source(h, w, t, seed, device)
+    rs = np.random.default_rng([seed, t, 1])
+    gen = torch.Generator(device=device).manual_seed(seed * 7919 + t)
+    if distortion == "dct":
+        step = rs.uniform(4.0, 32.0)
+        dist = (block_dct_quantise(src[0], step, 64, 940),
+                block_dct_quantise(src[1], 2 * step, 64, 960),
+                block_dct_quantise(src[2], 2 * step, 64, 960))
+    elif distortion == "blur_noise":
+        sigma = rs.uniform(0.5, 2.0)
+        ns = rs.uniform(1.0, 6.0)
+        dist = (gaussian_blur_noise(src[0], sigma, ns, 64, 940, gen),
+                gaussian_blur_noise(src[1], sigma, ns, 64, 960, gen),
+                gaussian_blur_noise(src[2], sigma, ns, 64, 960, gen))
+    else:
+        raise ValueError(distortion)
+    return src, dist
+
+
+def _upsample_chroma(c: torch.Tensor, h: int, w: int) -> torch.Tensor:
+    """Bilinear 2x upsampling with MPEG-2 siting: chroma sample i sits on luma column 2i and
+    halfway between luma rows 2j and 2j+1. Edge samples are clamped."""
+    ch, cw = c.shape
+    xs = torch.arange(w, dtype=torch.float64, device=c.device) / 2.0
+    ys = (torch.arange(h, dtype=torch.float64, device=c.device) - 0.5) / 2.0
+    x0 = torch.clamp(torch.floor(xs), 0, cw - 1).long()
+    x1 = torch.clamp(x0 + 1, max=cw - 1)
+    fx = torch.clamp(xs - x0.to(torch.float64), 0.0, 1.0)
+    y0f = torch.floor(ys)
+    fy = ys - y0f
+    y0 = torch.clamp(y0f, 0, ch - 1).long()
+    y1 = torch.clamp(y0f + 1, 0, ch - 1).long()
+    cf = c.to(torch.float64)
+    top = cf[y0][:, x0] * (1 - fx) + cf[y0][:, x1] * fx
+    bot = cf[y1][:, x0] * (1 - fx) + cf[y1][:, x1] * fx
+    return top * (1 - fy)[:, None] + bot * fy[:, None]
+
+
+def yuv420p10_to_rgb(yuv, dtype=torch.float32) -> torch.Tensor:
+    """BT.709 limited-range 10-bit 4:2:0 -> full-range gamma-encoded R'G'B' (3, h, w) in [0, 1]."""
+    Y, U, V = yuv
+    h, w = Y.shape
+    y = (Y.to(torch.float64) - 64.0) / 876.0
+    cb = (_upsample_chroma(U, h, w) - 512.0) / 896.0
+    cr = (_upsample_chroma(V, h, w) - 512.0) / 896.0
+    kr, kb = 0.2126, 0.0722
+    kg = 1.0 - kr - kb
+    r = y + 2.0 * (1.0 - kr) * cr
+    b = y + 2.0 * (1.0 - kb) * cb
+    g = y - (2.0 * (1.0 - kb) * kb / kg) * cb - (2.0 * (1.0 - kr) * kr / kg) * cr
+    rgb = torch.stack([r, g, b]).clamp_(0.0, 1.0)
+    return rgb.to(dtype)
+
+
+def rgb_float_pair(h: int, w: int, t: int, seed: int = 7, distortion: str = "dct", device="cpu"):
+    """Float32 (3, h, w) R'G'B' reference/distorted planes for pair t of a YUV sequence."""
+    ref, dist = yuv420p10_frames(h, w, t, seed, distortion, device)
+    return yuv420p10_to_rgb(ref), yuv420p10_to_rgb(dist)
