@@ -221,7 +221,8 @@ EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytes(int width, int height, in
 /* Instrumentation: when enabled, every kernel launch is bracketed by CUDA events on its stream.
  * Vship_ProfileReport synchronises those events and writes a JSON object
  * {"kernel": [launches, total_ms], ...} (same size/truncation contract as
- * Vship_GetErrorMessage), then clears the records. Off by default. */
+ * Vship_GetErrorMessage); a call with len > 0 also clears the records, a size query (len == 0)
+ * does not. Off by default. */
 EXPORTPREPROCESS void Vship_ProfileSetEnabled(int enabled);
 EXPORTPREPROCESS int Vship_ProfileReport(char* out_json, int len);
 

@@ -148,8 +148,7 @@ def profile_report() -> dict:
     """{kernel: (launches, total_ms)} since the last report; synchronises the recorded events."""
     import json
     L = lib()
-    n = L.Vship_ProfileReport(None, 0)
-    buf = ctypes.create_string_buffer(n + 4096)
+    buf = ctypes.create_string_buffer(1 << 20)  # one call: a report clears the records
     L.Vship_ProfileReport(buf, len(buf))
     return {k: (int(v[0]), float(v[1])) for k, v in json.loads(buf.value.decode() or "{}").items()}
 

@@ -52,9 +52,11 @@ void prof_end(int token, cudaStream_t st) {
     if (token < (int)g_recs.size()) cudaEventRecord(g_recs[token].b, st);
 }
 
-// JSON object {"kernel": [launches, total_ms], ...}; clears the records.
+// JSON object {"kernel": [launches, total_ms], ...}. A call with a buffer (len > 0) also clears
+// the records; a size query (len == 0) leaves them in place.
 int prof_report(char* buf, int len) {
     std::map<std::string, std::pair<long, double>> agg;
+    const bool consume = buf && len > 0;
     {
         std::lock_guard<std::mutex> g(g_mu);
         for (Rec& r : g_recs) {
@@ -65,10 +67,14 @@ int prof_report(char* buf, int len) {
                 e.first += 1;
                 e.second += ms;
             }
-            g_pool.push_back(r.a);
-            g_pool.push_back(r.b);
         }
-        g_recs.clear();
+        if (consume) {
+            for (Rec& r : g_recs) {
+                g_pool.push_back(r.a);
+                g_pool.push_back(r.b);
+            }
+            g_recs.clear();
+        }
     }
     std::string s = "{";
     bool first = true;
@@ -80,7 +86,7 @@ int prof_report(char* buf, int len) {
         first = false;
     }
     s += "}";
-    if (buf && len > 0) {
+    if (consume) {
         int n = (int)s.size() < len - 1 ? (int)s.size() : len - 1;
         for (int i = 0; i < n; i++) buf[i] = s[i];
         buf[n] = 0;

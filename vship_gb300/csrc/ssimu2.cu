@@ -171,14 +171,22 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
 // ------------------------------------------------------------------------------------------
 // Kernel 2: fused 5-moment blur + SSIM/edge maps + per-CTA pooling, all scales in one launch.
 // grid (tiles_total, npairs), 256 threads, dynamic smem kStatsSmem.
+//
+// Per CTA: one 32x48 output tile of one scale. For each channel the raw I1 and I2 tiles with an
+// 8-px halo (64 rows x 48 columns) are staged with cp.async (bytes outside the image are
+// zero-filled), double-buffered so channel c+1 streams in while channel c computes. The
+// horizontal pass reads the raw rows as float4 (row pitch 52 floats: the 8 lanes of each
+// quarter-warp phase hit distinct bank quads), forms the shifted samples and their products in
+// registers and scatters them into 8 outputs x 5 moments; the vertical pass gathers 22 rows per
+// thread and evaluates the maps.
 constexpr int ST_TW = 32, ST_TH = 48, ST_R = 8;
 constexpr int ST_IW = ST_TW + 2 * ST_R;  // 48 input columns
 constexpr int ST_IH = ST_TH + 2 * ST_R;  // 64 input rows
-constexpr int ST_IP = 49;                // input pitch (== 17 mod 32: conflict-free H-pass reads)
-constexpr int ST_HP = 33;                // H-pass output pitch (conflict-free H-pass stores)
-constexpr int ST_IPLANE = ST_IH * ST_IP;
+constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte multiple, 13 quads)
+constexpr int ST_HP = 33;                // horizontal-pass output pitch
+constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
 constexpr int ST_HPLANE = ST_IH * ST_HP;
-constexpr int kStatsSmem = (5 * ST_IPLANE + 5 * ST_HPLANE) * 4;
+constexpr int kStatsSmem = (2 * 2 * ST_RAW + 5 * ST_HPLANE) * 4;  // 2 stages x 2 images + 5 moments
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
@@ -187,11 +195,42 @@ __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     return 1.0f / (c_s2_I[end] - c_s2_I[beg]);
 }
 
+__device__ __forceinline__ void cp_async16(float* smem, const float* gmem, int src_bytes) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Stage the 64x48 halo tile of one plane: 768 16-byte chunks, 3 per thread. The tile's first
+// column (tile x - 8) is a multiple of 4 floats and every row starts 32-byte aligned, so each
+// chunk is either fully outside the image, fully inside, or cut by the right edge (partial
+// source size, the rest zero-filled).
+__device__ __forceinline__ void stage_tile(float* dst, const float* __restrict__ plane, int pitch, int w, int h,
+                                           int x0, int y0) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int ch = threadIdx.x + 256 * k;  // 0..767
+        const int r = ch / 12, q = ch - r * 12;
+        const int gx = x0 - ST_R + 4 * q, gy = y0 - ST_R + r;
+        int bytes = 0;
+        const float* src = plane;
+        if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
+            bytes = min(w - gx, 4) * 4;
+            src = plane + (int64_t)gy * pitch + gx;
+        }
+        cp_async16(dst + r * ST_RP + 4 * q, src, bytes);
+    }
+}
+
 __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __restrict__ pyr,
                                                               float* __restrict__ partials, Ssimu2Geom g) {
-    extern __shared__ float sm[];
-    float* inq = sm;                   // [5][64][49]: I1, I2, I1^2, I2^2, I1*I2
-    float* hb = sm + 5 * ST_IPLANE;    // [5][64][33]: horizontal pass
+    extern __shared__ __align__(16) float sm[];
+    float* raw = sm;                   // [stage][image][64][52]
+    float* hb = sm + 4 * ST_RAW;       // [5][64][33]
     const int pair = blockIdx.y;
     const int t = blockIdx.x;
     int s = 0;
@@ -204,12 +243,22 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
     const float* im1 = pyr + (int64_t)(pair * 2 + 0) * 3 * g.plane_elems + L.off;
     const float* im2 = pyr + (int64_t)(pair * 2 + 1) * 3 * g.plane_elems + L.off;
     const int tid = threadIdx.x;
+    const bool interior = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h;
 
-    // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7
+    // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23)
     const int hr = tid >> 2, hg = tid & 3;
     float rx[8];
 #pragma unroll
     for (int o = 0; o < 8; o++) rx[o] = s2_inv_mass(tx0 + 8 * hg + o, L.w);
+    const int hgy = ty0 - ST_R + hr;
+    const bool hrow_ok = hgy >= 0 && hgy < L.h;
+    unsigned colmask = 0;  // bit j: input column 8*hg + j lies inside the image
+#pragma unroll
+    for (int j = 0; j < 24; j++) {
+        const int gx = tx0 - ST_R + 8 * hg + j;
+        colmask |= (unsigned)(gx >= 0 && gx < L.w) << j;
+    }
+    if (!hrow_ok) colmask = 0;
     // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5
     const int vc = tid & 31, vg = tid >> 5;
     float ry[6];
@@ -220,41 +269,71 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
 #pragma unroll
     for (int i = 0; i < 18; i++) acc[i] = 0.f;
 
+    stage_tile(raw, im1, L.pitch, L.w, L.h, tx0, ty0);
+    stage_tile(raw + ST_RAW, im2, L.pitch, L.w, L.h, tx0, ty0);
+    cp_async_commit();
+
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        const float* p1 = im1 + (int64_t)c * g.plane_elems;
-        const float* p2 = im2 + (int64_t)c * g.plane_elems;
-        for (int e = tid; e < ST_IH * ST_IW; e += 256) {
-            const int r = e / ST_IW, col = e - r * ST_IW;
-            const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
-            float a = 0.f, b = 0.f;
-            if (gx >= 0 && gx < L.w && gy >= 0 && gy < L.h) {
-                const int64_t o = (int64_t)gy * L.pitch + gx;
-                a = __ldg(p1 + o);
-                b = __ldg(p2 + o);
-            }
-            const int so = r * ST_IP + col;
-            inq[so] = a;
-            inq[ST_IPLANE + so] = b;
-            inq[2 * ST_IPLANE + so] = a * a;
-            inq[3 * ST_IPLANE + so] = b * b;
-            inq[4 * ST_IPLANE + so] = a * b;
+        const float* r1 = raw + (c & 1) * 2 * ST_RAW;
+        const float* r2 = r1 + ST_RAW;
+        if (c < 2) {
+            float* n1 = raw + ((c + 1) & 1) * 2 * ST_RAW;
+            stage_tile(n1, im1 + (int64_t)(c + 1) * g.plane_elems, L.pitch, L.w, L.h, tx0, ty0);
+            stage_tile(n1 + ST_RAW, im2 + (int64_t)(c + 1) * g.plane_elems, L.pitch, L.w, L.h, tx0, ty0);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-        // horizontal 17-tap pass for the five moments over all 64 rows
+        // Moments are formed on values shifted by one per-tile constant (the reference image's
+        // value at the tile origin). The blur is normalised, so sigma = E[(x-s)^2] - (E[x]-s)^2
+        // is unchanged, while the FP32 cancellation of E[x^2] - E[x]^2 shrinks by the square of
+        // |x| / |x - s|. Out-of-image samples stay exactly zero (they carry no kernel mass).
+        const float shift = r1[ST_R * ST_RP + ST_R];
+        {
+            float h[5][8];
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-            const float* row = inq + q * ST_IPLANE + hr * ST_IP + 8 * hg;
-            float v[24];
+            for (int q = 0; q < 5; q++)
 #pragma unroll
-            for (int j = 0; j < 24; j++) v[j] = row[j];
-            float* dst = hb + q * ST_HPLANE + hr * ST_HP + 8 * hg;
+                for (int o = 0; o < 8; o++) h[q][o] = 0.f;
+            const float* ra = r1 + hr * ST_RP + 8 * hg;
+            const float* rb = r2 + hr * ST_RP + 8 * hg;
 #pragma unroll
-            for (int o = 0; o < 8; o++) {
-                float a = 0.f;
+            for (int j4 = 0; j4 < 6; j4++) {
+                const float4 va = *reinterpret_cast<const float4*>(ra + 4 * j4);
+                const float4 vb = *reinterpret_cast<const float4*>(rb + 4 * j4);
+                const float la[4] = {va.x, va.y, va.z, va.w};
+                const float lb[4] = {vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
-                for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_s2_k[i], a);
-                dst[o] = a * rx[o];
+                for (int u = 0; u < 4; u++) {
+                    const int j = 4 * j4 + u;
+                    float a = la[u] - shift, b = lb[u] - shift;
+                    if (!interior && !((colmask >> j) & 1u)) {
+                        a = 0.f;
+                        b = 0.f;
+                    }
+                    const float aa = a * a, bb = b * b, ab = a * b;
+#pragma unroll
+                    for (int o = 0; o < 8; o++) {
+                        const int i = j - o;  // tap index
+                        if (i >= 0 && i < 17) {
+                            const float k = c_s2_k[i];
+                            h[0][o] = fmaf(a, k, h[0][o]);
+                            h[1][o] = fmaf(b, k, h[1][o]);
+                            h[2][o] = fmaf(aa, k, h[2][o]);
+                            h[3][o] = fmaf(bb, k, h[3][o]);
+                            h[4][o] = fmaf(ab, k, h[4][o]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 5; q++) {
+                float* dst = hb + q * ST_HPLANE + hr * ST_HP + 8 * hg;
+#pragma unroll
+                for (int o = 0; o < 8; o++) dst[o] = h[q][o] * rx[o];
             }
         }
         __syncthreads();
@@ -278,14 +357,20 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
         for (int o = 0; o < 6; o++) {
             const int y = ty0 + 6 * vg + o, x = tx0 + vc;
             if (x < L.w && y < L.h) {
-                const int so = (6 * vg + o + ST_R) * ST_IP + vc + ST_R;
-                const float i1 = inq[so], i2 = inq[ST_IPLANE + so];
-                const float m1 = m[0][o], m2 = m[1][o];
-                const float m11 = m1 * m1, m22 = m2 * m2, m12 = m1 * m2, md = m1 - m2;
+                const int so = (6 * vg + o + ST_R) * ST_RP + vc + ST_R;
+                const float i1 = r1[so] - shift, i2 = r2[so] - shift;  // shifted samples
+                const float m1 = m[0][o], m2 = m[1][o];                 // shifted means
+                // ssim map (score.hpp:141-148); explicit fma so identical inputs give bitwise
+                // identical numerator and denominator whatever the compiler contracts
+                const float md = m1 - m2;
                 const float num_m = fmaf(md, -md, 1.0f);
-                const float num_s = fmaf(m[4][o] - m12, 2.0f, 0.0009f);
-                const float denom = (m[2][o] - m11) + (m[3][o] - m22) + 0.0009f;
+                const float s12 = fmaf(-m1, m2, m[4][o]);
+                const float s11 = fmaf(-m1, m1, m[2][o]);
+                const float s22 = fmaf(-m2, m2, m[3][o]);
+                const float num_s = fmaf(s12, 2.0f, 0.0009f);
+                const float denom = (s11 + s22) + 0.0009f;
                 const float d0 = fmaxf(1.0f - (num_m * num_s) / denom, 0.0f);
+                // edge maps (score.hpp:151-153): |I - mu| is shift-invariant
                 const float v1 = (fabsf(i2 - m2) + 1.0f) / (fabsf(i1 - m1) + 1.0f) - 1.0f;
                 const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
                 const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
