@@ -377,8 +377,8 @@ def bench_workload(v, kind, args, ws, rank):
                      "traffic": traffic * pairs_per_launch if traffic is not None else None,
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_s * 1e3},
         "pipeline_bytes_per_pair": ssimu2_pair_bytes(w, h) if kind == "ssimu2" else butter_pair_bytes(w, h),
-        "kernel_share": {k: round(t / total_kernel_ms, 4) for k, t in sorted(prof.items(), key=lambda x: -x[1][1])}
-        if total_kernel_ms > 0 else {},
+        "kernel_share": {k: {"launches": n, "ms": round(t, 3), "share": round(t / total_kernel_ms, 4)}
+                         for k, (n, t) in sorted(prof.items(), key=lambda x: -x[1][1])} if total_kernel_ms > 0 else {},
         "gpu_launches": launches,
         "clocks": clocks,
         "score_check": {"device_vs_e2e_max_abs": float(abs(
