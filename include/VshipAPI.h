@@ -218,6 +218,29 @@ EXPORTPREPROCESS Vship_Exception Vship_ButteraugliComputeDeviceAsync(Vship_Butte
                                                                      float* distmaps_dev, void* stream);
 EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytes(int width, int height, int max_pairs);
 
+/* SSIMU2 for callers that cannot allocate GPU memory -- no counterpart in the reference.
+ *
+ * Programs that fix their GPU memory budget at start-up (real-time encoders, servers with a
+ * static memory plan) and plugins hosted by a framework that owns the device memory cannot let
+ * a library call cudaMalloc while they run. This entry point allocates nothing: its scratch is
+ * a fixed array of VSHIP_SSIMU2_NOALLOC_SCRATCH_BYTES inside the library's device code, held by
+ * every GPU that loads that code until the process exits. The caller passes the two frames
+ * (device planes), the resolution, the sample type, a device pointer for the score and a
+ * cudaStream_t (NULL = legacy default stream); the call only enqueues work, so synchronise the
+ * stream before reading *score_dev.
+ *
+ * Limit: the two XYB pyramids plus per-tile sums must fit the array; 1280x720 does, larger
+ * frames are refused with Vship_OutOfVRAM before anything is launched.
+ * The first call on a device looks the array up and uploads that device's constant tables;
+ * make it before any stream capture on that device.
+ * All calls on one device share the array: calls whose GPU work overlaps (different streams or
+ * host threads) race, so order them on one stream. */
+#define VSHIP_SSIMU2_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2DeviceNoAlloc(const Vship_DeviceFrame* reference,
+                                                                  const Vship_DeviceFrame* distorted, int width,
+                                                                  int height, Vship_InputType input_type,
+                                                                  double* score_dev, void* stream);
+
 /* Instrumentation: when enabled, every kernel launch is bracketed by CUDA events on its stream.
  * Vship_ProfileReport synchronises those events and writes a JSON object
  * {"kernel": [launches, total_ms], ...} (same size/truncation contract as

@@ -104,6 +104,8 @@ SIGNATURES = {
     "Vship_ButteraugliComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_void_p, ctypes.c_void_p]),
     "Vship_ButteraugliDeviceBytes": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_ComputeSSIMU2DeviceNoAlloc": (_E, [ctypes.POINTER(DeviceFrame), ctypes.POINTER(DeviceFrame), ctypes.c_int,
+                                              ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "Vship_ProfileSetEnabled": (None, [ctypes.c_int]),
     "Vship_ProfileReport": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }

@@ -531,4 +531,41 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
     return E_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// Entry points for callers that provide their own device scratch (used by noalloc.cu).
+
+int ssimu2_prepare_device() {
+    int rc = upload_constants_once();
+    if (rc) return rc;
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStatsSmem));
+    return E_OK;
+}
+
+size_t ssimu2_scratch_floats(const Ssimu2Geom& g) {
+    return (size_t)g.plane_elems * 6 + (size_t)g.tiles_total * 18;
+}
+
+__global__ void ssimu2_store_frames_kernel(FrameDesc a, FrameDesc b, FrameDesc* dst) {
+    dst[0] = a;
+    dst[1] = b;
+}
+
+int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intype, const Ssimu2Geom& geom,
+                          FrameDesc* frames_scratch, float* scratch, double* out_score, cudaStream_t st) {
+    float* pyr = scratch;
+    float* partials = scratch + (size_t)geom.plane_elems * 6;
+    ssimu2_store_frames_kernel<<<1, 1, 0, st>>>(ref, dist, frames_scratch);
+    dim3 g1((unsigned)ceil_div(geom.lv[0].w, 32), (unsigned)ceil_div(geom.lv[0].h, 32), 2u);
+    switch (intype) {
+        case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
+        case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
+        case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
+        default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
+    }
+    ssimu2_stats_kernel<<<dim3((unsigned)geom.tiles_total, 1u), 256, kStatsSmem, st>>>(pyr, partials, geom);
+    ssimu2_finalize_kernel<<<1, 256, 0, st>>>(partials, out_score, geom);
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    return E_OK;
+}
+
 }  // namespace vship

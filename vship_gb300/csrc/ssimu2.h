@@ -45,4 +45,12 @@ public:
     static size_t device_bytes(int64_t w, int64_t h, int pairs);
 };
 
+// For callers that supply the scratch themselves (noalloc.cu): upload this device's constant
+// tables, the number of floats of scratch one pair needs, and the launch sequence for one pair
+// with every intermediate placed in `scratch` and the two frame descriptors in frames_scratch.
+int ssimu2_prepare_device();
+size_t ssimu2_scratch_floats(const Ssimu2Geom& g);
+int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intype, const Ssimu2Geom& geom,
+                          FrameDesc* frames_scratch, float* scratch, double* out_score, cudaStream_t st);
+
 }  // namespace vship
