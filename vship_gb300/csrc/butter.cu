@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
         for (int c = 0; c < 3; c++) {
             float v = 0.f;
             if (gx < F.w && gy < F.h) {
-                v = to_linear(load_sample<IT>(fd.plane[c], fd.stride, gx, gy));
+                v = to_linear_fast(load_sample<IT>(fd.plane[c], fd.stride, gx, gy));
                 bplane(work, g, F, pair, P_LIN + img * 3 + c)[(int64_t)gy * F.p + gx] = v;
             }
             sm[c][ly][tx] = v;
@@ -145,42 +145,45 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
 }
 
 // ------------------------------------------------------------------------------------------
-// 2-D tile blur, radius 8: 32x48 outputs per 256-thread CTA. `in` holds the 64x48 input tile
-// (8-px halo, zero outside the image) with pitch TB_IP; the horizontal pass writes 64x32 values
-// to `hb`; each thread returns the 6 vertical outputs of column (tid & 31), rows 6*(tid>>5)+o.
+// 2-D tile blur, radius 8: 32x48 outputs per 256-thread CTA. The 64x48 input tile (8-px halo,
+// zero outside the image) is staged with cp.async into rows of TB_IP floats; the horizontal pass
+// reads each thread's 24 inputs as six float4 (pitch 52 = 13 quads: the 8 lanes of a
+// quarter-warp phase hit distinct bank quads) and writes 64x32 sums to `hb`; each thread then
+// returns the 6 vertical outputs of column (tid & 31), rows 6*(tid>>5)+o, scaled by the product
+// of both passes' border renormalisations (gaussianblur.hpp:94-186 divides after each pass).
 constexpr int TB_TW = 32, TB_TH = 48, TB_R = 8;
 constexpr int TB_IW = TB_TW + 2 * TB_R, TB_IH = TB_TH + 2 * TB_R;
-constexpr int TB_IP = 49, TB_HP = 33;
-constexpr int TB_SMEM_FLOATS = TB_IH * TB_IP + TB_IH * TB_HP;
+constexpr int TB_IP = 52, TB_HP = 33;
+constexpr int TB_RAW = TB_IH * TB_IP;
+constexpr int TB_HPL = TB_IH * TB_HP;
 
-__device__ __forceinline__ void tile_load_r8(float* in, const float* __restrict__ plane, int pitch, int w, int h,
-                                             int x0, int y0) {
-    for (int e = threadIdx.x; e < TB_IH * TB_IW; e += 256) {
-        const int r = e / TB_IW, col = e - r * TB_IW;
-        const int gx = x0 - TB_R + col, gy = y0 - TB_R + r;
-        float v = 0.f;
-        if (gx >= 0 && gx < w && gy >= 0 && gy < h) v = __ldg(plane + (int64_t)gy * pitch + gx);
-        in[r * TB_IP + col] = v;
-    }
+__device__ __forceinline__ void tile_stage_r8(float* dst, const float* __restrict__ plane, int pitch, int w, int h,
+                                              int x0, int y0) {
+    stage_rows<256>(dst, TB_IP, plane, pitch, w, h, x0 - TB_R, y0 - TB_R, TB_IH, TB_IW / 4);
 }
 
 template <int KI>
-__device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const float rx[8], const float ry[6],
-                                             float out[6]) {
+__device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const float rxy[6], float out[6]) {
     const int tid = threadIdx.x;
     {
         const int hr = tid >> 2, hg = tid & 3;
         const float* row = in + hr * TB_IP + 8 * hg;
         float v[24];
 #pragma unroll
-        for (int j = 0; j < 24; j++) v[j] = row[j];
+        for (int j4 = 0; j4 < 6; j4++) {
+            const float4 q = *reinterpret_cast<const float4*>(row + 4 * j4);
+            v[4 * j4] = q.x;
+            v[4 * j4 + 1] = q.y;
+            v[4 * j4 + 2] = q.z;
+            v[4 * j4 + 3] = q.w;
+        }
         float* dst = hb + hr * TB_HP + 8 * hg;
 #pragma unroll
         for (int o = 0; o < 8; o++) {
             float a = 0.f;
 #pragma unroll
             for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
-            dst[o] = a * rx[o];
+            dst[o] = a;
         }
     }
     __syncthreads();
@@ -195,18 +198,17 @@ __device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const f
             float a = 0.f;
 #pragma unroll
             for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
-            out[o] = a * ry[o];
+            out[o] = a * rxy[o];
         }
     }
 }
 
 template <int KI>
-__device__ __forceinline__ void tile_masses_r8(int x0, int y0, int w, int h, float rx[8], float ry[6]) {
+__device__ __forceinline__ void tile_masses_r8(int x0, int y0, int w, int h, float rxy[6]) {
     const int tid = threadIdx.x;
+    const float rx = b_inv_mass<KI, 8>(x0 + (tid & 31), w);
 #pragma unroll
-    for (int o = 0; o < 8; o++) rx[o] = b_inv_mass<KI, 8>(x0 + 8 * (tid & 3) + o, w);
-#pragma unroll
-    for (int o = 0; o < 6; o++) ry[o] = b_inv_mass<KI, 8>(y0 + 6 * (tid >> 5) + o, h);
+    for (int o = 0; o < 6; o++) rxy[o] = rx * b_inv_mass<KI, 8>(y0 + 6 * (tid >> 5) + o, h);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -226,27 +228,38 @@ __device__ __forceinline__ void b_opsin(float& x, float& y, float& z, bool clamp
 }
 __device__ __forceinline__ float b_gamma(float v) {
     constexpr DConst kOff = dconst(9.9710635769299145);
-    return fmaf(19.245013259874995f, logf(add_dc(v, kOff)), -23.16046239805755f);
+    // logf(x) as log2(x) * ln 2 (x >= 9.97 here, so the approximation's absolute log2 error of
+    // ~2^-22 is ~1e-7 relative)
+    return fmaf(19.245013259874995f, lg2_approx(add_dc(v, kOff)) * 0.69314718055994531f, -23.16046239805755f);
 }
 
-// grid (ceil(w/32), ceil(h/48), 2*npairs)
+// grid (ceil(w/32), ceil(h/48), 2*npairs); the three channels' tiles are double-buffered.
 __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict__ work, BGeom g, int s,
                                                               float intensity) {
-    extern __shared__ float sm[];
-    float* in = sm;
-    float* hb = sm + TB_IH * TB_IP;
+    extern __shared__ __align__(16) float sm[];
+    float* hb = sm + 2 * TB_RAW;
     const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
-    float rx[8], ry[6];
-    tile_masses_r8<0>(x0, y0, S.w, S.h, rx, ry);
+    float rxy[6];
+    tile_masses_r8<0>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float src[3][6], blr[3][6];
+    tile_stage_r8(sm, bplane(work, g, S, pair, P_LIN + img * 3), S.p, S.w, S.h, x0, y0);
+    cp_async_commit();
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        tile_load_r8(in, bplane(work, g, S, pair, P_LIN + img * 3 + c), S.p, S.w, S.h, x0, y0);
+        float* in = sm + (c & 1) * TB_RAW;
+        if (c < 2) {
+            tile_stage_r8(sm + ((c + 1) & 1) * TB_RAW, bplane(work, g, S, pair, P_LIN + img * 3 + c + 1), S.p, S.w,
+                          S.h, x0, y0);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
         __syncthreads();
-        tile_blur_r8<0>(in, hb, rx, ry, blr[c]);
+        tile_blur_r8<0>(in, hb, rxy, blr[c]);
 #pragma unroll
         for (int o = 0; o < 6; o++) src[c][o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
@@ -264,9 +277,9 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
             bx = fmaxf(bx, 1e-4f);
             by = fmaxf(by, 1e-4f);
             bz = fmaxf(bz, 1e-4f);
-            const float ex = fmaxf(b_gamma(bx) / bx, 1e-4f);
-            const float ey = fmaxf(b_gamma(by) / by, 1e-4f);
-            const float ez = fmaxf(b_gamma(bz) / bz, 1e-4f);
+            const float ex = fmaxf(__fdividef(b_gamma(bx), bx), 1e-4f);
+            const float ey = fmaxf(__fdividef(b_gamma(by), by), 1e-4f);
+            const float ez = fmaxf(__fdividef(b_gamma(bz), bz), 1e-4f);
             b_opsin(sx, sy, sz, false);
             sx *= ex;
             sy *= ey;
@@ -284,44 +297,56 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
 
 // ------------------------------------------------------------------------------------------
 // Separable horizontal pass, radius R (21 or 9): 128x16 tile per CTA; each thread makes 8
-// consecutive outputs from 8+2R registers. Warp w covers rows (w>>2)*8..+7 and columns
-// (w&3)*32..+31; the smem pitch is 17 mod 32 so the 8 rows of a warp hit distinct banks.
+// consecutive outputs. The input rows start at x0 - RA (RA = R rounded up to a multiple of 4, so
+// the cp.async chunks are 16-byte aligned) and are read back as float4 (pitch 180 = 45 quads:
+// conflict-free); the thread's window starts RA - R floats into its first quad.
 // grid (ceil(w/128), ceil(h/16), 6*npairs): z -> pair = z/6, plane = src_id + z%6.
-constexpr int HB_TW = 128, HB_TH = 16, HB_P = 177;
+constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180;
 
 template <int KI, int R>
 __global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ work, BGeom g, int s, int src_id,
                                                            int dst_id) {
-    __shared__ float in[HB_TH * HB_P];
+    __shared__ __align__(16) float in[HB_TH * HB_P];
+    constexpr int RA = (R + 3) & ~3;
+    constexpr int IW = HB_TW + 2 * RA;
+    constexpr int OFF = RA - R;
+    constexpr int NV4 = (OFF + 8 + 2 * R + 3) / 4;
+    static_assert(IW <= HB_P && 120 + 4 * NV4 <= HB_P, "hblur tile");
     const int pair = blockIdx.z / 6, pl = blockIdx.z % 6;
     const BScaleDev S = pick_scale(g, s);
     const float* src = bplane(work, g, S, pair, src_id + pl);
     float* dst = bplane(work, g, S, pair, dst_id + pl);
     const int x0 = blockIdx.x * HB_TW, y0 = blockIdx.y * HB_TH;
-    constexpr int IW = HB_TW + 2 * R;
-    for (int e = threadIdx.x; e < HB_TH * IW; e += 256) {
-        const int r = e / IW, col = e - r * IW;
-        const int gx = x0 - R + col, gy = y0 + r;
-        float v = 0.f;
-        if (gx >= 0 && gx < S.w && gy < S.h) v = __ldg(src + (int64_t)gy * S.p + gx);
-        in[r * HB_P + col] = v;
-    }
+    stage_rows<256>(in, HB_P, src, S.p, S.w, S.h, x0 - RA, y0, HB_TH, IW / 4);
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = (warp >> 2) * 8 + (lane >> 2);
     const int col0 = (warp & 3) * 32 + 8 * (lane & 3);
     const int gy = y0 + row;
     if (gy >= S.h) return;
-    float v[8 + 2 * R];
+    float v[4 * NV4];
 #pragma unroll
-    for (int j = 0; j < 8 + 2 * R; j++) v[j] = in[row * HB_P + col0 + j];
+    for (int j4 = 0; j4 < NV4; j4++) {
+        const float4 q = *reinterpret_cast<const float4*>(in + row * HB_P + col0 + 4 * j4);
+        v[4 * j4] = q.x;
+        v[4 * j4 + 1] = q.y;
+        v[4 * j4 + 2] = q.z;
+        v[4 * j4 + 3] = q.w;
+    }
+    float out[8];
 #pragma unroll
     for (int o = 0; o < 8; o++) {
-        const int x = x0 + col0 + o;
         float a = 0.f;
 #pragma unroll
-        for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
-        if (x < S.w) dst[(int64_t)gy * S.p + x] = a * b_inv_mass<KI, R>(x, S.w);
+        for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[OFF + o + i], c_bk[KI][i], a);
+        out[o] = a * b_inv_mass<KI, R>(x0 + col0 + o, S.w);
+    }
+    float* d = dst + (int64_t)gy * S.p + x0 + col0;
+    if (x0 + col0 + 8 <= S.p) {  // rows are padded to a multiple of 8 floats
+        *reinterpret_cast<float4*>(d) = make_float4(out[0], out[1], out[2], out[3]);
+        *reinterpret_cast<float4*>(d + 4) = make_float4(out[4], out[5], out[6], out[7]);
     }
 }
 
@@ -337,16 +362,11 @@ __device__ __forceinline__ void vblur3(float* in, float* __restrict__ work, cons
     const int x0 = blockIdx.x * VB_TW, y0 = blockIdx.y * VB_TH;
     constexpr int IH = VB_TH + 2 * R;
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-        const float* src = bplane(work, g, S, pair, src_id + c);
-        for (int e = threadIdx.x; e < IH * VB_TW; e += 256) {
-            const int r = e >> 5, col = e & 31;
-            const int gx = x0 + col, gy = y0 - R + r;
-            float v = 0.f;
-            if (gx < S.w && gy >= 0 && gy < S.h) v = __ldg(src + (int64_t)gy * S.p + gx);
-            in[c * IH * VB_TW + e] = v;
-        }
-    }
+    for (int c = 0; c < 3; c++)
+        stage_rows<256>(in + c * IH * VB_TW, VB_TW, bplane(work, g, S, pair, src_id + c), S.p, S.w, S.h, x0, y0 - R,
+                        IH, VB_TW / 4);
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float ry[8];
@@ -370,7 +390,7 @@ __device__ __forceinline__ void vblur3(float* in, float* __restrict__ work, cons
 
 // LF vertical pass: D = XYB - LF (in place over XYB) and LF vals (separatefrequencies.hpp:3-12)
 __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ work, BGeom g, int s) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
     float lf[3][8];
     vblur3<4, 21>(sm, work, g, pair, s, P_TMP + img * 3, lf);
@@ -422,7 +442,7 @@ __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
 // MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
 // written over the D planes (separatefrequencies.hpp:37-99,160-187).
 __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ work, BGeom g, int s) {
-    extern __shared__ float sm[];
+    extern __shared__ __align__(16) float sm[];
     const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
     float mf[3][8];
     vblur3<3, 9>(sm, work, g, pair, s, P_TMP + img * 3, mf);
@@ -454,21 +474,24 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ wo
 
 // HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), 2*npairs)
 __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ work, BGeom g, int s) {
-    extern __shared__ float sm[];
-    float* in = sm;
-    float* hb = sm + TB_IH * TB_IP;
+    extern __shared__ __align__(16) float sm[];
+    float* hb = sm + 2 * TB_RAW;
     const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
-    float rx[8], ry[6];
-    tile_masses_r8<1>(x0, y0, S.w, S.h, rx, ry);
+    float rxy[6];
+    tile_masses_r8<1>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    tile_stage_r8(sm, bplane(work, g, S, pair, P_XYB + img * 3), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, bplane(work, g, S, pair, P_XYB + img * 3 + 1), S.p, S.w, S.h, x0, y0);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-        tile_load_r8(in, bplane(work, g, S, pair, P_XYB + img * 3 + c), S.p, S.w, S.h, x0, y0);
-        __syncthreads();
+        const float* in = sm + c * TB_RAW;
         float blr[6], pre[6];
-        tile_blur_r8<1>(in, hb, rx, ry, blr);
+        tile_blur_r8<1>(in, hb, rxy, blr);
 #pragma unroll
         for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
@@ -510,6 +533,7 @@ struct DiffParams {
     float l2asym_gt[2], l2asym_lt[2];  // already including the inner x0.8 (simplerdiff.hpp:297-298)
     float wmf[3], wlf[3];
 };
+__constant__ DiffParams c_dp;
 
 __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) {
     const float absval = 0.5f * fabsf(a) + 0.5f * fabsf(b);
@@ -580,7 +604,7 @@ constexpr int DF_IW = DF_TW + 2 * DF_H, DF_IH = DF_TH + 2 * DF_H;  // 40 x 72
 // Sliding 9x9 register window down one column: rows are loaded as they are first needed and
 // die after their last pattern, so about 81 values are live at a time.
 template <bool HF>
-__device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r0, int c, float acc[8]) {
+__device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r0, int c, float res[8]) {
     float win[16][9];
 #pragma unroll
     for (int r = 0; r < 16; r++) {
@@ -594,7 +618,7 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
             } else {
                 MALTA_LF_BODY
             }
-            acc[o] += ret;
+            res[o] = ret;
         }
     }
 }
@@ -602,8 +626,15 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 #undef SQ
 
 // grid (ceil(w/32), ceil(h/64), npairs), 256 threads; column tid&31, rows 8*(tid>>5)..+7.
-__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__ work, BGeom g, int s, DiffParams P) {
-    __shared__ float Dt[DF_IH * DF_IW];
+// The six maps' raw (l0, l1) tiles are staged with cp.async, double-buffered across maps;
+// samples outside the image arrive as zeros, for which malta_pre returns exactly 0, the
+// reference's padding value (maltaDiff.hpp:549-553).
+constexpr int DF_RAW = DF_IH * DF_IW;
+constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW) * 4;
+
+__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__ work, BGeom g, int s) {
+    extern __shared__ __align__(16) float sm[];
+    float* Dt = sm + 4 * DF_RAW;
     const int pair = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * DF_TW, y0 = blockIdx.y * DF_TH;
@@ -614,28 +645,45 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
         acX[o] = 0.f;
         acY[o] = 0.f;
     }
-    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X
-    const int ids[6] = {P_UHF + 1, P_UHF + 0, P_HF + 1, P_HF + 0, P_MF + 1, P_MF + 0};
-    const int stride_img[6] = {2, 2, 2, 2, 3, 3};
-#pragma unroll
+    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X; image 1's plane is
+    // `per_img` ids after image 0's.
+    auto plane_id = [](int m) { return (m < 2 ? P_UHF : m < 4 ? P_HF : P_MF) + 1 - (m & 1); };
+    auto per_img = [](int m) { return m < 4 ? 2 : 3; };
+    stage_rows<256>(sm, DF_IW, bplane(work, g, S, pair, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+                    DF_IW / 4);
+    stage_rows<256>(sm + DF_RAW, DF_IW, bplane(work, g, S, pair, plane_id(0) + per_img(0)), S.p, S.w, S.h,
+                    x0 - DF_H, y0 - DF_H, DF_IH, DF_IW / 4);
+    cp_async_commit();
+#pragma unroll 1
     for (int m = 0; m < 6; m++) {
-        const float* l0 = bplane(work, g, S, pair, ids[m]);
-        const float* l1 = bplane(work, g, S, pair, ids[m] + stride_img[m]);
-        const MaltaMap mm = P.mm[m];
-        for (int e = threadIdx.x; e < DF_IH * DF_IW; e += 256) {
-            const int r = e / DF_IW, col = e - r * DF_IW;
-            const int gx = x0 - DF_H + col, gy = y0 - DF_H + r;
-            float v = 0.f;
-            if (gx >= 0 && gx < S.w && gy >= 0 && gy < S.h) {
-                const int64_t i = (int64_t)gy * S.p + gx;
-                v = malta_pre(__ldg(l0 + i), __ldg(l1 + i), mm);
-            }
-            Dt[e] = v;
+        const float* r0 = sm + (m & 1) * 2 * DF_RAW;
+        const float* r1 = r0 + DF_RAW;
+        if (m < 5) {
+            float* n0 = sm + ((m + 1) & 1) * 2 * DF_RAW;
+            const int id = plane_id(m + 1);
+            stage_rows<256>(n0, DF_IW, bplane(work, g, S, pair, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+                            DF_IW / 4);
+            stage_rows<256>(n0 + DF_RAW, DF_IW, bplane(work, g, S, pair, id + per_img(m + 1)), S.p, S.w, S.h,
+                            x0 - DF_H, y0 - DF_H, DF_IH, DF_IW / 4);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-        if (m < 2) malta_column<true>(Dt, 8 * vg, vc, (m & 1) ? acX : acY);
-        else malta_column<false>(Dt, 8 * vg, vc, (m & 1) ? acX : acY);
+        const MaltaMap mm = c_dp.mm[m];
+        for (int e = threadIdx.x; e < DF_RAW; e += 256) Dt[e] = malta_pre(r0[e], r1[e], mm);
         __syncthreads();
+        float res[8];
+        if (m < 2) malta_column<true>(Dt, 8 * vg, vc, res);
+        else malta_column<false>(Dt, 8 * vg, vc, res);
+        if (m & 1) {
+#pragma unroll
+            for (int o = 0; o < 8; o++) acX[o] += res[o];
+        } else {
+#pragma unroll
+            for (int o = 0; o < 8; o++) acY[o] += res[o];
+        }
     }
     const int x = x0 + vc;
     if (x >= S.w) return;
@@ -643,56 +691,61 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
     const float bias = mul * 12.61050594197f;
     const float sqb = sqrtf(bias);
     constexpr DConst k04 = dconst(0.4);
+    const DiffParams& P = c_dp;
 #pragma unroll
     for (int o = 0; o < 8; o++) {
         const int y = y0 + 8 * vg + o;
-        if (y >= S.h) break;
-        const int64_t i = (int64_t)y * S.p + x;
-        float ac[3] = {acX[o], acY[o], 0.f};
-        float dc[3] = {0.f, 0.f, 0.f};
-        float hf[2][2], uhf[2][2];
+        if (y < S.h) {
+            const int64_t i = (int64_t)y * S.p + x;
+            float ac[3] = {acX[o], acY[o], 0.f};
+            float dc[3] = {0.f, 0.f, 0.f};
+            float hf[2][2], uhf[2][2], mf[2][3], lf[2][3];
 #pragma unroll
-        for (int m = 0; m < 2; m++)
+            for (int m = 0; m < 2; m++) {
 #pragma unroll
-            for (int c = 0; c < 2; c++) {
-                hf[m][c] = bplane(work, g, S, pair, P_HF + m * 2 + c)[i];
-                uhf[m][c] = bplane(work, g, S, pair, P_UHF + m * 2 + c)[i];
-            }
+                for (int c = 0; c < 2; c++) {
+                    hf[m][c] = __ldg(bplane(work, g, S, pair, P_HF + m * 2 + c) + i);
+                    uhf[m][c] = __ldg(bplane(work, g, S, pair, P_UHF + m * 2 + c) + i);
+                }
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            if (c < 2) {  // L2AsymDiff (simplerdiff.hpp:263-293)
-                const float s1 = hf[0][c], s2 = hf[1][c];
-                const float diff = s1 - s2;
-                ac[c] += P.l2asym_gt[c] * diff * diff;
-                const float fabs0 = fabsf(s1);
-                const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
-                const float wl = P.l2asym_lt[c];
-                if (s1 < 0) {
-                    if (s2 > -too_small) { const float v = s2 + too_small; ac[c] += wl * v * v; }
-                    else if (s2 < -too_big) { const float v = -s2 - too_big; ac[c] += wl * v * v; }
-                } else {
-                    if (s2 < too_small) { const float v = too_small - s2; ac[c] += wl * v * v; }
-                    else if (s2 > too_big) { const float v = s2 - too_big; ac[c] += wl * v * v; }
+                for (int c = 0; c < 3; c++) {
+                    mf[m][c] = __ldg(bplane(work, g, S, pair, P_MF + m * 3 + c) + i);
+                    lf[m][c] = __ldg(bplane(work, g, S, pair, P_LFV + m * 3 + c) + i);
                 }
             }
-            {
-                const float d = bplane(work, g, S, pair, P_MF + c)[i] - bplane(work, g, S, pair, P_MF + 3 + c)[i];
-                ac[c] += P.wmf[c] * d * d;
-            }
-            {
-                const float d = bplane(work, g, S, pair, P_LFV + c)[i] - bplane(work, g, S, pair, P_LFV + 3 + c)[i];
-                dc[c] += P.wlf[c] * d * d;
-            }
-        }
-        bplane(work, g, S, pair, P_SAC)[i] = ac[0] + ac[1] + ac[2];
-        bplane(work, g, S, pair, P_SDC)[i] = dc[0] + dc[1] + dc[2];
-        // maskinit + diffPrecompute (maskPsycho.hpp:3-40)
 #pragma unroll
-        for (int m = 0; m < 2; m++) {
-            const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
-            const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
-            const float mk = sqrtf(xd * xd + yd * yd);
-            bplane(work, g, S, pair, P_PRE0 + m)[i] = sqrtf(mul * fabsf(mk) + bias) - sqb;
+            for (int c = 0; c < 3; c++) {
+                if (c < 2) {  // L2AsymDiff (simplerdiff.hpp:263-293)
+                    const float s1 = hf[0][c], s2 = hf[1][c];
+                    const float diff = s1 - s2;
+                    ac[c] += P.l2asym_gt[c] * diff * diff;
+                    const float fabs0 = fabsf(s1);
+                    const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
+                    const float wl = P.l2asym_lt[c];
+                    if (s1 < 0) {
+                        if (s2 > -too_small) { const float v = s2 + too_small; ac[c] += wl * v * v; }
+                        else if (s2 < -too_big) { const float v = -s2 - too_big; ac[c] += wl * v * v; }
+                    } else {
+                        if (s2 < too_small) { const float v = too_small - s2; ac[c] += wl * v * v; }
+                        else if (s2 > too_big) { const float v = s2 - too_big; ac[c] += wl * v * v; }
+                    }
+                }
+                const float dm = mf[0][c] - mf[1][c];
+                ac[c] += P.wmf[c] * dm * dm;
+                const float dl = lf[0][c] - lf[1][c];
+                dc[c] += P.wlf[c] * dl * dl;
+            }
+            bplane(work, g, S, pair, P_SAC)[i] = ac[0] + ac[1] + ac[2];
+            bplane(work, g, S, pair, P_SDC)[i] = dc[0] + dc[1] + dc[2];
+            // maskinit + diffPrecompute (maskPsycho.hpp:3-40). sqrt(m + b) - sqrt(b) is evaluated
+            // as m / (sqrt(m + b) + sqrt(b)): the same value without the cancellation.
+#pragma unroll
+            for (int m = 0; m < 2; m++) {
+                const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
+                const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
+                const float mk = mul * sqrtf(xd * xd + yd * yd);
+                bplane(work, g, S, pair, P_PRE0 + m)[i] = mk / (sqrtf(mk + bias) + sqb);
+            }
         }
     }
 }
@@ -700,20 +753,22 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
 // Blur both mask planes (sigma 2.7); store B0 and add 10*(B0-B1)^2 to the AC sum.
 // grid (ceil(w/32), ceil(h/48), npairs)
 __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restrict__ work, BGeom g, int s) {
-    extern __shared__ float sm[];
-    float* in = sm;
-    float* hb = sm + TB_IH * TB_IP;
+    extern __shared__ __align__(16) float sm[];
+    float* hb = sm + 2 * TB_RAW;
     const int pair = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
-    float rx[8], ry[6];
-    tile_masses_r8<2>(x0, y0, S.w, S.h, rx, ry);
+    float rxy[6];
+    tile_masses_r8<2>(x0, y0, S.w, S.h, rxy);
+    tile_stage_r8(sm, bplane(work, g, S, pair, P_PRE0), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, bplane(work, g, S, pair, P_PRE1), S.p, S.w, S.h, x0, y0);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
     float b[2][6];
 #pragma unroll
     for (int m = 0; m < 2; m++) {
-        tile_load_r8(in, bplane(work, g, S, pair, P_PRE0 + m), S.p, S.w, S.h, x0, y0);
-        __syncthreads();
-        tile_blur_r8<2>(in, hb, rx, ry, b[m]);
+        tile_blur_r8<2>(sm + m * TB_RAW, hb, rxy, b[m]);
         __syncthreads();
     }
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
@@ -825,7 +880,7 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__
             float v = red[lane][0];
             for (int w = 1; w < 8; w++) v = lane == 2 ? fmaxf(v, red[lane][w]) : v + red[lane][w];
             const int blk = blockIdx.y * gridDim.x + blockIdx.x;
-            partials[((int64_t)pair * g.norm_tiles + blk) * 3 + lane] = v;
+            partials[((int64_t)pair * 3 + lane) * g.norm_tiles + blk] = v;
         }
     }
 }
@@ -837,11 +892,11 @@ __global__ void __launch_bounds__(256) butter_finalize_kernel(const float* __res
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     double sq = 0.0, s3 = 0.0;
     float mx = 0.f;
+    const float* p = partials + (int64_t)pair * 3 * g.norm_tiles;
     for (int t = tid; t < g.norm_tiles; t += 256) {
-        const float* p = partials + ((int64_t)pair * g.norm_tiles + t) * 3;
-        sq += (double)p[0];
-        s3 += (double)p[1];
-        mx = fmaxf(mx, p[2]);
+        sq += (double)__ldg(p + t);
+        s3 += (double)__ldg(p + g.norm_tiles + t);
+        mx = fmaxf(mx, __ldg(p + 2 * g.norm_tiles + t));
     }
     sq = warp_sum(sq);
     s3 = warp_sum(s3);
@@ -929,7 +984,7 @@ static DiffParams make_diff_params() {
     return P;
 }
 
-constexpr int kTileSmem = TB_SMEM_FLOATS * 4;
+constexpr int kTileSmem = (2 * TB_RAW + TB_HPL) * 4;
 constexpr int kVLfSmem = 3 * (VB_TH + 42) * VB_TW * 4;
 constexpr int kVMfSmem = 3 * (VB_TH + 18) * VB_TW * 4;
 
@@ -950,6 +1005,11 @@ int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensit
     int rc = upload_butter_tables();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
+    {
+        const DiffParams P = make_diff_params();
+        VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
+    }
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
     VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * work_floats * max_pairs));
     VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
@@ -979,7 +1039,6 @@ size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs) {
 int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st) {
     if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
     const BGeom g = make_bgeom(w, h);
-    static const DiffParams P = make_diff_params();
     const unsigned np = (unsigned)npairs;
     {
         dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), 2 * np);
@@ -1003,7 +1062,7 @@ int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
         { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(work, g, s); }
         { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s); }
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
-        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, 0, st>>>(work, g, s, P); }
+        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(work, g, s); }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
         { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(work, g, s); }
         const dim3 gf((unsigned)ceil_div(sw, 32), (unsigned)ceil_div(sh, 8), np);

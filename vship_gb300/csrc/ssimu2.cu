@@ -76,9 +76,9 @@ __device__ __forceinline__ void positive_xyb(float& r, float& g, float& b) {
     float oy = fmaf(0.23f, r, fmaf(0.692f, g, fmaf(0.078f, b, bias)));
     float oz = fmaf(0.24342269f, r, fmaf(0.20476745f, g, fmaf(0.55180986f, b, bias)));
     const float abs_bias = -0.1559542025327239f;
-    ox = cbrtf(ox * (float)(ox >= 0.f)) + abs_bias;
-    oy = cbrtf(oy * (float)(oy >= 0.f)) + abs_bias;
-    oz = cbrtf(oz * (float)(oz >= 0.f)) + abs_bias;
+    ox = cbrt_pos(fmaxf(ox, 0.f)) + abs_bias;
+    oy = cbrt_pos(fmaxf(oy, 0.f)) + abs_bias;
+    oz = cbrt_pos(fmaxf(oz, 0.f)) + abs_bias;
     float X = 0.5f * (ox - oy);
     float Y = X + oy;
     float B = oz;
@@ -108,9 +108,9 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
             const int gx = bx * 32 + tx, gy = by * 32 + ly;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f;
             if (gx < L.w && gy < L.h) {
-                v0 = to_linear(load_sample<IT>(fd.plane[0], fd.stride, gx, gy));
-                v1 = to_linear(load_sample<IT>(fd.plane[1], fd.stride, gx, gy));
-                v2 = to_linear(load_sample<IT>(fd.plane[2], fd.stride, gx, gy));
+                v0 = to_linear_fast(load_sample<IT>(fd.plane[0], fd.stride, gx, gy));
+                v1 = to_linear_fast(load_sample<IT>(fd.plane[1], fd.stride, gx, gy));
+                v2 = to_linear_fast(load_sample<IT>(fd.plane[2], fd.stride, gx, gy));
                 float X = v0, Y = v1, B = v2;
                 positive_xyb(X, Y, B);
                 int64_t o = L.off + (int64_t)gy * L.pitch + gx;
@@ -186,23 +186,13 @@ constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte 
 constexpr int ST_HP = 33;                // horizontal-pass output pitch
 constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
 constexpr int ST_HPLANE = ST_IH * ST_HP;
-constexpr int kStatsSmem = (2 * 2 * ST_RAW + 5 * ST_HPLANE) * 4;  // 2 stages x 2 images + 5 moments
+constexpr int kStatsSmem = (2 * 2 * ST_RAW + 5 * ST_HPLANE + 3 * 8 * 6) * 4;  // 2 stages x 2 images, 5 moments, pools
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
     const int beg = max(0, pos - 8) - (pos - 8);
     const int end = min(extent, pos + 9) - (pos - 8);
     return 1.0f / (c_s2_I[end] - c_s2_I[beg]);
-}
-
-__device__ __forceinline__ void cp_async16(float* smem, const float* gmem, int src_bytes) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(src_bytes) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
 // Stage the 64x48 halo tile of one plane: 768 16-byte chunks, 3 per thread. The tile's first
@@ -231,6 +221,7 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
     extern __shared__ __align__(16) float sm[];
     float* raw = sm;                   // [stage][image][64][52]
     float* hb = sm + 4 * ST_RAW;       // [5][64][33]
+    float* red = hb + 5 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
     const int pair = blockIdx.y;
     const int t = blockIdx.x;
     int s = 0;
@@ -242,41 +233,27 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
     const int ty0 = (lt / L.tiles_x) * ST_TH;
     const float* im1 = pyr + (int64_t)(pair * 2 + 0) * 3 * g.plane_elems + L.off;
     const float* im2 = pyr + (int64_t)(pair * 2 + 1) * 3 * g.plane_elems + L.off;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool interior = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h;
 
     // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23)
     const int hr = tid >> 2, hg = tid & 3;
-    float rx[8];
-#pragma unroll
-    for (int o = 0; o < 8; o++) rx[o] = s2_inv_mass(tx0 + 8 * hg + o, L.w);
-    const int hgy = ty0 - ST_R + hr;
-    const bool hrow_ok = hgy >= 0 && hgy < L.h;
-    unsigned colmask = 0;  // bit j: input column 8*hg + j lies inside the image
-#pragma unroll
-    for (int j = 0; j < 24; j++) {
-        const int gx = tx0 - ST_R + 8 * hg + j;
-        colmask |= (unsigned)(gx >= 0 && gx < L.w) << j;
-    }
-    if (!hrow_ok) colmask = 0;
-    // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5
+    // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5. Both passes' border
+    // renormalisations (out / tot, gaussianblur.hpp:63-92) are applied here as one product.
     const int vc = tid & 31, vg = tid >> 5;
-    float ry[6];
+    const float rxv = s2_inv_mass(tx0 + vc, L.w);
+    float rxy[6];
 #pragma unroll
-    for (int o = 0; o < 6; o++) ry[o] = s2_inv_mass(ty0 + 6 * vg + o, L.h);
-
-    float acc[18];
-#pragma unroll
-    for (int i = 0; i < 18; i++) acc[i] = 0.f;
+    for (int o = 0; o < 6; o++) rxy[o] = rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
 
     stage_tile(raw, im1, L.pitch, L.w, L.h, tx0, ty0);
     stage_tile(raw + ST_RAW, im2, L.pitch, L.w, L.h, tx0, ty0);
     cp_async_commit();
 
-#pragma unroll
+#pragma unroll 1
     for (int c = 0; c < 3; c++) {
-        const float* r1 = raw + (c & 1) * 2 * ST_RAW;
-        const float* r2 = r1 + ST_RAW;
+        float* r1 = raw + (c & 1) * 2 * ST_RAW;
+        float* r2 = r1 + ST_RAW;
         if (c < 2) {
             float* n1 = raw + ((c + 1) & 1) * 2 * ST_RAW;
             stage_tile(n1, im1 + (int64_t)(c + 1) * g.plane_elems, L.pitch, L.w, L.h, tx0, ty0);
@@ -290,8 +267,20 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
         // Moments are formed on values shifted by one per-tile constant (the reference image's
         // value at the tile origin). The blur is normalised, so sigma = E[(x-s)^2] - (E[x]-s)^2
         // is unchanged, while the FP32 cancellation of E[x^2] - E[x]^2 shrinks by the square of
-        // |x| / |x - s|. Out-of-image samples stay exactly zero (they carry no kernel mass).
+        // |x| / |x - s|. Samples outside the image must carry nothing: on border tiles their
+        // slots are set to the shift itself, so that x - s is exactly zero there.
         const float shift = r1[ST_R * ST_RP + ST_R];
+        if (!interior) {
+            for (int e = tid; e < ST_IH * ST_IW; e += 256) {
+                const int r = e / ST_IW, col = e - r * ST_IW;
+                const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
+                if (gx < 0 || gx >= L.w || gy < 0 || gy >= L.h) {
+                    r1[r * ST_RP + col] = shift;
+                    r2[r * ST_RP + col] = shift;
+                }
+            }
+            __syncthreads();
+        }
         {
             float h[5][8];
 #pragma unroll
@@ -309,11 +298,7 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const int j = 4 * j4 + u;
-                    float a = la[u] - shift, b = lb[u] - shift;
-                    if (!interior && !((colmask >> j) & 1u)) {
-                        a = 0.f;
-                        b = 0.f;
-                    }
+                    const float a = la[u] - shift, b = lb[u] - shift;
                     const float aa = a * a, bb = b * b, ab = a * b;
 #pragma unroll
                     for (int o = 0; o < 8; o++) {
@@ -333,7 +318,7 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
             for (int q = 0; q < 5; q++) {
                 float* dst = hb + q * ST_HPLANE + hr * ST_HP + 8 * hg;
 #pragma unroll
-                for (int o = 0; o < 8; o++) dst[o] = h[q][o] * rx[o];
+                for (int o = 0; o < 8; o++) dst[o] = h[q][o];
             }
         }
         __syncthreads();
@@ -350,9 +335,10 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
                 float a = 0.f;
 #pragma unroll
                 for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_s2_k[i], a);
-                m[q][o] = a * ry[o];
+                m[q][o] = a * rxy[o];
             }
         }
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
         for (int o = 0; o < 6; o++) {
             const int y = ty0 + 6 * vg + o, x = tx0 + vc;
@@ -360,8 +346,9 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
                 const int so = (6 * vg + o + ST_R) * ST_RP + vc + ST_R;
                 const float i1 = r1[so] - shift, i2 = r2[so] - shift;  // shifted samples
                 const float m1 = m[0][o], m2 = m[1][o];                 // shifted means
-                // ssim map (score.hpp:141-148); explicit fma so identical inputs give bitwise
-                // identical numerator and denominator whatever the compiler contracts
+                // SSIM map (score.hpp:141-148) as max((den - num) / den, 0), the same quantity
+                // as max(1 - num / den, 0) without the cancellation; explicit fma so identical
+                // frames give num == den bitwise whatever the compiler contracts
                 const float md = m1 - m2;
                 const float num_m = fmaf(md, -md, 1.0f);
                 const float s12 = fmaf(-m1, m2, m[4][o]);
@@ -369,80 +356,74 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
                 const float s22 = fmaf(-m2, m2, m[3][o]);
                 const float num_s = fmaf(s12, 2.0f, 0.0009f);
                 const float denom = (s11 + s22) + 0.0009f;
-                const float d0 = fmaxf(1.0f - (num_m * num_s) / denom, 0.0f);
-                // edge maps (score.hpp:151-153): |I - mu| is shift-invariant
-                const float v1 = (fabsf(i2 - m2) + 1.0f) / (fabsf(i1 - m1) + 1.0f) - 1.0f;
+                const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
+                // edge maps (score.hpp:151-153): (|I2-m2| + 1) / (|I1-m1| + 1) - 1 written as
+                // (|I2-m2| - |I1-m1|) / (|I1-m1| + 1); |I - mu| is shift-invariant
+                const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
+                const float v1 = __fdividef(e2 - e1, e1 + 1.0f);
                 const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
                 const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
-                acc[0 * 3 + c] += d0;
-                acc[1 * 3 + c] += q0 * q0;
-                acc[2 * 3 + c] += d1;
-                acc[3 * 3 + c] += q1 * q1;
-                acc[4 * 3 + c] += d2;
-                acc[5 * 3 + c] += q2 * q2;
+                acc[0] += d0;
+                acc[1] += q0 * q0;
+                acc[2] += d1;
+                acc[3] += q1 * q1;
+                acc[4] += d2;
+                acc[5] += q2 * q2;
             }
+        }
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            const float v = warp_sum(acc[i]);
+            if (lane == 0) red[(c * 8 + warp) * 6 + i] = v;
         }
         __syncthreads();
     }
-    // block reduction of the 18 pools
-    float* red = sm;  // reuse: [8 warps][18]
-    const int lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-    for (int i = 0; i < 18; i++) {
-        float v = warp_sum(acc[i]);
-        if (lane == 0) red[warp * 18 + i] = v;
-    }
-    __syncthreads();
+    // pools: partials[pair][pool * 3 + channel][tile], pool = map * 2 + norm
     if (tid < 18) {
+        const int pool = tid / 3, c = tid - pool * 3;
         float v = 0.f;
 #pragma unroll
-        for (int w = 0; w < 8; w++) v += red[w * 18 + tid];
-        partials[((int64_t)pair * g.tiles_total + t) * 18 + tid] = v;
+        for (int w = 0; w < 8; w++) v += red[(c * 8 + w) * 6 + pool];
+        partials[((int64_t)pair * 18 + tid) * g.tiles_total + t] = v;
     }
 }
 
 // ------------------------------------------------------------------------------------------
-// Kernel 3: FP64 finalisation, one CTA per pair.
+// Kernel 3: FP64 finalisation, one CTA per pair. The 108 (scale, pool, channel) sums are
+// reduced warp-parallel over their tiles (coalesced), then the 108 weighted features are summed
+// in parallel; only the score mapping runs on one thread (FP64 is a slow pipe on this GPU).
 __global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __restrict__ partials,
                                                               double* __restrict__ scores, Ssimu2Geom g) {
-    __shared__ double red[8][18];
     __shared__ double pooled[6][18];
+    __shared__ double red[8];
     const int pair = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int s = 0; s < 6; s++) {
-        double acc[18];
-#pragma unroll
-        for (int i = 0; i < 18; i++) acc[i] = 0.0;
-        for (int t = g.tile_begin[s] + tid; t < g.tile_begin[s + 1]; t += 256) {
-            const float* p = partials + ((int64_t)pair * g.tiles_total + t) * 18;
-#pragma unroll
-            for (int i = 0; i < 18; i++) acc[i] += (double)p[i];
-        }
-#pragma unroll
-        for (int i = 0; i < 18; i++) {
-            double v = warp_sum(acc[i]);
-            if (lane == 0) red[warp][i] = v;
-        }
-        __syncthreads();
-        if (tid < 18) {
-            double v = 0.0;
-            for (int w = 0; w < 8; w++) v += red[w][tid];
-            pooled[s][tid] = v / ((double)g.lv[s].w * (double)g.lv[s].h);
-        }
-        __syncthreads();
+    for (int seg = warp; seg < 108; seg += 8) {
+        const int s = seg / 18, i = seg - 18 * (seg / 18);
+        const float* p = partials + ((int64_t)pair * 18 + i) * g.tiles_total + g.tile_begin[s];
+        const int n = g.tile_begin[s + 1] - g.tile_begin[s];
+        double a = 0.0;
+        for (int t = lane; t < n; t += 32) a += (double)__ldg(p + t);
+        a = warp_sum(a);
+        if (lane == 0) pooled[s][i] = a / ((double)g.lv[s].w * (double)g.lv[s].h);
     }
+    __syncthreads();
+    // feature k = plane*36 + scale*6 + norm*3 + map (ssimu2/main.hpp:83-95); pooled index
+    // (map*2 + norm)*3 + plane; 4th root for the 4-norm (score.hpp:263-267)
+    double v = 0.0;
+    if (tid < 108) {
+        const int plane = tid / 36, sc = (tid % 36) / 6, nrm = (tid % 6) / 3, mi = tid % 3;
+        double x = pooled[sc][(mi * 2 + nrm) * 3 + plane];
+        if (nrm == 1) x = sqrt(sqrt(x));
+        v = c_s2_w[tid] * x;
+    }
+    v = warp_sum(v);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
     if (tid == 0) {
-        // pooled[s][pool*3 + channel], pool = map*2 + norm (map: ssim, artifact, detail)
         double ssim = 0.0;
-        for (int plane = 0; plane < 3; plane++)
-            for (int s = 0; s < 6; s++)
-                for (int n = 0; n < 2; n++)
-                    for (int i = 0; i < 3; i++) {
-                        double v = pooled[s][(i * 2 + n) * 3 + plane];
-                        if (n == 1) v = sqrt(sqrt(v));
-                        ssim = fma(c_s2_w[plane * 36 + s * 6 + n * 3 + i], v, ssim);
-                    }
-        ssim *= 0.9562382616834844;
+        for (int w = 0; w < 8; w++) ssim += red[w];
+        ssim *= 0.9562382616834844;  // score.hpp:388-397
         ssim = (6.248496625763138e-5 * ssim * ssim) * ssim + 2.326765642916932 * ssim -
                0.020884521182843837 * ssim * ssim;
         scores[pair] = ssim > 0.0 ? pow(ssim, 0.6276336467831387) * -10.0 + 100.0 : 100.0;
