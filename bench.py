@@ -179,14 +179,17 @@ def max_over_ranks(x: float, ws: int) -> float:
 # ------------------------------------------------------------------------------------------
 # workloads
 
-def make_inputs(kind: str, npairs: int, device):
+def parse_size(txt: str):
+    w, h = txt.lower().split("x")
+    return int(w), int(h)
+
+
+def make_inputs(kind: str, npairs: int, device, size):
     """Device-resident float32 R'G'B' planes: (npairs, 3, H, W) for reference and distorted."""
     import torch
     from vship_gb300 import synth
-    if kind == "ssimu2":
-        h, w, dist = H1080, W1080, "dct"
-    else:
-        h, w, dist = H4K, W4K, "blur_noise"
+    w, h = size
+    dist = "dct" if kind == "ssimu2" else "blur_noise"
     ref = torch.empty((npairs, 3, h, w), dtype=torch.float32, device=device)
     dst = torch.empty_like(ref)
     for t in range(npairs):
@@ -342,7 +345,8 @@ def bench_workload(v, kind, args, ws, rank):
     import torch
     npairs = args.pairs if kind == "ssimu2" else args.butter_pairs
     chunk = args.chunk if kind == "ssimu2" else args.butter_chunk
-    ref, dst = make_inputs(kind, npairs, "cuda")
+    size = parse_size(args.ssimu2_size if kind == "ssimu2" else args.butter_size)
+    ref, dst = make_inputs(kind, npairs, "cuda", size)
     torch.cuda.synchronize()
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
@@ -353,7 +357,7 @@ def bench_workload(v, kind, args, ws, rank):
     e2e_sec, h2d, d2h, host_scores = run_e2e(v, kind, ref, dst, args.e2e_steps, 1, args.e2e_threads)
     e2e_sec = max_over_ranks(e2e_sec, ws)
     e2e_value = npairs * ws * args.e2e_steps / e2e_sec
-    w, h = (W1080, H1080) if kind == "ssimu2" else (W4K, H4K)
+    w, h = size
     kname = "ssimu2_stats" if kind == "ssimu2" else "butter_diff"
     per_pair = ssimu2_stats_bytes(w, h) if kind == "ssimu2" else butter_diff_bytes(w, h)
     peak, peak_kind = measured_peaks()
@@ -403,6 +407,11 @@ def main_ours(args):
         from vship_gb300 import build
         build.build()
     v.lib()
+    if args.skip_ssimu2:
+        b = bench_workload(v, "butter", args, ws, rank)
+        if rank == 0:
+            print(json.dumps({"metric": "frame-pairs/s (Butteraugli)", "butteraugli": b}), flush=True)
+        return
     s2 = bench_workload(v, "ssimu2", args, ws, rank)
     out = {
         "metric": "frame-pairs/s (1080p SSIMU2)", "value": s2["value"], "unit": "frame-pairs/s", "n_gpus": ws,
@@ -487,6 +496,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=4)
     ap.add_argument("--skip-butter", action="store_true")
+    ap.add_argument("--skip-ssimu2", action="store_true")
+    ap.add_argument("--ssimu2-size", default=f"{W1080}x{H1080}")
+    ap.add_argument("--butter-size", default=f"{W4K}x{H4K}")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

@@ -81,14 +81,26 @@ int map_cuda(cudaError_t e) {
         if (_rc != E_OK) return _rc;                \
     } while (0)
 
-// Copy the three planes of one frame into dense device rows of `row_bytes`.
+// Copy the three planes of one frame into dense device rows of `row_bytes`. Rows without
+// padding travel as one linear copy per plane, or as a single copy when the three planes are
+// also adjacent in host memory; padded rows use a 2-D copy that skips the padding.
 int upload_frame(uint8_t* dst, const uint8_t* const* src, int64_t stride, int64_t row_bytes, int64_t h,
                  cudaStream_t st) {
-    for (int c = 0; c < 3; c++) {
+    for (int c = 0; c < 3; c++)
         if (!src[c]) return E_BAD_POINTER;
-        TRY_CUDA(cudaMemcpy2DAsync(dst + (size_t)c * row_bytes * h, row_bytes, src[c], stride, row_bytes, h,
-                                   cudaMemcpyHostToDevice, st));
+    const size_t plane = (size_t)row_bytes * h;
+    if (stride == row_bytes) {
+        if (src[1] == src[0] + plane && src[2] == src[1] + plane) {
+            TRY_CUDA(cudaMemcpyAsync(dst, src[0], 3 * plane, cudaMemcpyHostToDevice, st));
+            return E_OK;
+        }
+        for (int c = 0; c < 3; c++)
+            TRY_CUDA(cudaMemcpyAsync(dst + (size_t)c * plane, src[c], plane, cudaMemcpyHostToDevice, st));
+        return E_OK;
     }
+    for (int c = 0; c < 3; c++)
+        TRY_CUDA(cudaMemcpy2DAsync(dst + (size_t)c * plane, row_bytes, src[c], stride, row_bytes, h,
+                                   cudaMemcpyHostToDevice, st));
     return E_OK;
 }
 
