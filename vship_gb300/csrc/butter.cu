@@ -356,8 +356,8 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ w
 constexpr int VB_TW = 32, VB_TH = 64;
 
 template <int KI, int R>
-__device__ __forceinline__ void vblur3(float* in, float* __restrict__ work, const BGeom& g, int pair, int s, int src_id,
-                                       float out[3][8]) {
+__device__ __forceinline__ void vblur3(float* in, float* ctr, float* __restrict__ work, const BGeom& g, int pair,
+                                       int s, int src_id, int ctr_id, int nctr, float out[3][8]) {
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * VB_TW, y0 = blockIdx.y * VB_TH;
     constexpr int IH = VB_TH + 2 * R;
@@ -365,6 +365,10 @@ __device__ __forceinline__ void vblur3(float* in, float* __restrict__ work, cons
     for (int c = 0; c < 3; c++)
         stage_rows<256>(in + c * IH * VB_TW, VB_TW, bplane(work, g, S, pair, src_id + c), S.p, S.w, S.h, x0, y0 - R,
                         IH, VB_TW / 4);
+    // the epilogue's own-pixel planes, staged with the blur input so their latency overlaps
+    for (int c = 0; c < nctr; c++)
+        stage_rows<256>(ctr + c * VB_TH * VB_TW, VB_TW, bplane(work, g, S, pair, ctr_id + c), S.p, S.w, S.h, x0, y0,
+                        VB_TH, VB_TW / 4);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -389,14 +393,17 @@ __device__ __forceinline__ void vblur3(float* in, float* __restrict__ work, cons
 }
 
 // LF vertical pass: D = XYB - LF (in place over XYB) and LF vals (separatefrequencies.hpp:3-12)
+constexpr int kVLfSmem = (3 * (VB_TH + 42) * VB_TW + 3 * VB_TH * VB_TW) * 4;
 __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ work, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
+    float* ctr = sm + 3 * (VB_TH + 42) * VB_TW;
     const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
     float lf[3][8];
-    vblur3<4, 21>(sm, work, g, pair, s, P_TMP + img * 3, lf);
+    vblur3<4, 21>(sm, ctr, work, g, pair, s, P_TMP + img * 3, P_XYB + img * 3, 3, lf);
     const BScaleDev S = pick_scale(g, s);
-    const int x = blockIdx.x * VB_TW + (threadIdx.x & 31);
-    const int yb = blockIdx.y * VB_TH + 8 * (threadIdx.x >> 5);
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    const int x = blockIdx.x * VB_TW + vc;
+    const int yb = blockIdx.y * VB_TH + 8 * vg;
     if (x >= S.w) return;
     float* xyb[3];
     float* lfv[3];
@@ -408,18 +415,19 @@ __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ wo
 #pragma unroll
     for (int o = 0; o < 8; o++) {
         const int y = yb + o;
-        if (y >= S.h) break;
-        const int64_t i = (int64_t)y * S.p + x;
+        if (y < S.h) {
+            const int64_t i = (int64_t)y * S.p + x;
 #pragma unroll
-        for (int c = 0; c < 3; c++) xyb[c][i] = xyb[c][i] - lf[c][o];
-        float vx = lf[0][o], vy = lf[1][o], vb = lf[2][o];
-        vb = vb + -0.362267051518f * vy;
-        vb = vb * 49.87984651440f;
-        vx = vx * 33.832837186260f;
-        vy = vy * 14.458268100570f;
-        lfv[0][i] = vx;
-        lfv[1][i] = vy;
-        lfv[2][i] = vb;
+            for (int c = 0; c < 3; c++) xyb[c][i] = ctr[(c * VB_TH + 8 * vg + o) * VB_TW + vc] - lf[c][o];
+            float vx = lf[0][o], vy = lf[1][o], vb = lf[2][o];
+            vb = vb + -0.362267051518f * vy;
+            vb = vb * 49.87984651440f;
+            vx = vx * 33.832837186260f;
+            vy = vy * 14.458268100570f;
+            lfv[0][i] = vx;
+            lfv[1][i] = vy;
+            lfv[2][i] = vb;
+        }
     }
 }
 
@@ -441,14 +449,17 @@ __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
 
 // MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
 // written over the D planes (separatefrequencies.hpp:37-99,160-187).
+constexpr int kVMfSmem = (3 * (VB_TH + 18) * VB_TW + 2 * VB_TH * VB_TW) * 4;
 __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ work, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
+    float* ctr = sm + 3 * (VB_TH + 18) * VB_TW;
     const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
     float mf[3][8];
-    vblur3<3, 9>(sm, work, g, pair, s, P_TMP + img * 3, mf);
+    vblur3<3, 9>(sm, ctr, work, g, pair, s, P_TMP + img * 3, P_XYB + img * 3, 2, mf);
     const BScaleDev S = pick_scale(g, s);
-    const int x = blockIdx.x * VB_TW + (threadIdx.x & 31);
-    const int yb = blockIdx.y * VB_TH + 8 * (threadIdx.x >> 5);
+    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
+    const int x = blockIdx.x * VB_TW + vc;
+    const int yb = blockIdx.y * VB_TH + 8 * vg;
     if (x >= S.w) return;
     float* d0 = bplane(work, g, S, pair, P_XYB + img * 3 + 0);
     float* d1 = bplane(work, g, S, pair, P_XYB + img * 3 + 1);
@@ -459,16 +470,18 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ wo
 #pragma unroll
     for (int o = 0; o < 8; o++) {
         const int y = yb + o;
-        if (y >= S.h) break;
-        const int64_t i = (int64_t)y * S.p + x;
-        float hx = d0[i] - mf[0][o];
-        const float hy = d1[i] - mf[1][o];
-        hx *= sx + (yw * (1.0f - sx)) / (yw + hy * hy);
-        d0[i] = hx;
-        d1[i] = hy;
-        m0[i] = remove_range(mf[0][o], 0.29f);
-        m1[i] = amplify_range(mf[1][o], 0.1f);
-        m2[i] = mf[2][o];
+        if (y < S.h) {
+            const int64_t i = (int64_t)y * S.p + x;
+            const int ci = (8 * vg + o) * VB_TW + vc;
+            float hx = ctr[ci] - mf[0][o];
+            const float hy = ctr[VB_TH * VB_TW + ci] - mf[1][o];
+            hx *= sx + (yw * (1.0f - sx)) / (yw + hy * hy);
+            d0[i] = hx;
+            d1[i] = hy;
+            m0[i] = remove_range(mf[0][o], 0.29f);
+            m1[i] = amplify_range(mf[1][o], 0.1f);
+            m2[i] = mf[2][o];
+        }
     }
 }
 
@@ -538,9 +551,10 @@ __constant__ DiffParams c_dp;
 __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) {
     const float absval = 0.5f * fabsf(a) + 0.5f * fabsf(b);
     const float diff = a - b;
-    const float scaler = m.n2gt / (m.norm1 + absval);
+    const float inv = __frcp_rn(m.norm1 + absval);  // one reciprocal for both scalers
+    const float scaler = m.n2gt * inv;
     float v = scaler * diff;
-    const float scaler2 = m.n2lt / (m.norm1 + absval);
+    const float scaler2 = m.n2lt * inv;
     const float fabs0 = fabsf(a);
     const float too_small = 0.55f * fabs0, too_big = 1.05f * fabs0;
     float impact = 0.0f;
@@ -672,7 +686,11 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
         }
         __syncthreads();
         const MaltaMap mm = c_dp.mm[m];
-        for (int e = threadIdx.x; e < DF_RAW; e += 256) Dt[e] = malta_pre(r0[e], r1[e], mm);
+#pragma unroll
+        for (int k = 0; k < (DF_RAW + 255) / 256; k++) {
+            const int e = threadIdx.x + 256 * k;
+            if (e < DF_RAW) Dt[e] = malta_pre(r0[e], r1[e], mm);
+        }
         __syncthreads();
         float res[8];
         if (m < 2) malta_column<true>(Dt, 8 * vg, vc, res);
@@ -893,10 +911,20 @@ __global__ void __launch_bounds__(256) butter_finalize_kernel(const float* __res
     double sq = 0.0, s3 = 0.0;
     float mx = 0.f;
     const float* p = partials + (int64_t)pair * 3 * g.norm_tiles;
-    for (int t = tid; t < g.norm_tiles; t += 256) {
-        sq += (double)__ldg(p + t);
-        s3 += (double)__ldg(p + g.norm_tiles + t);
-        mx = fmaxf(mx, __ldg(p + 2 * g.norm_tiles + t));
+    // float partial sums of 8 tiles at a time (loads issued together), combined in FP64
+    for (int t0 = tid; t0 < g.norm_tiles; t0 += 256 * 8) {
+        float a = 0.f, b = 0.f;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int t = t0 + 256 * k;
+            if (t < g.norm_tiles) {
+                a += __ldg(p + t);
+                b += __ldg(p + g.norm_tiles + t);
+                mx = fmaxf(mx, __ldg(p + 2 * g.norm_tiles + t));
+            }
+        }
+        sq += (double)a;
+        s3 += (double)b;
     }
     sq = warp_sum(sq);
     s3 = warp_sum(s3);
@@ -985,8 +1013,6 @@ static DiffParams make_diff_params() {
 }
 
 constexpr int kTileSmem = (2 * TB_RAW + TB_HPL) * 4;
-constexpr int kVLfSmem = 3 * (VB_TH + 42) * VB_TW * 4;
-constexpr int kVMfSmem = 3 * (VB_TH + 18) * VB_TW * 4;
 
 int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensity_, int max_pairs_) {
     w = width;
@@ -1005,12 +1031,12 @@ int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensit
     int rc = upload_butter_tables();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
     {
         const DiffParams P = make_diff_params();
         VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
     }
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
     VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * work_floats * max_pairs));
     VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
     VSHIP_CUDA_TRY(cudaMalloc(&distmap, sizeof(float) * (size_t)w * h * max_pairs));

@@ -28,6 +28,7 @@ namespace vship {
 // ssimu2/gaussianblur.hpp:7-18 builds them.
 __constant__ float c_s2_k[17];
 __constant__ float c_s2_I[18];
+__constant__ f2_t c_s2_k2[17];  // {k, k} pairs for the f32x2 FMA
 // SSIMULACRA2 feature weights (ssimu2/score.hpp:272-379), FP64.
 __constant__ double c_s2_w[108];
 
@@ -64,6 +65,9 @@ static int upload_constants_once() {
     }
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k, k, sizeof(k)));
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_I, I, sizeof(I)));
+    float k2[34];
+    for (int i = 0; i < 17; i++) k2[2 * i] = k2[2 * i + 1] = k[i];
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k2, k2, sizeof(k2)));
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_w, kSsimu2Weights, sizeof(kSsimu2Weights)));
     return E_OK;
 }
@@ -186,7 +190,9 @@ constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte 
 constexpr int ST_HP = 33;                // horizontal-pass output pitch
 constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
 constexpr int ST_HPLANE = ST_IH * ST_HP;
-constexpr int kStatsSmem = (2 * 2 * ST_RAW + 5 * ST_HPLANE + 3 * 8 * 6) * 4;  // 2 stages x 2 images, 5 moments, pools
+// smem: 2 stages x 2 raw images, the horizontal pass as two float-pair planes {m1,m2} and
+// {s11,s22} plus one float plane s12, and the per-warp pools
+constexpr int kStatsSmem = (2 * 2 * ST_RAW + 5 * ST_HPLANE + 3 * 8 * 6) * 4;
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
@@ -236,8 +242,10 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool interior = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h;
 
-    // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23)
-    const int hr = tid >> 2, hg = tid & 3;
+    // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23).
+    // A warp covers 8 consecutive rows x 4 column groups, which keeps the float4 raw reads, the
+    // float-pair stores (pitch 33 pairs) and the float stores (pitch 33) bank-conflict free.
+    const int hr = 8 * warp + (lane & 7), hg = lane >> 3;
     // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5. Both passes' border
     // renormalisations (out / tot, gaussianblur.hpp:63-92) are applied here as one product.
     const int vc = tid & 31, vg = tid >> 5;
@@ -282,11 +290,18 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
             __syncthreads();
         }
         {
-            float h[5][8];
+            // Horizontal pass. Lane mapping: row hr = 8*warp + (lane & 7), outputs 8*hg..+7 with
+            // hg = lane >> 3. The reference / distorted moments travel as float pairs through the
+            // f32x2 FMA: {a, b} and {a^2, b^2} share every weight; a*b is scalar.
+            f2_t h1[8], h2[8];
+            float h3[8];
+            const f2_t z2 = f2_pack(0.f, 0.f);
 #pragma unroll
-            for (int q = 0; q < 5; q++)
-#pragma unroll
-                for (int o = 0; o < 8; o++) h[q][o] = 0.f;
+            for (int o = 0; o < 8; o++) {
+                h1[o] = z2;
+                h2[o] = z2;
+                h3[o] = 0.f;
+            }
             const float* ra = r1 + hr * ST_RP + 8 * hg;
             const float* rb = r2 + hr * ST_RP + 8 * hg;
 #pragma unroll
@@ -299,43 +314,61 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
                 for (int u = 0; u < 4; u++) {
                     const int j = 4 * j4 + u;
                     const float a = la[u] - shift, b = lb[u] - shift;
-                    const float aa = a * a, bb = b * b, ab = a * b;
+                    const f2_t p1 = f2_pack(a, b);
+                    const f2_t p2 = f2_mul(p1, p1);
+                    const float ab = a * b;
 #pragma unroll
                     for (int o = 0; o < 8; o++) {
                         const int i = j - o;  // tap index
                         if (i >= 0 && i < 17) {
-                            const float k = c_s2_k[i];
-                            h[0][o] = fmaf(a, k, h[0][o]);
-                            h[1][o] = fmaf(b, k, h[1][o]);
-                            h[2][o] = fmaf(aa, k, h[2][o]);
-                            h[3][o] = fmaf(bb, k, h[3][o]);
-                            h[4][o] = fmaf(ab, k, h[4][o]);
+                            h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
+                            h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
+                            h3[o] = fmaf(ab, c_s2_k[i], h3[o]);
                         }
                     }
                 }
             }
+            f2_t* d1 = reinterpret_cast<f2_t*>(hb) + hr * ST_HP + 8 * hg;
+            f2_t* d2 = reinterpret_cast<f2_t*>(hb + 2 * ST_HPLANE) + hr * ST_HP + 8 * hg;
+            float* d3 = hb + 4 * ST_HPLANE + hr * ST_HP + 8 * hg;
 #pragma unroll
-            for (int q = 0; q < 5; q++) {
-                float* dst = hb + q * ST_HPLANE + hr * ST_HP + 8 * hg;
-#pragma unroll
-                for (int o = 0; o < 8; o++) dst[o] = h[q][o];
+            for (int o = 0; o < 8; o++) {
+                d1[o] = h1[o];
+                d2[o] = h2[o];
+                d3[o] = h3[o];
             }
         }
         __syncthreads();
-        // vertical pass + maps
+        // vertical pass + maps (column vc, rows 6*vg .. 6*vg+5)
         float m[5][6];
+        {
+            const f2_t* c1 = reinterpret_cast<const f2_t*>(hb) + (6 * vg) * ST_HP + vc;
+            const f2_t* c2 = reinterpret_cast<const f2_t*>(hb + 2 * ST_HPLANE) + (6 * vg) * ST_HP + vc;
+            const float* c3 = hb + 4 * ST_HPLANE + (6 * vg) * ST_HP + vc;
 #pragma unroll
-        for (int q = 0; q < 5; q++) {
-            const float* col = hb + q * ST_HPLANE + (6 * vg) * ST_HP + vc;
+            for (int q = 0; q < 2; q++) {
+                const f2_t* col = q == 0 ? c1 : c2;
+                f2_t v[22];
+#pragma unroll
+                for (int j = 0; j < 22; j++) v[j] = col[j * ST_HP];
+#pragma unroll
+                for (int o = 0; o < 6; o++) {
+                    f2_t a = f2_pack(0.f, 0.f);
+#pragma unroll
+                    for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], c_s2_k2[i], a);
+                    a = f2_mul(a, f2_pack(rxy[o], rxy[o]));
+                    f2_unpack(a, m[2 * q][o], m[2 * q + 1][o]);
+                }
+            }
             float v[22];
 #pragma unroll
-            for (int j = 0; j < 22; j++) v[j] = col[j * ST_HP];
+            for (int j = 0; j < 22; j++) v[j] = c3[j * ST_HP];
 #pragma unroll
             for (int o = 0; o < 6; o++) {
                 float a = 0.f;
 #pragma unroll
                 for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_s2_k[i], a);
-                m[q][o] = a * rxy[o];
+                m[4][o] = a * rxy[o];
             }
         }
         float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
