@@ -192,11 +192,16 @@ def make_inputs(kind: str, npairs: int, device, size):
     dist = "dct" if kind == "ssimu2" else "blur_noise"
     ref = torch.empty((npairs, 3, h, w), dtype=torch.float32, device=device)
     dst = torch.empty_like(ref)
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    # the same frames as 10-bit 4:2:0 planes (uint16 containers): [pair][image] -> (Y, Cb, Cr)
+    yuv = torch.empty((npairs, 2, h * w + 2 * ch * cw), dtype=torch.int16, device=device)
     for t in range(npairs):
         r, d = synth.yuv420p10_frames(h, w, t, seed=7 if kind == "ssimu2" else 11, distortion=dist, device=device)
         ref[t] = synth.yuv420p10_to_rgb(r)
         dst[t] = synth.yuv420p10_to_rgb(d)
-    return ref, dst
+        for m, f in enumerate((r, d)):
+            yuv[t, m] = torch.cat([p.reshape(-1) for p in f]).to(torch.int16)
+    return ref, dst, yuv
 
 
 def frames_table(v, ref, dst, start, count):
@@ -207,10 +212,25 @@ def frames_table(v, ref, dst, start, count):
     return v.device_frames_table(frames)
 
 
-def run_device(v, kind, ref, dst, steps, warmup, ws, chunk):
+def yuv_table(v, yuv, start, count):
+    yuvt, (w, h) = yuv
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    frames = []
+    for t in range(start, start + count):
+        for m in range(2):
+            base = yuvt[t, m].data_ptr()
+            frames.append(([base, base + 2 * h * w, base + 2 * (h * w + ch * cw)], 2 * w, 2 * cw))
+    return v.device_frames_table(frames)
+
+
+def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None):
     """Batched device-resident throughput; returns (seconds for `steps` steps, profile dict, launches)."""
     import torch
-    npairs, _, h, w = ref.shape
+    if yuv is not None:
+        yuvt, (w, h) = yuv
+        npairs = yuvt.shape[0]
+    else:
+        npairs, _, h, w = ref.shape
     if kind == "ssimu2":
         eng = v.SSIMU2Batch(w, h, chunk)
         out = torch.zeros(npairs, dtype=torch.float64, device="cuda")
@@ -220,15 +240,16 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk):
     tables = []
     for s in range(0, npairs, chunk):
         c = min(chunk, npairs - s)
-        tables.append((s, c, frames_table(v, ref, dst, s, c)))
+        tables.append((s, c, frames_table(v, ref, dst, s, c) if yuv is None else yuv_table(v, yuv, s, c)))
     stream = torch.cuda.current_stream()
+    itype = v.IN_FLOAT if yuv is None else v.IN_YUV420P10
 
     def step():
         for s, c, tb in tables:
             if kind == "ssimu2":
-                eng.compute_async(tb.data_ptr(), c, v.IN_FLOAT, out[s:].data_ptr(), stream.cuda_stream)
+                eng.compute_async(tb.data_ptr(), c, itype, out[s:].data_ptr(), stream.cuda_stream)
             else:
-                eng.compute_async(tb.data_ptr(), c, v.IN_FLOAT, out[3 * s:].data_ptr(), 0, stream.cuda_stream)
+                eng.compute_async(tb.data_ptr(), c, itype, out[3 * s:].data_ptr(), 0, stream.cuda_stream)
 
     for _ in range(warmup):
         step()
@@ -254,20 +275,34 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk):
     return sec, prof, launches, result
 
 
-def run_e2e(v, kind, ref, dst, steps, warmup, nthreads):
-    """Through the reference-facing C ABI from pinned host memory, one handler per thread."""
+def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
+    """Through the C ABI from pinned host memory, one handler per thread: the reference-facing
+    float-RGB calls, or (yuv=...) the 4:2:0 extension calls."""
     import ctypes
     import numpy as np
     import torch
-    npairs, _, h, w = ref.shape
-    href = ref.cpu().pin_memory()
-    hdst = dst.cpu().pin_memory()
     L = v.lib()
     plane_ptrs = []
-    for t in range(npairs):
-        a = (ctypes.c_void_p * 3)(*[href[t, c].data_ptr() for c in range(3)])
-        b = (ctypes.c_void_p * 3)(*[hdst[t, c].data_ptr() for c in range(3)])
-        plane_ptrs.append((a, b))
+    if yuv is None:
+        npairs, _, h, w = ref.shape
+        href = ref.cpu().pin_memory()
+        hdst = dst.cpu().pin_memory()
+        for t in range(npairs):
+            a = (ctypes.c_void_p * 3)(*[href[t, c].data_ptr() for c in range(3)])
+            b = (ctypes.c_void_p * 3)(*[hdst[t, c].data_ptr() for c in range(3)])
+            plane_ptrs.append((a, b))
+    else:
+        yuvt, (w, h) = yuv
+        npairs = yuvt.shape[0]
+        cw, ch = (w + 1) // 2, (h + 1) // 2
+        hy = yuvt.cpu().pin_memory()
+        ystr = (ctypes.c_int64 * 3)(2 * w, 2 * cw, 2 * cw)
+        for t in range(npairs):
+            pp = []
+            for m in range(2):
+                base = hy[t, m].data_ptr()
+                pp.append((ctypes.c_void_p * 3)(base, base + 2 * h * w, base + 2 * (h * w + ch * cw)))
+            plane_ptrs.append(tuple(pp))
     stride = w * 4
     handlers = []
     for _ in range(nthreads):
@@ -288,7 +323,15 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads):
         norms = (ctypes.c_double * 3)()
         for i in range(k, npairs, nthreads):
             a, b = plane_ptrs[i]
-            if kind == "ssimu2":
+            if yuv is not None and kind == "ssimu2":
+                rc = L.Vship_ComputeSSIMU2Yuv420p10(hd, ctypes.byref(sc), ctypes.cast(a, v._PP), ystr,
+                                                    ctypes.cast(b, v._PP), ystr)
+                scores[i] = sc.value
+            elif yuv is not None:
+                rc = L.Vship_ComputeButteraugliYuv420p10(hd, norms, None, 0, ctypes.cast(a, v._PP), ystr,
+                                                         ctypes.cast(b, v._PP), ystr)
+                scores[i] = norms[0]
+            elif kind == "ssimu2":
                 rc = L.Vship_ComputeSSIMU2Float(hd, ctypes.byref(sc), ctypes.cast(a, v._PP), ctypes.cast(b, v._PP),
                                                 stride)
                 scores[i] = sc.value
@@ -319,7 +362,7 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads):
             L.Vship_ButteraugliFree(hd)
     if errors:
         raise v.VshipError(errors[0], "e2e compute")
-    h2d = npairs * 2 * 3 * w * h * 4
+    h2d = npairs * 2 * 3 * w * h * 4 if yuv is None else npairs * 2 * 2 * (h * w + 2 * ((w + 1) // 2) * ((h + 1) // 2))
     d2h = npairs * (8 if kind == "ssimu2" else 24)
     return sec, h2d, d2h, np.array(scores)
 
@@ -346,7 +389,7 @@ def bench_workload(v, kind, args, ws, rank):
     npairs = args.pairs if kind == "ssimu2" else args.butter_pairs
     chunk = args.chunk if kind == "ssimu2" else args.butter_chunk
     size = parse_size(args.ssimu2_size if kind == "ssimu2" else args.butter_size)
-    ref, dst = make_inputs(kind, npairs, "cuda", size)
+    ref, dst, yuv = make_inputs(kind, npairs, "cuda", size)
     torch.cuda.synchronize()
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
@@ -371,8 +414,17 @@ def bench_workload(v, kind, args, ws, rank):
     pairs_per_launch = npairs * args.steps / max(n_launch, 1)
     traffic = ncu_traffic(kname)
     total_kernel_ms = sum(t for _, t in prof.values())
+    # the same workload from 10-bit 4:2:0 input converted on the GPU (the configuration's native
+    # format: a quarter of the bytes of float RGB)
+    ysec, _, _, _ = run_device(v, kind, None, None, args.steps, args.warmup, ws, chunk, yuv=(yuv, size))
+    ysec = max_over_ranks(ysec, ws)
+    ye2e_sec, yh2d, _, _ = run_e2e(v, kind, None, None, args.e2e_steps, 1, args.e2e_threads, yuv=(yuv, size))
+    ye2e_sec = max_over_ranks(ye2e_sec, ws)
     res = {
         "value": value, "unit": "frame-pairs/s", "ms_per_step": sec / args.steps * 1e3,
+        "yuv420p10": {"value": npairs * ws * args.steps / ysec,
+                      "e2e": {"value": npairs * ws * args.e2e_steps / ye2e_sec, "unit": "frame-pairs/s",
+                              "h2d_bytes_per_step": yh2d, "d2h_bytes_per_step": d2h}},
         "pairs_per_step": npairs,
         "e2e": {"value": e2e_value, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "threads": args.e2e_threads, "steps": args.e2e_steps},
@@ -423,13 +475,14 @@ def main_ours(args):
                    "launch_chunk_pairs": args.chunk},
         "e2e": s2["e2e"], "roofline": s2["roofline"], "gpu_launches": s2["gpu_launches"], "clocks": s2["clocks"],
         "kernel_share": s2["kernel_share"], "pipeline_bytes_per_pair": s2["pipeline_bytes_per_pair"],
+        "yuv420p10": s2["yuv420p10"],
         "score_check": s2["score_check"],
     }
     if "cpu_baseline" in s2:
         out["cpu_baseline"] = s2["cpu_baseline"]
     if not args.skip_butter:
         b = bench_workload(v, "butter", args, ws, rank)
-        out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e",
+        out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e", "yuv420p10",
                                                    "roofline", "gpu_launches", "clocks", "kernel_share",
                                                    "pipeline_bytes_per_pair", "score_check")
                                  if k in b}

@@ -179,20 +179,37 @@ EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliUint16v3(Vship_Butterau
                                                                   const uint8_t* srcp1[3], const uint8_t* srcp2[3],
                                                                   int64_t stride, int64_t stride2);
 
-/* Sample formats of the device-resident entry points (numbered as the reference's InputMemType,
- * src/util/preprocessor.hpp:94). */
+/* Sample formats of the device-resident entry points (0..3 numbered as the reference's
+ * InputMemType, src/util/preprocessor.hpp:94). Vship_InYuv420p10 is 10-bit 4:2:0 Y'CbCr in
+ * 16-bit little-endian containers, BT.709 limited range, converted on the GPU to full-range
+ * R'G'B' (chroma upsampled bilinearly with MPEG-2 siting) -- the conversion the reference's
+ * front-ends do on the CPU before calling the ABI, at a quarter of the bytes of float RGB. */
 typedef enum {
     Vship_InUint8 = 0,
     Vship_InUint16 = 1,
     Vship_InHalf = 2,
     Vship_InFloat = 3,
+    Vship_InYuv420p10 = 4,
 } Vship_InputType;
 
-/* One frame resident in device memory: three planes (R, G, B) and the row pitch in bytes. */
+/* One frame resident in device memory: three planes (R, G, B, or Y, Cb, Cr) and row pitches in
+ * bytes (`stride` for RGB planes and luma, `stride_c` for the two chroma planes). */
 typedef struct {
     const uint8_t* plane[3];
     int64_t stride;
+    int64_t stride_c;
 } Vship_DeviceFrame;
+
+/* Host-buffer scoring of 10-bit 4:2:0 Y'CbCr frames (see Vship_InYuv420p10): planes Y, Cb, Cr
+ * with their own row strides in bytes (stride1[3], stride2[3]). Synchronous like the reference's
+ * compute calls; handlers come from Vship_SSIMU2Init / Vship_ButteraugliInit[v2]. */
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2Yuv420p10(Vship_SSIMU2Handler handler, double* score,
+                                                              const uint8_t* srcp1[3], const int64_t stride1[3],
+                                                              const uint8_t* srcp2[3], const int64_t stride2[3]);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliYuv420p10(Vship_ButteraugliHandler handler, double norms[3],
+                                                                   const uint8_t* dstp, int64_t dststride,
+                                                                   const uint8_t* srcp1[3], const int64_t stride1[3],
+                                                                   const uint8_t* srcp2[3], const int64_t stride2[3]);
 
 /* Batched, device-resident SSIMU2 for callers whose frames already live in GPU memory (decoders,
  * encoders' candidate buffers): one launch scores up to max_pairs pairs of one resolution.

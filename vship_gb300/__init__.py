@@ -26,7 +26,7 @@ EXCEPTION_NAMES = ["NoError", "OutOfVRAM", "OutOfRAM", "DifferingInputType", "No
                    "BadErrorType"]
 
 # Vship_InputType
-IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT = 0, 1, 2, 3
+IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT, IN_YUV420P10 = 0, 1, 2, 3, 4
 
 
 class VshipError(RuntimeError):
@@ -55,7 +55,7 @@ class ButteraugliScore(ctypes.Structure):
 
 
 class DeviceFrame(ctypes.Structure):
-    _fields_ = [("plane", ctypes.c_void_p * 3), ("stride", ctypes.c_int64)]
+    _fields_ = [("plane", ctypes.c_void_p * 3), ("stride", ctypes.c_int64), ("stride_c", ctypes.c_int64)]
 
 
 # Every exported entry point: name -> (restype, argtypes). The tests check this list against
@@ -95,6 +95,11 @@ SIGNATURES = {
                                              _PP, _PP, ctypes.c_int64, ctypes.c_int64]),
     "Vship_ComputeButteraugliUint16v3": (_E, [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
                                               ctypes.c_int64, _PP, _PP, ctypes.c_int64, ctypes.c_int64]),
+    "Vship_ComputeSSIMU2Yuv420p10": (_E, [_H, ctypes.POINTER(ctypes.c_double), _PP, ctypes.POINTER(ctypes.c_int64),
+                                          _PP, ctypes.POINTER(ctypes.c_int64)]),
+    "Vship_ComputeButteraugliYuv420p10": (_E, [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int64,
+                                               _PP, ctypes.POINTER(ctypes.c_int64), _PP,
+                                               ctypes.POINTER(ctypes.c_int64)]),
     "Vship_SSIMU2BatchInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "Vship_SSIMU2ComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_void_p]),
@@ -204,6 +209,19 @@ def planes_of(frame):
     return arr, strides.pop(), w, h, dt, planes
 
 
+def _yuv_planes(frame, w, h):
+    """(Y, Cb, Cr) uint16 arrays of a w x h 4:2:0 frame -> (pointer array, stride array)."""
+    planes = [np.asarray(p) for p in frame]
+    cw, ch = (w + 1) // 2, (h + 1) // 2
+    shapes = [(h, w), (ch, cw), (ch, cw)]
+    for p, shp in zip(planes, shapes):
+        if p.dtype != np.uint16 or p.shape != shp or p.strides[1] != 2:
+            raise VshipError(DifferingInputType, "4:2:0 planes must be uint16 (h, w), (ceil(h/2), ceil(w/2)) x2")
+    ptrs = (ctypes.c_void_p * 3)(*[p.ctypes.data for p in planes])
+    strides = (ctypes.c_int64 * 3)(*[p.strides[0] for p in planes])
+    return ptrs, strides
+
+
 class SSIMU2Handler:
     """One SSIMULACRA2 scorer for a fixed resolution (Vship_SSIMU2Init / Compute / Free)."""
 
@@ -221,6 +239,15 @@ class SSIMU2Handler:
         f = lib().Vship_ComputeSSIMU2Floatv2 if dt == np.float32 else lib().Vship_ComputeSSIMU2Uint16v2
         _check(f(self._h, ctypes.byref(out), ctypes.cast(a1, _PP), ctypes.cast(a2, _PP), s1, s2),
                "Vship_ComputeSSIMU2")
+        return out.value
+
+    def compute_yuv420p10(self, reference, distorted) -> float:
+        """Score 10-bit 4:2:0 frames given as (Y, Cb, Cr) uint16 arrays (Vship_ComputeSSIMU2Yuv420p10)."""
+        a1, s1 = _yuv_planes(reference, self.width, self.height)
+        a2, s2 = _yuv_planes(distorted, self.width, self.height)
+        out = ctypes.c_double()
+        _check(lib().Vship_ComputeSSIMU2Yuv420p10(self._h, ctypes.byref(out), ctypes.cast(a1, _PP), s1,
+                                                  ctypes.cast(a2, _PP), s2), "Vship_ComputeSSIMU2Yuv420p10")
         return out.value
 
     def free(self):
@@ -262,6 +289,18 @@ class ButteraugliHandler:
         f = lib().Vship_ComputeButteraugliFloatv3 if dt == np.float32 else lib().Vship_ComputeButteraugliUint16v3
         _check(f(self._h, norms, dm.ctypes.data if dm is not None else None, w * 4,
                  ctypes.cast(a1, _PP), ctypes.cast(a2, _PP), s1, s2), "Vship_ComputeButteraugli")
+        res = (norms[0], norms[1], norms[2])
+        return (res, dm) if distmap else res
+
+    def compute_yuv420p10(self, reference, distorted, distmap: bool = False):
+        """Butteraugli of 10-bit 4:2:0 frames given as (Y, Cb, Cr) uint16 arrays."""
+        a1, s1 = _yuv_planes(reference, self.width, self.height)
+        a2, s2 = _yuv_planes(distorted, self.width, self.height)
+        norms = (ctypes.c_double * 3)()
+        dm = np.empty((self.height, self.width), np.float32) if distmap else None
+        _check(lib().Vship_ComputeButteraugliYuv420p10(self._h, norms, dm.ctypes.data if dm is not None else None,
+                                                       self.width * 4, ctypes.cast(a1, _PP), s1,
+                                                       ctypes.cast(a2, _PP), s2), "Vship_ComputeButteraugliYuv420p10")
         res = (norms[0], norms[1], norms[2])
         return (res, dm) if distmap else res
 
@@ -341,14 +380,16 @@ class ButteraugliBatch:
 
 
 def device_frames_table(frames, device="cuda"):
-    """Pack [(planes, stride_bytes), ...] of device pointers into a device array of
-    Vship_DeviceFrame (32 bytes each) held in a torch uint8 tensor."""
+    """Pack [(planes, stride_bytes[, chroma_stride_bytes]), ...] of device pointers into a device
+    array of Vship_DeviceFrame held in a torch uint8 tensor."""
     import torch
 
     arr = (DeviceFrame * len(frames))()
-    for i, (planes, stride) in enumerate(frames):
+    for i, fr in enumerate(frames):
+        planes, stride = fr[0], fr[1]
         for c in range(3):
             arr[i].plane[c] = int(planes[c])
         arr[i].stride = int(stride)
+        arr[i].stride_c = int(fr[2]) if len(fr) > 2 else int(stride)
     host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
     return host.to(device)

@@ -109,7 +109,7 @@ struct HostPath {
     int device = 0;
     cudaStream_t stream = nullptr;
     uint8_t* staging = nullptr;      // 2 frames x 3 planes x h x (w*4) bytes
-    FrameDesc* frames_d = nullptr;   // [0..1]: 2-byte samples, [2..3]: 4-byte samples
+    FrameDesc* frames_d = nullptr;   // [0..1]: 2-byte samples, [2..3]: 4-byte, [4..5]: YUV 4:2:0
     void* result_h = nullptr;        // pinned
     std::mutex mu;                   // one compute at a time per handler
 
@@ -118,14 +118,20 @@ struct HostPath {
         TRY_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         const size_t plane4 = (size_t)w * 4 * h;
         TRY_CUDA(cudaMalloc(&staging, plane4 * 6));
-        TRY_CUDA(cudaMalloc(&frames_d, sizeof(FrameDesc) * 4));
-        FrameDesc fd[4];
+        TRY_CUDA(cudaMalloc(&frames_d, sizeof(FrameDesc) * 6));
+        FrameDesc fd[6];
         for (int bps = 2, k = 0; bps <= 4; bps += 2, k++)
             for (int m = 0; m < 2; m++) {
                 const size_t plane = (size_t)w * bps * h;
                 for (int c = 0; c < 3; c++) fd[k * 2 + m].plane[c] = staging + (size_t)(m * 3 + c) * plane;
                 fd[k * 2 + m].stride = w * bps;
+                fd[k * 2 + m].stride_c = w * bps;
             }
+        for (int m = 0; m < 2; m++) {  // YUV: planes at the float-plane slots of each frame
+            for (int c = 0; c < 3; c++) fd[4 + m].plane[c] = staging + (size_t)(m * 3 + c) * plane4;
+            fd[4 + m].stride = w * 2;
+            fd[4 + m].stride_c = ((w + 1) / 2) * 2;
+        }
         TRY_CUDA(cudaMemcpy(frames_d, fd, sizeof(fd), cudaMemcpyHostToDevice));
         if (cudaMallocHost(&result_h, result_bytes) != cudaSuccess) return E_OUT_OF_RAM;
         return E_OK;
@@ -153,6 +159,29 @@ struct HostPath {
         rc = upload_frame(staging + 3 * plane, s2, stride2, row, h, stream);
         if (rc) return rc;
         *fd_out = frames_d + (bps == 4 ? 2 : 0);
+        return E_OK;
+    }
+    // Uploads two 4:2:0 frames (Y, Cb, Cr with their own strides) into the YUV slots.
+    int upload_yuv(const uint8_t* const* s1, const int64_t* st1, const uint8_t* const* s2, const int64_t* st2,
+                   int64_t w, int64_t h, const FrameDesc** fd_out) {
+        if (!s1 || !s2 || !st1 || !st2) return E_BAD_POINTER;
+        const int64_t cw = (w + 1) / 2, ch = (h + 1) / 2;
+        const size_t plane4 = (size_t)w * 4 * h;
+        for (int m = 0; m < 2; m++) {
+            const uint8_t* const* src = m == 0 ? s1 : s2;
+            const int64_t* st = m == 0 ? st1 : st2;
+            for (int c = 0; c < 3; c++) {
+                if (!src[c]) return E_BAD_POINTER;
+                const int64_t row = (c == 0 ? w : cw) * 2, rows = c == 0 ? h : ch;
+                if (st[c] < row) return E_BAD_POINTER;
+                uint8_t* dst = staging + (size_t)(m * 3 + c) * plane4;
+                if (st[c] == row)
+                    TRY_CUDA(cudaMemcpyAsync(dst, src[c], (size_t)row * rows, cudaMemcpyHostToDevice, stream));
+                else
+                    TRY_CUDA(cudaMemcpy2DAsync(dst, row, src[c], st[c], row, rows, cudaMemcpyHostToDevice, stream));
+            }
+        }
+        *fd_out = frames_d + 4;
         return E_OK;
     }
 };
@@ -216,7 +245,7 @@ __global__ void probe_kernel(int* out) { *out = 4320984; }
 // compute bodies
 
 int ssimu2_compute(int id, double* score, const uint8_t* s1[3], const uint8_t* s2[3], int64_t stride1,
-                   int64_t stride2, int intype) {
+                   int64_t stride2, int intype, const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr) {
     Ssimu2Handle* h = g_ssimu2.get(id);
     if (!h || !h->host_io) return E_BAD_HANDLER;
     if (!score) return E_BAD_POINTER;
@@ -224,7 +253,8 @@ int ssimu2_compute(int id, double* score, const uint8_t* s1[3], const uint8_t* s
     DeviceGuard dg(h->io.device);
     const int bps = intype == IN_FLOAT ? 4 : 2;
     const FrameDesc* fd = nullptr;
-    int rc = h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
+    int rc = intype == IN_YUV420P10 ? h->io.upload_yuv(s1, ystr1, s2, ystr2, h->eng.w, h->eng.h, &fd)
+                                    : h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
     if (rc) return rc;
     rc = h->eng.launch(fd, intype, 1, nullptr, h->io.stream);
     if (rc) return rc;
@@ -235,14 +265,16 @@ int ssimu2_compute(int id, double* score, const uint8_t* s1[3], const uint8_t* s
 }
 
 int butter_compute(int id, double norms[3], const uint8_t* dstp, int64_t dststride, const uint8_t* s1[3],
-                   const uint8_t* s2[3], int64_t stride1, int64_t stride2, int intype) {
+                   const uint8_t* s2[3], int64_t stride1, int64_t stride2, int intype,
+                   const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr) {
     ButterHandle* h = g_butter.get(id);
     if (!h || !h->host_io) return E_BAD_HANDLER;
     std::lock_guard<std::mutex> lk(h->io.mu);
     DeviceGuard dg(h->io.device);
     const int bps = intype == IN_FLOAT ? 4 : 2;
     const FrameDesc* fd = nullptr;
-    int rc = h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
+    int rc = intype == IN_YUV420P10 ? h->io.upload_yuv(s1, ystr1, s2, ystr2, h->eng.w, h->eng.h, &fd)
+                                    : h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
     if (rc) return rc;
     rc = h->eng.launch(fd, intype, 1, nullptr, h->io.stream);
     if (rc) return rc;
@@ -435,6 +467,12 @@ Vship_Exception Vship_ComputeSSIMU2Uint16v2(Vship_SSIMU2Handler handler, double*
     return to_exc(ssimu2_compute(handler.id, score, srcp1, srcp2, stride, stride2, IN_UINT16));
 }
 
+Vship_Exception Vship_ComputeSSIMU2Yuv420p10(Vship_SSIMU2Handler handler, double* score, const uint8_t* srcp1[3],
+                                             const int64_t stride1[3], const uint8_t* srcp2[3],
+                                             const int64_t stride2[3]) {
+    return to_exc(ssimu2_compute(handler.id, score, srcp1, srcp2, 0, 0, IN_YUV420P10, stride1, stride2));
+}
+
 Vship_Exception Vship_SSIMU2ComputeDeviceAsync(Vship_SSIMU2Handler handler, const Vship_DeviceFrame* frames,
                                                int npairs, Vship_InputType input_type, double* scores_dev,
                                                void* stream) {
@@ -442,7 +480,7 @@ Vship_Exception Vship_SSIMU2ComputeDeviceAsync(Vship_SSIMU2Handler handler, cons
     if (!h) return Vship_BadHandler;
     if (!frames || !scores_dev) return Vship_BadPointer;
     if (npairs <= 0 || npairs > h->eng.max_pairs) return Vship_BadPointer;
-    if ((int)input_type < 0 || (int)input_type > 3) return Vship_BadPointer;
+    if ((int)input_type < 0 || (int)input_type > 4) return Vship_BadPointer;
     static_assert(sizeof(Vship_DeviceFrame) == sizeof(FrameDesc), "frame descriptor layout");
     DeviceGuard dg(h->io.device);
     return to_exc(h->eng.launch(reinterpret_cast<const FrameDesc*>(frames), (int)input_type, npairs, scores_dev,
@@ -489,7 +527,7 @@ Vship_Exception Vship_ButteraugliComputeDeviceAsync(Vship_ButteraugliHandler han
     if (!h) return Vship_BadHandler;
     if (!frames || !norms_dev) return Vship_BadPointer;
     if (npairs <= 0 || npairs > h->eng.max_pairs) return Vship_BadPointer;
-    if ((int)input_type < 0 || (int)input_type > 3) return Vship_BadPointer;
+    if ((int)input_type < 0 || (int)input_type > 4) return Vship_BadPointer;
     DeviceGuard dg(h->io.device);
     cudaStream_t st = (cudaStream_t)stream;
     int rc = h->eng.launch(reinterpret_cast<const FrameDesc*>(frames), (int)input_type, npairs, norms_dev, st);
@@ -543,6 +581,15 @@ Vship_Exception Vship_ComputeButteraugliFloatv3(Vship_ButteraugliHandler handler
     if (!norms) return Vship_BadPointer;
     return to_exc(butter_compute(handler.id, norms, dstp, dststride, srcp1, srcp2, stride, stride2, IN_FLOAT));
 }
+Vship_Exception Vship_ComputeButteraugliYuv420p10(Vship_ButteraugliHandler handler, double norms[3],
+                                                  const uint8_t* dstp, int64_t dststride, const uint8_t* srcp1[3],
+                                                  const int64_t stride1[3], const uint8_t* srcp2[3],
+                                                  const int64_t stride2[3]) {
+    if (!norms) return Vship_BadPointer;
+    return to_exc(butter_compute(handler.id, norms, dstp, dststride, srcp1, srcp2, 0, 0, IN_YUV420P10, stride1,
+                                 stride2));
+}
+
 Vship_Exception Vship_ComputeButteraugliUint16v3(Vship_ButteraugliHandler handler, double norms[3],
                                                  const uint8_t* dstp, int64_t dststride, const uint8_t* srcp1[3],
                                                  const uint8_t* srcp2[3], int64_t stride, int64_t stride2) {

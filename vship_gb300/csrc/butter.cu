@@ -116,15 +116,17 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
     for (int r = 0; r < 4; r++) {
         const int ly = ty + 8 * r;
         const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ly;
+        float v[3] = {0.f, 0.f, 0.f};
+        if (gx < F.w && gy < F.h) {
+            load_rgb<IT>(fd, gx, gy, F.w, F.h, v[0], v[1], v[2]);
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-            float v = 0.f;
-            if (gx < F.w && gy < F.h) {
-                v = to_linear_fast(load_sample<IT>(fd.plane[c], fd.stride, gx, gy));
-                bplane(work, g, F, pair, P_LIN + img * 3 + c)[(int64_t)gy * F.p + gx] = v;
+            for (int c = 0; c < 3; c++) {
+                v[c] = to_linear_fast(v[c]);
+                bplane(work, g, F, pair, P_LIN + img * 3 + c)[(int64_t)gy * F.p + gx] = v[c];
             }
-            sm[c][ly][tx] = v;
         }
+#pragma unroll
+        for (int c = 0; c < 3; c++) sm[c][ly][tx] = v[c];
     }
     __syncthreads();
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;
@@ -1073,6 +1075,7 @@ int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
             case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
             case IN_UINT16: butter_decode_kernel<IN_UINT16><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
             case IN_HALF: butter_decode_kernel<IN_HALF><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
+            case IN_YUV420P10: butter_decode_kernel<IN_YUV420P10><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
             default: butter_decode_kernel<IN_FLOAT><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
         }
     }

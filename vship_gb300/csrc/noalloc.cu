@@ -60,7 +60,7 @@ extern "C" Vship_Exception Vship_ComputeSSIMU2DeviceNoAlloc(const Vship_DeviceFr
     using namespace vship;
     if (!reference || !distorted || !score_dev) return Vship_BadPointer;
     if (width <= 0 || height <= 0) return Vship_BadPointer;
-    if ((int)input_type < 0 || (int)input_type > 3) return Vship_BadPointer;
+    if ((int)input_type < 0 || (int)input_type > 4) return Vship_BadPointer;
     const int bps = input_type == Vship_InUint8 ? 1 : input_type == Vship_InFloat ? 4 : 2;
     for (const Vship_DeviceFrame* f : {reference, distorted}) {
         if (!f->plane[0] || !f->plane[1] || !f->plane[2]) return Vship_BadPointer;

@@ -112,9 +112,10 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
             const int gx = bx * 32 + tx, gy = by * 32 + ly;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f;
             if (gx < L.w && gy < L.h) {
-                v0 = to_linear_fast(load_sample<IT>(fd.plane[0], fd.stride, gx, gy));
-                v1 = to_linear_fast(load_sample<IT>(fd.plane[1], fd.stride, gx, gy));
-                v2 = to_linear_fast(load_sample<IT>(fd.plane[2], fd.stride, gx, gy));
+                load_rgb<IT>(fd, gx, gy, L.w, L.h, v0, v1, v2);
+                v0 = to_linear_fast(v0);
+                v1 = to_linear_fast(v1);
+                v2 = to_linear_fast(v2);
                 float X = v0, Y = v1, B = v2;
                 positive_xyb(X, Y, B);
                 int64_t o = L.off + (int64_t)gy * L.pitch + gx;
@@ -529,6 +530,7 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
         case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
         case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
         case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
+        case IN_YUV420P10: ssimu2_pyramid_kernel<IN_YUV420P10><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
         default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
     }
     }
@@ -574,6 +576,7 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
         case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
         case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
         case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
+        case IN_YUV420P10: ssimu2_pyramid_kernel<IN_YUV420P10><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
         default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
     }
     ssimu2_stats_kernel<<<dim3((unsigned)geom.tiles_total, 1u), 256, kStatsSmem, st>>>(pyr, partials, geom);
