@@ -24,6 +24,7 @@ NVCC_FLAGS = ARCH + [
     "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
 ]
 SOURCES = ["ssimu2.cu", "butter.cu", "api.cu", "profile.cu", "noalloc.cu"]
+CLI = os.path.join(HERE, "ffvship")
 
 
 def nvcc_path() -> str:
@@ -31,6 +32,15 @@ def nvcc_path() -> str:
         if cand and os.path.exists(cand):
             return cand
     raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libvship.so")
+
+
+def vapoursynth_include() -> str | None:
+    """Directory holding the VapourSynth SDK headers, if any (VAPOURSYNTH_INCLUDE or the usual
+    system locations). libvship.so is also a VapourSynth plugin when they are found."""
+    for d in (os.environ.get("VAPOURSYNTH_INCLUDE"), "/usr/include/vapoursynth", "/usr/local/include/vapoursynth"):
+        if d and os.path.exists(os.path.join(d, "VapourSynth4.h")) and os.path.exists(os.path.join(d, "VSHelper4.h")):
+            return d
+    return None
 
 
 def _needs_rebuild(obj: str, deps: list[str]) -> bool:
@@ -64,8 +74,22 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(run, jobs))
     objs = [os.path.join(BUILD, s.replace(".cu", ".o")) for s in SOURCES]
+    vsinc = vapoursynth_include()
+    if vsinc:
+        src = os.path.join(CSRC, "vs_plugin.cpp")
+        obj = os.path.join(BUILD, "vs_plugin.o")
+        if _needs_rebuild(obj, [src] + headers):
+            run(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-I" + vsinc,
+                 "-I" + os.path.join(ROOT, "include"), "-c", src, "-o", obj])
+            jobs.append("vs_plugin")
+        objs.append(obj)
     if jobs or not os.path.exists(LIB):
         run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
+    cli_src = os.path.join(CSRC, "ffvship.cpp")
+    if _needs_rebuild(CLI, [cli_src, LIB, os.path.join(ROOT, "include", "VshipAPI.h")]):
+        # the FFVship-compatible command-line tool, linked against the library next to it
+        run(["g++", "-O2", "-std=c++17", cli_src, "-I" + os.path.join(ROOT, "include"), "-L" + HERE, "-lvship",
+             "-Wl,-rpath,$ORIGIN", "-lpthread", "-o", CLI])
     return LIB
 
 

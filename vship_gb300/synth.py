@@ -182,3 +182,18 @@ def rgb_float_pair(h: int, w: int, t: int, seed: int = 7, distortion: str = "dct
     """Float32 (3, h, w) R'G'B' reference/distorted planes for pair t of a YUV sequence."""
     ref, dist = yuv420p10_frames(h, w, t, seed, distortion, device)
     return yuv420p10_to_rgb(ref), yuv420p10_to_rgb(dist)
+
+
+def write_y4m(path: str, frames, w: int, h: int, bits: int = 10, fps: str = "24:1") -> None:
+    """Write 4:2:0 frames [(Y, Cb, Cr) integer arrays] as YUV4MPEG2 (8-bit C420 or 10-bit
+    C420p10, little-endian 16-bit containers)."""
+    import numpy as np
+
+    tag = "C420p10 XYSCSS=420P10" if bits == 10 else "C420jpeg"
+    with open(path, "wb") as f:
+        f.write(f"YUV4MPEG2 W{w} H{h} F{fps} Ip A1:1 {tag}\n".encode())
+        for fr in frames:
+            f.write(b"FRAME\n")
+            for p in fr:
+                a = np.asarray(p.cpu().numpy() if hasattr(p, "cpu") else p)
+                f.write(a.astype("<u2" if bits > 8 else "u1").tobytes())
