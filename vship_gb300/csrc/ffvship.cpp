@@ -467,7 +467,7 @@ int main(int argc, char** argv) {
                 const int d = ++done;
                 std::lock_guard<std::mutex> lk(out_mu);
                 if (o.live) {
-                    std::cout << jobs[l.idx].src_frame;
+                    std::cout << std::setprecision(9) << jobs[l.idx].src_frame;
                     for (int i = 0; i < nres; i++) std::cout << " " << scores[(size_t)nres * l.idx + i];
                     std::cout << "\n";
                 } else if (d % 16 == 0 || d == nframes) {
