@@ -258,6 +258,53 @@ EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2DeviceNoAlloc(const Vship_De
                                                                   int height, Vship_InputType input_type,
                                                                   double* score_dev, void* stream);
 
+/* Batched multi-resolution scoring with source reuse -- no counterpart in the reference, whose
+ * API scores one pair of one resolution per call (src/VshipAPI.h:96-148).
+ *
+ * An encoder's quality search scores each source frame against several encodes of it. One call
+ * here scores `npairs` (source, candidate) pairs whose `nsources` sources come in up to 8
+ * resolutions: source i has resolution source_res[i] (an index into the widths/heights given
+ * at init) and candidate j is scored against source candidate_source[j]. Each source's
+ * SSIMULACRA2 XYB pyramid is built once per call and shared by all its candidates; with
+ * Vship_MultiFp16 the candidates' pyramids are stored as FP16 differences from their source's.
+ * `sources` and `candidates` are HOST arrays of frame descriptors whose planes live in device
+ * memory; ssimu2_dev receives npairs doubles, butter_norms_dev 3 doubles per pair {Qnorm,
+ * 3-norm, inf-norm} (both device memory, each required when its metric is enabled).
+ * max_sources[r] and max_pairs[r] bound the sources and pairs of resolution r in one call.
+ * The launch sequence of a batch layout (source_res, candidate_source, input_type) is captured
+ * in a CUDA graph on its first call and replayed while the layout repeats (unless
+ * Vship_MultiNoGraph). With Vship_MultiAutotune the first call of a new layout times the
+ * SSIMULACRA2 stats-launch knobs and keeps the fastest; choices are stored in the JSON file
+ * tune_cache_path (NULL: $VSHIP_TUNE_CACHE, unset: kept in memory only) and reused by later
+ * handlers. The call only enqueues device work (after waiting for the previous call's table
+ * upload); calls on one handler must be ordered on one stream. */
+typedef struct {
+    int id;
+} Vship_MultiHandler;
+typedef enum {
+    Vship_MultiSSIMU2 = 1,
+    Vship_MultiButteraugli = 2,
+    Vship_MultiFp16 = 4,
+    Vship_MultiNoGraph = 8,
+    Vship_MultiAutotune = 16,
+} Vship_MultiFlags;
+EXPORTPREPROCESS Vship_Exception Vship_MultiInit(Vship_MultiHandler* handler, int nres, const int* widths,
+                                                 const int* heights, const int* max_sources, const int* max_pairs,
+                                                 int flags, int Qnorm, float intensity_multiplier,
+                                                 const char* tune_cache_path);
+EXPORTPREPROCESS Vship_Exception Vship_MultiFree(Vship_MultiHandler handler);
+EXPORTPREPROCESS Vship_Exception Vship_MultiComputeDeviceAsync(Vship_MultiHandler handler, int nsources,
+                                                               const Vship_DeviceFrame* sources,
+                                                               const int* source_res, int npairs,
+                                                               const Vship_DeviceFrame* candidates,
+                                                               const int* candidate_source,
+                                                               Vship_InputType input_type, double* ssimu2_dev,
+                                                               double* butter_norms_dev, void* stream);
+/* The launch knobs in use as JSON (same size/truncation contract as Vship_GetErrorMessage). */
+EXPORTPREPROCESS int Vship_MultiKnobs(Vship_MultiHandler handler, char* out_json, int len);
+EXPORTPREPROCESS uint64_t Vship_MultiDeviceBytes(int nres, const int* widths, const int* heights,
+                                                 const int* max_sources, const int* max_pairs, int flags);
+
 /* Instrumentation: when enabled, every kernel launch is bracketed by CUDA events on its stream.
  * Vship_ProfileReport synchronises those events and writes a JSON object
  * {"kernel": [launches, total_ms], ...} (same size/truncation contract as

@@ -95,6 +95,26 @@ inline T decode(const uint8_t* plane, int64_t stride, int64_t x, int64_t y, int 
     }
 }
 
+// Round to the nearest IEEE half-precision value (ties to even), returned as T. Used to model
+// FP16 storage of intermediate planes.
+template <typename T> T round_half(T v) {
+    float f = (float)v;
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    const uint32_t sign = b & 0x80000000u;
+    const float a = std::fabs(f);
+    if (!(a < 65520.f)) return (T)(sign ? -INFINITY : INFINITY);
+    if (a < 6.103515625e-05f) {  // subnormal half: quantum 2^-24
+        const float q = std::nearbyint(a * 16777216.f) / 16777216.f;
+        return (T)(sign ? -q : q);
+    }
+    int e;
+    std::frexp(a, &e);  // a = m * 2^e, m in [0.5, 1)
+    const double quantum = std::ldexp(1.0, e - 11);
+    const double q = std::nearbyint((double)a / quantum) * quantum;
+    return (T)(sign ? -q : q);
+}
+
 // ssimu2/makeXYB.hpp:52-58 and butter/colors.hpp:7-13: sign-preserving x^2.4
 template <typename T> inline T to_linear(T a) {
     return a < 0 ? -std::pow(-a, (T)2.4) : std::pow(a, (T)2.4);
@@ -334,9 +354,12 @@ void ssimu2_channel_stats(const T* i1, const T* i2, int64_t w, int64_t h, const 
 }
 
 // ssimu2/main.hpp:34-151 (getTotalScaleSize, ssimu2GPUProcess, ssimu2process)
+// FP16 storage model for the XYB pyramid: each value is stored as half(v - offset[c]).
+const double kXybHalfOffset[3] = {0.42, 0.45, 0.55};
+
 template <typename T>
 double ssimu2(const uint8_t* const* src1, const uint8_t* const* src2, int64_t stride1, int64_t stride2,
-              int64_t w, int64_t h, int intype, int nthreads, T* measure_out) {
+              int64_t w, int64_t h, int intype, int nthreads, T* measure_out, int storage16 = 0) {
     const Kernel<T> g = ssimu2_kernel<T>();
     // planar linear RGB at every scale, both images
     std::vector<Dims> dims;
@@ -367,7 +390,21 @@ double ssimu2(const uint8_t* const* src1, const uint8_t* const* src2, int64_t st
             T* r = img[m][s * 3 + 0].data();
             T* gg = img[m][s * 3 + 1].data();
             T* b = img[m][s * 3 + 2].data();
-            for (int64_t i = 0; i < n; i++) positive_xyb(r[i], gg[i], b[i]);
+            for (int64_t i = 0; i < n; i++) {
+                positive_xyb(r[i], gg[i], b[i]);
+                if (storage16 == 1) {
+                    r[i] = round_half(r[i] - (T)kXybHalfOffset[0]) + (T)kXybHalfOffset[0];
+                    gg[i] = round_half(gg[i] - (T)kXybHalfOffset[1]) + (T)kXybHalfOffset[1];
+                    b[i] = round_half(b[i] - (T)kXybHalfOffset[2]) + (T)kXybHalfOffset[2];
+                }
+            }
+        }
+        if (storage16 == 2 && m == 1) {  // distorted pyramid stored as FP16 differences
+            for (int k = 0; k < 18; k++) {
+                std::vector<T>& d = img[1][k];
+                const std::vector<T>& r = img[0][k];
+                for (size_t i = 0; i < d.size(); i++) d[i] = r[i] + round_half(d[i] - r[i]);
+            }
         }
     }
     // res[scale][channel][6]
@@ -799,6 +836,13 @@ int oracle_ssimu2(const uint8_t* const* src1, const uint8_t* const* src2, int64_
                   int64_t width, int64_t height, int intype, int precision, int nthreads, double* score,
                   double* measure108) {
     if (width <= 0 || height <= 0 || !score) return 1;
+    if (precision == 16 || precision == 17) {
+        // FP64 arithmetic over an FP16-stored XYB pyramid: 16 = both pyramids as half(v - offset),
+        // 17 = reference in full precision, distorted as half(distorted - reference)
+        *score = ssimu2<double>(src1, src2, stride1, stride2, width, height, intype, nthreads, nullptr,
+                                precision == 16 ? 1 : 2);
+        return 0;
+    }
     if (precision == 64) {
         double m[108];
         *score = ssimu2<double>(src1, src2, stride1, stride2, width, height, intype, nthreads, m);

@@ -1,0 +1,199 @@
+"""Batched multi-resolution scoring with source reuse (Vship_MultiInit / MultiComputeDeviceAsync).
+
+* FP32 pyramids: every score equals, bit for bit, the one-resolution batch path on the same pair
+  (the work-list kernels run the same tile code; only the scheduling differs).
+* FP16-delta candidate pyramids: within the 1e-3 SSIMU2 tolerance of the FP64 oracle.
+* Butteraugli norms equal the one-resolution batch path's.
+* Graph replay: a second call with the same layout and new frames gives that layout's scores;
+  a changed layout is re-planned; results agree with direct launches.
+* Autotuner: the chosen knobs go to the JSON cache and a new handler reads them back.
+"""
+import json
+
+import numpy as np
+import pytest
+import torch
+
+from helpers import float_planes
+from vship_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+RES = [(96, 64), (131, 75), (256, 144)]
+
+
+def _dev_yuv(frame):
+    t = [torch.from_numpy(np.asarray(p, dtype=np.int32)).to(torch.int16).cuda() for p in frame]
+    return t, ([x.data_ptr() for x in t], t[0].stride(0) * 2, t[1].stride(0) * 2)
+
+
+def _batch(nsrc_per_res=(2, 1, 1), ncand=3, seed=11):
+    """Sources of each resolution, each with `ncand` DCT-quantised candidates (steps 4..)."""
+    keep, srcs, src_res, cands, cand_src, host = [], [], [], [], [], []
+    steps = [4, 8, 16, 26, 32]
+    for r, n in enumerate(nsrc_per_res):
+        w, h = RES[r]
+        for k in range(n):
+            src = synth.yuv420p10_source(h, w, k, seed + r)
+            t, fd = _dev_yuv(src)
+            keep.append(t)
+            si = len(srcs)
+            srcs.append(fd)
+            src_res.append(r)
+            for c in range(ncand):
+                st = steps[(k + c) % len(steps)]
+                cand = (synth.block_dct_quantise(src[0], st, 64, 940),
+                        synth.block_dct_quantise(src[1], 2 * st, 64, 960),
+                        synth.block_dct_quantise(src[2], 2 * st, 64, 960))
+                t, fd = _dev_yuv(cand)
+                keep.append(t)
+                cands.append(fd)
+                cand_src.append(si)
+                host.append((r, src, cand))
+    return keep, srcs, src_res, cands, cand_src, host
+
+
+def _run(vlib, scorer, b, metrics):
+    keep, srcs, src_res, cands, cand_src, _ = b
+    n = len(cands)
+    s2 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    bn = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    scorer.compute_async(srcs, src_res, cands, cand_src, vlib.IN_YUV420P10,
+                         s2.data_ptr() if metrics & vlib.MULTI_SSIMU2 else 0,
+                         bn.data_ptr() if metrics & vlib.MULTI_BUTTERAUGLI else 0,
+                         torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return s2.cpu().tolist(), bn.view(n, 3).cpu().tolist()
+
+
+def _caps(b):
+    _, _, src_res, _, cand_src, _ = b
+    ms = [src_res.count(r) for r in range(len(RES))]
+    mp = [sum(1 for s in cand_src if src_res[s] == r) for r in range(len(RES))]
+    return ms, mp
+
+
+def _plain_ssimu2(vlib, b):
+    keep, srcs, src_res, cands, cand_src, _ = b
+    out = []
+    for j, fd in enumerate(cands):
+        r = src_res[cand_src[j]]
+        w, h = RES[r]
+        table = vlib.device_frames_table([srcs[cand_src[j]], fd])
+        o = torch.zeros(1, dtype=torch.float64, device="cuda")
+        bt = vlib.SSIMU2Batch(w, h, 1)
+        bt.compute_async(table.data_ptr(), 1, vlib.IN_YUV420P10, o.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        bt.free()
+        out.append(o.item())
+    return out
+
+
+def test_multi_ssimu2_fp32_matches_plain(vlib):
+    b = _batch()
+    ms, mp = _caps(b)
+    want = _plain_ssimu2(vlib, b)
+    for flags in (vlib.MULTI_SSIMU2, vlib.MULTI_SSIMU2 | vlib.MULTI_NO_GRAPH):
+        sc = vlib.MultiScorer(RES, ms, mp, flags)
+        got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
+        got2, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)  # graph replay
+        sc.free()
+        assert got == want, (flags, got, want)
+        assert got2 == want
+
+
+def test_multi_ssimu2_fp16_delta_vs_fp64(vlib, orc):
+    b = _batch()
+    ms, mp = _caps(b)
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2 | vlib.MULTI_FP16)
+    got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
+    sc.free()
+    for s, (r, src, cand) in zip(got, b[5]):
+        ra = float_planes(synth.yuv420p10_to_rgb(src))
+        rb = float_planes(synth.yuv420p10_to_rgb(cand))
+        o64 = orc.ssimu2(ra, rb, precision=64)
+        o32 = orc.ssimu2(ra, rb, precision=32)
+        # FP32 sensitivity on these small frames bounds what any FP32 path can reach
+        tol = max(1e-3, 2 * abs(o32 - o64))
+        assert abs(s - o64) <= tol, (RES[r], s, o64, o32)
+
+
+def test_multi_butteraugli_matches_batch(vlib):
+    b = _batch((1, 1, 1), ncand=2)
+    ms, mp = _caps(b)
+    keep, srcs, src_res, cands, cand_src, _ = b
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2 | vlib.MULTI_BUTTERAUGLI | vlib.MULTI_FP16)
+    s2, bn = _run(vlib, sc, b, vlib.MULTI_SSIMU2 | vlib.MULTI_BUTTERAUGLI)
+    sc.free()
+    for j, fd in enumerate(cands):
+        w, h = RES[src_res[cand_src[j]]]
+        table = vlib.device_frames_table([srcs[cand_src[j]], fd])
+        o = torch.zeros(3, dtype=torch.float64, device="cuda")
+        bt = vlib.ButteraugliBatch(w, h, 1)
+        bt.compute_async(table.data_ptr(), 1, vlib.IN_YUV420P10, o.data_ptr(), 0,
+                         torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        bt.free()
+        assert bn[j] == o.cpu().tolist(), (j, bn[j], o)
+    assert all(0 < s < 100 for s in s2)
+
+
+def test_multi_layout_change_and_replay(vlib):
+    b = _batch()
+    ms, mp = _caps(b)
+    keep, srcs, src_res, cands, cand_src, host = b
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2)
+    full, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
+    # same layout, candidates of each source rotated: scores rotate with them
+    rot = list(cands)
+    groups = {}
+    for j, s in enumerate(cand_src):
+        groups.setdefault(s, []).append(j)
+    perm = list(range(len(cands)))
+    for js in groups.values():
+        for a, j in enumerate(js):
+            perm[j] = js[(a + 1) % len(js)]
+    rot = [cands[perm[j]] for j in range(len(cands))]
+    got, _ = _run(vlib, sc, (keep, srcs, src_res, rot, cand_src, host), vlib.MULTI_SSIMU2)
+    assert got == [full[perm[j]] for j in range(len(cands))]
+    # new layout: only the last two pairs
+    sub = (keep, srcs, src_res, cands[-2:], cand_src[-2:], host[-2:])
+    got, _ = _run(vlib, sc, sub, vlib.MULTI_SSIMU2)
+    assert got == full[-2:]
+    sc.free()
+
+
+def test_multi_autotune_cache(vlib, tmp_path):
+    b = _batch()
+    ms, mp = _caps(b)
+    cache = str(tmp_path / "tune.json")
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2 | vlib.MULTI_AUTOTUNE, tune_cache=cache)
+    want = _plain_ssimu2(vlib, b)
+    got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
+    k = sc.knobs()
+    sc.free()
+    assert got == want
+    assert k["source"] == "tuned"
+    entries = json.load(open(cache))
+    assert len(entries) == 1
+    (key, val), = entries.items()
+    assert key.startswith("ssimu2_multi_stats|") and val["grid_per_sm"] == k["grid_per_sm"]
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2 | vlib.MULTI_AUTOTUNE, tune_cache=cache)
+    got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
+    assert sc.knobs()["source"] == "cache" and got == want
+    sc.free()
+
+
+def test_multi_rejects_bad_layouts(vlib):
+    b = _batch((1, 1, 1), ncand=2)
+    ms, mp = _caps(b)
+    keep, srcs, src_res, cands, cand_src, host = b
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2)
+    out = torch.zeros(8, dtype=torch.float64, device="cuda")
+    with pytest.raises(vlib.VshipError):  # candidate of a source that does not exist
+        sc.compute_async(srcs, src_res, cands, [0, 1, 2, 3, 4, 3], vlib.IN_YUV420P10, out.data_ptr())
+    with pytest.raises(vlib.VshipError):  # more pairs of resolution 0 than declared
+        sc.compute_async(srcs, src_res, cands, [0, 0, 0, 1, 2, 2], vlib.IN_YUV420P10, out.data_ptr())
+    got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)  # still usable afterwards
+    assert all(0 < s <= 100 for s in got)
+    sc.free()

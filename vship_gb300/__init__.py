@@ -63,6 +63,8 @@ class DeviceFrame(ctypes.Structure):
 _PP = ctypes.POINTER(ctypes.c_void_p)
 _H = Handler
 _E = ctypes.c_int
+_IP = ctypes.POINTER(ctypes.c_int)
+
 SIGNATURES = {
     "Vship_GetVersion": (Version, []),
     "Vship_GetDeviceCount": (_E, [ctypes.POINTER(ctypes.c_int)]),
@@ -111,6 +113,14 @@ SIGNATURES = {
     "Vship_ButteraugliDeviceBytes": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "Vship_ComputeSSIMU2DeviceNoAlloc": (_E, [ctypes.POINTER(DeviceFrame), ctypes.POINTER(DeviceFrame), ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
+    "Vship_MultiInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, _IP, _IP, _IP, _IP, ctypes.c_int, ctypes.c_int,
+                             ctypes.c_float, ctypes.c_char_p]),
+    "Vship_MultiFree": (_E, [_H]),
+    "Vship_MultiComputeDeviceAsync": (_E, [_H, ctypes.c_int, ctypes.POINTER(DeviceFrame), _IP, ctypes.c_int,
+                                           ctypes.POINTER(DeviceFrame), _IP, ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p]),
+    "Vship_MultiKnobs": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
+    "Vship_MultiDeviceBytes": (ctypes.c_uint64, [ctypes.c_int, _IP, _IP, _IP, _IP, ctypes.c_int]),
     "Vship_ProfileSetEnabled": (None, [ctypes.c_int]),
     "Vship_ProfileReport": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }
@@ -379,11 +389,14 @@ class ButteraugliBatch:
             pass
 
 
-def device_frames_table(frames, device="cuda"):
-    """Pack [(planes, stride_bytes[, chroma_stride_bytes]), ...] of device pointers into a device
-    array of Vship_DeviceFrame held in a torch uint8 tensor."""
-    import torch
+MULTI_SSIMU2, MULTI_BUTTERAUGLI, MULTI_FP16, MULTI_NO_GRAPH, MULTI_AUTOTUNE = 1, 2, 4, 8, 16
 
+
+def _ints(v):
+    return (ctypes.c_int * len(v))(*[int(x) for x in v])
+
+
+def _frames(frames):
     arr = (DeviceFrame * len(frames))()
     for i, fr in enumerate(frames):
         planes, stride = fr[0], fr[1]
@@ -391,5 +404,66 @@ def device_frames_table(frames, device="cuda"):
             arr[i].plane[c] = int(planes[c])
         arr[i].stride = int(stride)
         arr[i].stride_c = int(fr[2]) if len(fr) > 2 else int(stride)
+    return arr
+
+
+class MultiScorer:
+    """Batched multi-resolution scoring with source reuse (Vship_MultiInit /
+    Vship_MultiComputeDeviceAsync). ``resolutions`` is a list of (width, height); the capacities
+    are per resolution."""
+
+    def __init__(self, resolutions, max_sources, max_pairs, flags=MULTI_SSIMU2, qnorm=2,
+                 intensity_multiplier=203.0, tune_cache=None):
+        self.resolutions = [(int(w), int(h)) for w, h in resolutions]
+        self.flags = int(flags)
+        n = len(self.resolutions)
+        self._h = Handler()
+        _check(lib().Vship_MultiInit(ctypes.byref(self._h), n, _ints([w for w, _ in self.resolutions]),
+                                     _ints([h for _, h in self.resolutions]), _ints(max_sources), _ints(max_pairs),
+                                     self.flags, int(qnorm), ctypes.c_float(intensity_multiplier),
+                                     tune_cache.encode() if tune_cache else None), "Vship_MultiInit")
+
+    @staticmethod
+    def device_bytes(resolutions, max_sources, max_pairs, flags=MULTI_SSIMU2) -> int:
+        return int(lib().Vship_MultiDeviceBytes(len(resolutions), _ints([w for w, _ in resolutions]),
+                                                _ints([h for _, h in resolutions]), _ints(max_sources),
+                                                _ints(max_pairs), int(flags)))
+
+    def compute_async(self, sources, source_res, candidates, candidate_source, input_type: int,
+                      ssimu2_dev_ptr: int = 0, butter_dev_ptr: int = 0, stream_ptr: int = 0) -> None:
+        """sources / candidates: [(planes, stride_bytes[, chroma_stride_bytes]), ...] of device
+        pointers; results land in device memory (npairs doubles / 3*npairs doubles)."""
+        _check(lib().Vship_MultiComputeDeviceAsync(self._h, len(sources), _frames(sources), _ints(source_res),
+                                                   len(candidates), _frames(candidates), _ints(candidate_source),
+                                                   int(input_type), ctypes.c_void_p(ssimu2_dev_ptr or None),
+                                                   ctypes.c_void_p(butter_dev_ptr or None),
+                                                   ctypes.c_void_p(stream_ptr)), "Vship_MultiComputeDeviceAsync")
+
+    def knobs(self) -> dict:
+        import json
+
+        n = lib().Vship_MultiKnobs(self._h, None, 0)
+        buf = ctypes.create_string_buffer(n)
+        lib().Vship_MultiKnobs(self._h, buf, n)
+        return json.loads(buf.value.decode())
+
+    def free(self):
+        if self._h is not None:
+            _check(lib().Vship_MultiFree(self._h), "Vship_MultiFree")
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def device_frames_table(frames, device="cuda"):
+    """Pack [(planes, stride_bytes[, chroma_stride_bytes]), ...] of device pointers into a device
+    array of Vship_DeviceFrame held in a torch uint8 tensor."""
+    import torch
+
+    arr = _frames(frames)
     host = torch.frombuffer(bytearray(bytes(arr)), dtype=torch.uint8)
     return host.to(device)

@@ -14,6 +14,7 @@
 #include "butter.h"
 #include "common.cuh"
 #include "ssimu2.h"
+#include "multi.h"
 #include "profile.h"
 
 #include <cuda_runtime.h>
@@ -216,6 +217,18 @@ struct ButterHandle {
 
 HandleTable<Ssimu2Handle> g_ssimu2;
 HandleTable<ButterHandle> g_butter;
+
+struct MultiHandle {
+    MultiEngine eng;
+    ~MultiHandle() {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaSetDevice(eng.device);
+        eng.destroy();
+        cudaSetDevice(dev);
+    }
+};
+HandleTable<MultiHandle> g_multi;
 
 // Device guard: make the handler's device current for the duration of a call.
 struct DeviceGuard {
@@ -595,6 +608,58 @@ Vship_Exception Vship_ComputeButteraugliUint16v3(Vship_ButteraugliHandler handle
                                                  const uint8_t* srcp2[3], int64_t stride, int64_t stride2) {
     if (!norms) return Vship_BadPointer;
     return to_exc(butter_compute(handler.id, norms, dstp, dststride, srcp1, srcp2, stride, stride2, IN_UINT16));
+}
+
+// ----- batched multi-resolution ------------------------------------------------------------
+
+Vship_Exception Vship_MultiInit(Vship_MultiHandler* handler, int nres, const int* widths, const int* heights,
+                                const int* max_sources, const int* max_pairs, int flags, int Qnorm,
+                                float intensity_multiplier, const char* tune_cache_path) {
+    if (!handler) return Vship_BadPointer;
+    int c = 0;
+    int rc = check_gpu_count(&c);
+    if (rc) return to_exc(rc);
+    std::unique_ptr<MultiHandle> h(new MultiHandle());
+    rc = h->eng.init(nres, widths, heights, max_sources, max_pairs, flags, Qnorm, intensity_multiplier,
+                     tune_cache_path);
+    if (rc) return to_exc(rc);
+    handler->id = g_multi.put(std::move(h));
+    return Vship_NoError;
+}
+
+Vship_Exception Vship_MultiFree(Vship_MultiHandler handler) {
+    std::unique_ptr<MultiHandle> h = g_multi.take(handler.id);
+    if (!h) return Vship_BadHandler;
+    return Vship_NoError;
+}
+
+Vship_Exception Vship_MultiComputeDeviceAsync(Vship_MultiHandler handler, int nsources, const Vship_DeviceFrame* sources,
+                                              const int* source_res, int npairs, const Vship_DeviceFrame* candidates,
+                                              const int* candidate_source, Vship_InputType input_type,
+                                              double* ssimu2_dev, double* butter_norms_dev, void* stream) {
+    MultiHandle* h = g_multi.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    DeviceGuard dg(h->eng.device);
+    return to_exc(h->eng.compute(nsources, reinterpret_cast<const FrameDesc*>(sources), source_res, npairs,
+                                 reinterpret_cast<const FrameDesc*>(candidates), candidate_source, (int)input_type,
+                                 ssimu2_dev, butter_norms_dev, (cudaStream_t)stream));
+}
+
+int Vship_MultiKnobs(Vship_MultiHandler handler, char* out_json, int len) {
+    MultiHandle* h = g_multi.get(handler.id);
+    const std::string s = h ? h->eng.knobs_json() : std::string("{}");
+    const int need = (int)s.size() + 1;
+    if (len <= 0 || !out_json) return need;
+    const int ncopy = std::min(len - 1, need - 1);
+    std::memcpy(out_json, s.data(), ncopy);
+    out_json[ncopy] = '\0';
+    return need;
+}
+
+uint64_t Vship_MultiDeviceBytes(int nres, const int* widths, const int* heights, const int* max_sources,
+                                const int* max_pairs, int flags) {
+    if (nres <= 0 || nres > kMaxRes || !widths || !heights || !max_sources || !max_pairs) return 0;
+    return (uint64_t)MultiEngine::device_bytes(nres, widths, heights, max_sources, max_pairs, flags);
 }
 
 }  // extern "C"

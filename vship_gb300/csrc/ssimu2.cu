@@ -93,17 +93,37 @@ __device__ __forceinline__ void positive_xyb(float& r, float& g, float& b) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Kernel 1: decode + linearise + pyramid + XYB. grid (tiles_x0, tiles_y0, 2*npairs), 256 thr.
-template <int IT>
-__global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
-                                                             float* __restrict__ pyr, Ssimu2Geom g) {
+// Kernel 1: decode + linearise + pyramid + XYB, one 32x32 level-0 tile per CTA (256 threads).
+// A pyramid is written either as FP32 planes, or (DELTA) as FP16 differences against an FP32
+// reference pyramid of the same geometry: the batched form keeps each source's pyramid in FP32
+// and its candidates' as FP16 deltas (identical samples stay exactly identical, small
+// distortions keep FP16's relative precision).
+struct PyrOut {
+    float* f32;         // FP32 planes [3][plane_elems]
+    __half* d16;        // FP16 delta planes [3][plane_elems]
+    const float* ref;   // reference FP32 planes for the deltas
+};
+
+template <bool DELTA>
+__device__ __forceinline__ void pyr_store(const PyrOut& out, int64_t pe, int64_t o, float X, float Y, float B) {
+    if (DELTA) {
+        out.d16[o] = __float2half_rn(X - __ldg(out.ref + o));
+        out.d16[pe + o] = __float2half_rn(Y - __ldg(out.ref + pe + o));
+        out.d16[2 * pe + o] = __float2half_rn(B - __ldg(out.ref + 2 * pe + o));
+    } else {
+        out.f32[o] = X;
+        out.f32[pe + o] = Y;
+        out.f32[2 * pe + o] = B;
+    }
+}
+
+template <int IT, bool DELTA>
+__device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const PyrOut& out, const Ssimu2Geom& g, int bx,
+                                             int by) {
     __shared__ float smA[3 * 32 * 33];
     __shared__ float smB[3 * 16 * 17];
-    const int img = blockIdx.z;  // pair*2 + image
-    const FrameDesc fd = frames[img];
-    float* base = pyr + (int64_t)img * 3 * g.plane_elems;
+    const int64_t pe = g.plane_elems;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    const int bx = blockIdx.x, by = blockIdx.y;
     {
         const Ssimu2Level L = g.lv[0];
 #pragma unroll
@@ -118,10 +138,7 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
                 v2 = to_linear_fast(v2);
                 float X = v0, Y = v1, B = v2;
                 positive_xyb(X, Y, B);
-                int64_t o = L.off + (int64_t)gy * L.pitch + gx;
-                base[o] = X;
-                base[g.plane_elems + o] = Y;
-                base[2 * g.plane_elems + o] = B;
+                pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);
             }
             smA[(0 * 32 + ly) * 33 + tx] = v0;
             smA[(1 * 32 + ly) * 33 + tx] = v1;
@@ -131,15 +148,15 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
     __syncthreads();
     float* cur = smA;
     float* nxt = smB;
-    int cside = 32;
-#pragma unroll 1
+    // levels 1..5: the tile side halves each level (16, 8, 4, 2, 1), so indices are shifts
+#pragma unroll
     for (int k = 1; k < 6; k++) {
-        const int nside = cside >> 1;
+        const int cside = 32 >> (k - 1), nside = 32 >> k, lg = 5 - k;
         const Ssimu2Level L = g.lv[k], P = g.lv[k - 1];
         const int ox = bx * nside, oy = by * nside;
         const int pox = bx * cside, poy = by * cside;
         for (int i = threadIdx.x; i < nside * nside; i += 256) {
-            const int lx = i % nside, ly = i / nside;
+            const int lx = i & (nside - 1), ly = i >> lg;
             const int gx = ox + lx, gy = oy + ly;
             float v[3] = {0.f, 0.f, 0.f};
             if (gx < L.w && gy < L.h) {
@@ -157,10 +174,7 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
                 }
                 float X = v[0], Y = v[1], B = v[2];
                 positive_xyb(X, Y, B);
-                int64_t o = L.off + (int64_t)gy * L.pitch + gx;
-                base[o] = X;
-                base[g.plane_elems + o] = Y;
-                base[2 * g.plane_elems + o] = B;
+                pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);
             }
 #pragma unroll
             for (int c = 0; c < 3; c++) nxt[c * nside * (nside + 1) + ly * (nside + 1) + lx] = v[c];
@@ -169,8 +183,17 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
         float* t = cur;
         cur = nxt;
         nxt = t;
-        cside = nside;
     }
+}
+
+// grid (tiles_x0, tiles_y0, 2*npairs)
+template <int IT>
+__global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
+                                                             float* __restrict__ pyr, Ssimu2Geom g) {
+    const int img = blockIdx.z;  // pair*2 + image
+    const FrameDesc fd = frames[img];
+    PyrOut out{pyr + (int64_t)img * 3 * g.plane_elems, nullptr, nullptr};
+    pyramid_tile<IT, false>(fd, out, g, blockIdx.x, blockIdx.y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -223,23 +246,38 @@ __device__ __forceinline__ void stage_tile(float* dst, const float* __restrict__
     }
 }
 
-__global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __restrict__ pyr,
-                                                              float* __restrict__ partials, Ssimu2Geom g) {
+// FP16 delta tile: 64 rows x 48 halves, row pitch 56 halves (7 quads: conflict-free 16-byte reads)
+constexpr int ST_DP = 56;
+
+__device__ __forceinline__ void stage_tile_h(__half* dst, const __half* __restrict__ plane, int pitch, int w, int h,
+                                             int x0, int y0) {
+    for (int ch = threadIdx.x; ch < ST_IH * 6; ch += 256) {
+        const int r = ch / 6, q = ch - r * 6;
+        const int gx = x0 - ST_R + 8 * q, gy = y0 - ST_R + r;
+        int bytes = 0;
+        const __half* src = plane;
+        if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
+            bytes = min(w - gx, 8) * 2;
+            src = plane + (int64_t)gy * pitch + gx;
+        }
+        cp_async16(reinterpret_cast<float*>(dst + r * ST_DP + 8 * q), reinterpret_cast<const float*>(src), bytes);
+    }
+}
+
+// One 32x48 output tile of one scale: the five moments, the maps and 18 pooled sums written to
+// out[pool * stride] (pool = map * 2 + norm, times 3 channels). im1 / im2 point at the tile's scale
+// in the channel-0 plane; DELTA: im2 holds FP16 differences against im1.
+template <bool DELTA>
+__device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const void* __restrict__ im2v, int64_t pe,
+                                           const Ssimu2Level& L, int lt, float* __restrict__ out, int stride) {
     extern __shared__ __align__(16) float sm[];
     float* raw = sm;                   // [stage][image][64][52]
     float* hb = sm + 4 * ST_RAW;       // [5][64][33]
     float* red = hb + 5 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
-    const int pair = blockIdx.y;
-    const int t = blockIdx.x;
-    int s = 0;
-#pragma unroll
-    for (int k = 1; k < 6; k++) s += (t >= g.tile_begin[k]);
-    const Ssimu2Level L = g.lv[s];
-    const int lt = t - g.tile_begin[s];
+    const float* im2 = static_cast<const float*>(im2v);
+    const __half* im2h = static_cast<const __half*>(im2v);
     const int tx0 = (lt % L.tiles_x) * ST_TW;
     const int ty0 = (lt / L.tiles_x) * ST_TH;
-    const float* im1 = pyr + (int64_t)(pair * 2 + 0) * 3 * g.plane_elems + L.off;
-    const float* im2 = pyr + (int64_t)(pair * 2 + 1) * 3 * g.plane_elems + L.off;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool interior = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h;
 
@@ -256,7 +294,8 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
     for (int o = 0; o < 6; o++) rxy[o] = rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
 
     stage_tile(raw, im1, L.pitch, L.w, L.h, tx0, ty0);
-    stage_tile(raw + ST_RAW, im2, L.pitch, L.w, L.h, tx0, ty0);
+    if (DELTA) stage_tile_h(reinterpret_cast<__half*>(raw + ST_RAW), im2h, L.pitch, L.w, L.h, tx0, ty0);
+    else stage_tile(raw + ST_RAW, im2, L.pitch, L.w, L.h, tx0, ty0);
     cp_async_commit();
 
 #pragma unroll 1
@@ -265,8 +304,12 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
         float* r2 = r1 + ST_RAW;
         if (c < 2) {
             float* n1 = raw + ((c + 1) & 1) * 2 * ST_RAW;
-            stage_tile(n1, im1 + (int64_t)(c + 1) * g.plane_elems, L.pitch, L.w, L.h, tx0, ty0);
-            stage_tile(n1 + ST_RAW, im2 + (int64_t)(c + 1) * g.plane_elems, L.pitch, L.w, L.h, tx0, ty0);
+            stage_tile(n1, im1 + (int64_t)(c + 1) * pe, L.pitch, L.w, L.h, tx0, ty0);
+            if (DELTA)
+                stage_tile_h(reinterpret_cast<__half*>(n1 + ST_RAW), im2h + (int64_t)(c + 1) * pe, L.pitch, L.w, L.h,
+                             tx0, ty0);
+            else
+                stage_tile(n1 + ST_RAW, im2 + (int64_t)(c + 1) * pe, L.pitch, L.w, L.h, tx0, ty0);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -285,7 +328,7 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
                 const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
                 if (gx < 0 || gx >= L.w || gy < 0 || gy >= L.h) {
                     r1[r * ST_RP + col] = shift;
-                    r2[r * ST_RP + col] = shift;
+                    if (!DELTA) r2[r * ST_RP + col] = shift;  // FP16 deltas arrive as zeros there
                 }
             }
             __syncthreads();
@@ -305,16 +348,33 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
             }
             const float* ra = r1 + hr * ST_RP + 8 * hg;
             const float* rb = r2 + hr * ST_RP + 8 * hg;
+            float dl[24];  // DELTA: the 24 deltas of this thread's window
+            if (DELTA) {
+                const __half* rd = reinterpret_cast<const __half*>(r2) + hr * ST_DP + 8 * hg;
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const uint4 q = *reinterpret_cast<const uint4*>(rd + 8 * k);
+                    const __half2* hq = reinterpret_cast<const __half2*>(&q);
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const float2 f = __half22float2(hq[u]);
+                        dl[8 * k + 2 * u] = f.x;
+                        dl[8 * k + 2 * u + 1] = f.y;
+                    }
+                }
+            }
 #pragma unroll
             for (int j4 = 0; j4 < 6; j4++) {
                 const float4 va = *reinterpret_cast<const float4*>(ra + 4 * j4);
-                const float4 vb = *reinterpret_cast<const float4*>(rb + 4 * j4);
+                float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (!DELTA) vb = *reinterpret_cast<const float4*>(rb + 4 * j4);
                 const float la[4] = {va.x, va.y, va.z, va.w};
                 const float lb[4] = {vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
                     const int j = 4 * j4 + u;
-                    const float a = la[u] - shift, b = lb[u] - shift;
+                    const float a = la[u] - shift;
+                    const float b = DELTA ? a + dl[j] : lb[u] - shift;
                     const f2_t p1 = f2_pack(a, b);
                     const f2_t p2 = f2_mul(p1, p1);
                     const float ab = a * b;
@@ -378,7 +438,10 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
             const int y = ty0 + 6 * vg + o, x = tx0 + vc;
             if (x < L.w && y < L.h) {
                 const int so = (6 * vg + o + ST_R) * ST_RP + vc + ST_R;
-                const float i1 = r1[so] - shift, i2 = r2[so] - shift;  // shifted samples
+                const float i1 = r1[so] - shift;  // shifted samples
+                const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(6 * vg + o + ST_R) * ST_DP +
+                                                                                                 vc + ST_R])
+                                       : r2[so] - shift;
                 const float m1 = m[0][o], m2 = m[1][o];                 // shifted means
                 // SSIM map (score.hpp:141-148) as max((den - num) / den, 0), the same quantity
                 // as max(1 - num / den, 0) without the cancellation; explicit fma so identical
@@ -412,29 +475,45 @@ __global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __res
         }
         __syncthreads();
     }
-    // pools: partials[pair][pool * 3 + channel][tile], pool = map * 2 + norm
+    // pools: out[(pool * 3 + channel) * stride], pool = map * 2 + norm
     if (tid < 18) {
         const int pool = tid / 3, c = tid - pool * 3;
         float v = 0.f;
 #pragma unroll
         for (int w = 0; w < 8; w++) v += red[(c * 8 + w) * 6 + pool];
-        partials[((int64_t)pair * 18 + tid) * g.tiles_total + t] = v;
+        out[(int64_t)tid * stride] = v;
     }
+}
+
+// grid (tiles_total, npairs), dynamic smem kStatsSmem
+__global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __restrict__ pyr,
+                                                              float* __restrict__ partials, Ssimu2Geom g) {
+    const int pair = blockIdx.y;
+    const int t = blockIdx.x;
+    int s = 0;
+#pragma unroll
+    for (int k = 1; k < 6; k++) s += (t >= g.tile_begin[k]);
+    const Ssimu2Level L = g.lv[s];
+    const float* im1 = pyr + (int64_t)(pair * 2 + 0) * 3 * g.plane_elems + L.off;
+    const float* im2 = pyr + (int64_t)(pair * 2 + 1) * 3 * g.plane_elems + L.off;
+    stats_tile<false>(im1, im2, g.plane_elems, L, t - g.tile_begin[s],
+                      partials + (int64_t)pair * 18 * g.tiles_total + t, g.tiles_total);
 }
 
 // ------------------------------------------------------------------------------------------
 // Kernel 3: FP64 finalisation, one CTA per pair. The 108 (scale, pool, channel) sums are
 // reduced warp-parallel over their tiles (coalesced), then the 108 weighted features are summed
 // in parallel; only the score mapping runs on one thread (FP64 is a slow pipe on this GPU).
-__global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __restrict__ partials,
-                                                              double* __restrict__ scores, Ssimu2Geom g) {
+// partials: this pair's [18][tiles_total] block.
+__device__ __forceinline__ void finalize_pair(const float* __restrict__ partials, const Ssimu2Geom& g,
+                                              double* __restrict__ score) {
     __shared__ double pooled[6][18];
     __shared__ double red[8];
-    const int pair = blockIdx.x;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tiles_total = g.tiles_total;
     for (int seg = warp; seg < 108; seg += 8) {
         const int s = seg / 18, i = seg - 18 * (seg / 18);
-        const float* p = partials + ((int64_t)pair * 18 + i) * g.tiles_total + g.tile_begin[s];
+        const float* p = partials + (int64_t)i * tiles_total + g.tile_begin[s];
         const int n = g.tile_begin[s + 1] - g.tile_begin[s];
         double a = 0.0;
         for (int t = lane; t < n; t += 32) a += (double)__ldg(p + t);
@@ -460,8 +539,53 @@ __global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __res
         ssim *= 0.9562382616834844;  // score.hpp:388-397
         ssim = (6.248496625763138e-5 * ssim * ssim) * ssim + 2.326765642916932 * ssim -
                0.020884521182843837 * ssim * ssim;
-        scores[pair] = ssim > 0.0 ? pow(ssim, 0.6276336467831387) * -10.0 + 100.0 : 100.0;
+        *score = ssim > 0.0 ? pow(ssim, 0.6276336467831387) * -10.0 + 100.0 : 100.0;
     }
+}
+
+__global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __restrict__ partials,
+                                                              double* __restrict__ scores, Ssimu2Geom g) {
+    finalize_pair(partials + (int64_t)blockIdx.x * 18 * g.tiles_total, g, scores + blockIdx.x);
+}
+
+// ------------------------------------------------------------------------------------------
+// Work-list kernels of the batched multi-resolution form (Ssimu2MultiEngine).
+// one 32x32 level-0 tile per CTA: items {image, tile x, tile y, unused}
+template <int IT, bool DELTA>
+__global__ void __launch_bounds__(256) ssimu2_multi_pyramid_kernel(const Ssimu2MultiImage* __restrict__ imgs,
+                                                                   const int4* __restrict__ items,
+                                                                   const Ssimu2Geom* __restrict__ geoms) {
+    const int4 it = items[blockIdx.x];
+    const Ssimu2MultiImage im = imgs[it.x];
+    const PyrOut out{im.f32, static_cast<__half*>(im.d16), im.ref};
+    pyramid_tile<IT, DELTA>(im.fd, out, geoms[im.geom], it.y, it.z);
+}
+
+// persistent: CTA b takes items b, b + gridDim.x, ...; items {pair, tile}
+template <bool DELTA>
+__global__ void __launch_bounds__(256, 2) ssimu2_multi_stats_kernel(const Ssimu2MultiPair* __restrict__ pairs,
+                                                                    const int2* __restrict__ items, int nitems,
+                                                                    const Ssimu2Geom* __restrict__ geoms) {
+    for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
+        const int2 it = items[i];
+        const Ssimu2MultiPair P = pairs[it.x];
+        const Ssimu2Geom& g = geoms[P.geom];
+        int s = 0;
+#pragma unroll
+        for (int k = 1; k < 6; k++) s += (it.y >= g.tile_begin[k]);
+        const Ssimu2Level L = g.lv[s];
+        const void* im2 = DELTA ? static_cast<const void*>(static_cast<const __half*>(P.cand) + L.off)
+                                : static_cast<const void*>(static_cast<const float*>(P.cand) + L.off);
+        stats_tile<DELTA>(P.src + L.off, im2, g.plane_elems, L, it.y - g.tile_begin[s], P.partials + it.y,
+                          g.tiles_total);
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) ssimu2_multi_finalize_kernel(const Ssimu2MultiPair* __restrict__ pairs,
+                                                                    const Ssimu2Geom* __restrict__ geoms) {
+    const Ssimu2MultiPair P = pairs[blockIdx.x];
+    finalize_pair(P.partials, geoms[P.geom], P.score);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -581,6 +705,73 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
     }
     ssimu2_stats_kernel<<<dim3((unsigned)geom.tiles_total, 1u), 256, kStatsSmem, st>>>(pyr, partials, geom);
     ssimu2_finalize_kernel<<<1, 256, 0, st>>>(partials, out_score, geom);
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    return E_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// Work-list launches (Ssimu2MultiEngine, multi.cu).
+
+int ssimu2_multi_prepare() {
+    int rc = ssimu2_prepare_device();
+    if (rc) return rc;
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kStatsSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        kStatsSmem));
+    return E_OK;
+}
+
+int ssimu2_multi_stats_blocks_per_sm(bool delta, int* blocks) {
+    VSHIP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        blocks, delta ? ssimu2_multi_stats_kernel<true> : ssimu2_multi_stats_kernel<false>, 256, kStatsSmem));
+    return E_OK;
+}
+
+template <bool DELTA>
+static void launch_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items, int nitems,
+                                 const Ssimu2Geom* geoms, int intype, cudaStream_t st) {
+    const unsigned n = (unsigned)nitems;
+    switch (intype) {
+        case IN_UINT8: ssimu2_multi_pyramid_kernel<IN_UINT8, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
+        case IN_UINT16: ssimu2_multi_pyramid_kernel<IN_UINT16, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
+        case IN_HALF: ssimu2_multi_pyramid_kernel<IN_HALF, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
+        case IN_YUV420P10:
+            ssimu2_multi_pyramid_kernel<IN_YUV420P10, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms);
+            break;
+        default: ssimu2_multi_pyramid_kernel<IN_FLOAT, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
+    }
+}
+
+int ssimu2_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items, int nitems, const Ssimu2Geom* geoms,
+                         int intype, bool delta, cudaStream_t st) {
+    if (nitems <= 0) return E_OK;
+    ProfScope ps(delta ? "ssimu2_multi_pyramid_cand" : "ssimu2_multi_pyramid_src", st);
+    if (delta)
+        launch_multi_pyramid<true>(imgs, items, nitems, geoms, intype, st);
+    else
+        launch_multi_pyramid<false>(imgs, items, nitems, geoms, intype, st);
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    return E_OK;
+}
+
+int ssimu2_multi_stats(const Ssimu2MultiPair* pairs, const int2* items, int nitems, const Ssimu2Geom* geoms,
+                       bool delta, int grid, cudaStream_t st) {
+    if (nitems <= 0) return E_OK;
+    const unsigned gr = (unsigned)std::max(1, std::min(grid, nitems));
+    ProfScope ps("ssimu2_multi_stats", st);
+    if (delta)
+        ssimu2_multi_stats_kernel<true><<<gr, 256, kStatsSmem, st>>>(pairs, items, nitems, geoms);
+    else
+        ssimu2_multi_stats_kernel<false><<<gr, 256, kStatsSmem, st>>>(pairs, items, nitems, geoms);
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    return E_OK;
+}
+
+int ssimu2_multi_finalize(const Ssimu2MultiPair* pairs, int npairs, const Ssimu2Geom* geoms, cudaStream_t st) {
+    if (npairs <= 0) return E_OK;
+    ProfScope ps("ssimu2_multi_finalize", st);
+    ssimu2_multi_finalize_kernel<<<(unsigned)npairs, 256, 0, st>>>(pairs, geoms);
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
 }

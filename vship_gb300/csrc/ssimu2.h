@@ -5,9 +5,9 @@
 #include <cstddef>
 #include <cstdint>
 
-namespace vship {
+#include "common.cuh"
 
-struct FrameDesc;
+namespace vship {
 
 // One pyramid level in device memory: planar FP32, rows padded to `pitch` floats.
 struct Ssimu2Level {
@@ -52,5 +52,36 @@ int ssimu2_prepare_device();
 size_t ssimu2_scratch_floats(const Ssimu2Geom& g);
 int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intype, const Ssimu2Geom& geom,
                           FrameDesc* frames_scratch, float* scratch, double* out_score, cudaStream_t st);
+
+// ------------------------------------------------------------------------------------------
+// Work-list form over many images of several resolutions (multi.cu builds the tables).
+// One entry per image whose pyramid is built: sources write FP32 planes to f32; candidates
+// write FP32 planes to f32, or (d16 != null) FP16 deltas against their source's planes `ref`.
+struct Ssimu2MultiImage {
+    int geom;
+    FrameDesc fd;
+    float* f32;
+    void* d16;
+    const float* ref;
+};
+// One scored pair: its geometry, the source pyramid, the candidate pyramid (FP32 or FP16
+// deltas), the pair's [18][tiles_total] partial sums and where the score goes.
+struct Ssimu2MultiPair {
+    int geom;
+    const float* src;
+    const void* cand;
+    float* partials;
+    double* score;
+};
+
+int ssimu2_multi_prepare();
+int ssimu2_multi_stats_blocks_per_sm(bool delta, int* blocks);
+// items: {image, level-0 tile x, tile y, 0}, one CTA each. delta selects the FP16-delta store.
+int ssimu2_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items, int nitems, const Ssimu2Geom* geoms,
+                         int intype, bool delta, cudaStream_t st);
+// Persistent: `grid` CTAs walk items {pair, tile} with stride grid.
+int ssimu2_multi_stats(const Ssimu2MultiPair* pairs, const int2* items, int nitems, const Ssimu2Geom* geoms,
+                       bool delta, int grid, cudaStream_t st);
+int ssimu2_multi_finalize(const Ssimu2MultiPair* pairs, int npairs, const Ssimu2Geom* geoms, cudaStream_t st);
 
 }  // namespace vship
