@@ -138,6 +138,31 @@ def test_multi_butteraugli_matches_batch(vlib):
     assert all(0 < s < 100 for s in s2)
 
 
+def test_multi_butteraugli_split_groups(vlib, monkeypatch):
+    """A workspace budget that holds two 256x144 images: that source's five candidates run in
+    five chunks (the source's own stage reruns in each); norms still equal the batch path's."""
+    b = _batch((1, 1, 1), ncand=5)
+    ms, mp = _caps(b)
+    keep, srcs, src_res, cands, cand_src, _ = b
+    w, h = RES[2]
+    monkeypatch.setenv("VSHIP_BUTTER_CHUNK_BYTES", str(3 * 16 * 4 * ((w + 7) // 8 * 8 * h + 4096)))
+    sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_BUTTERAUGLI)
+    _, bn = _run(vlib, sc, b, vlib.MULTI_BUTTERAUGLI)
+    _, bn2 = _run(vlib, sc, b, vlib.MULTI_BUTTERAUGLI)
+    sc.free()
+    assert bn == bn2
+    for j, fd in enumerate(cands):
+        w, h = RES[src_res[cand_src[j]]]
+        table = vlib.device_frames_table([srcs[cand_src[j]], fd])
+        o = torch.zeros(3, dtype=torch.float64, device="cuda")
+        bt = vlib.ButteraugliBatch(w, h, 1)
+        bt.compute_async(table.data_ptr(), 1, vlib.IN_YUV420P10, o.data_ptr(), 0,
+                         torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        bt.free()
+        assert bn[j] == o.cpu().tolist(), (j, bn[j], o)
+
+
 def test_multi_layout_change_and_replay(vlib):
     b = _batch()
     ms, mp = _caps(b)

@@ -65,37 +65,41 @@ __device__ __forceinline__ float b_inv_mass(int pos, int extent) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Workspace layout. Per pair and per scale, NPLANES dense planes of pitch p:
+// Workspace layout. Every image (a reference / source or a distorted / candidate frame) owns, per
+// scale, NIMG dense planes of pitch p; a scored pair reads its two images' planes and writes its
+// own planes into planes of the distorted image that are dead by then, so that an image shared by
+// several pairs (a source scored against several candidates) is read-only after its own stage.
 enum : int {
-    P_LIN = 0,    // 0..5   linear RGB (image*3 + c); dead after opsin
-    P_TMP = 0,    // 0..5   horizontal-pass output (reuses LIN)
-    P_SAC = 0,    // 0      sum of AC terms          } written by diff, after the last use of TMP
-    P_SDC = 1,    // 1      sum of DC terms          }
-    P_PRE0 = 2,   // 2      mask precompute, image 0 }
-    P_PRE1 = 3,   // 3      mask precompute, image 1 }
-    P_B0 = 4,     // 4      blurred mask, image 0
-    P_XYB = 6,    // 6..11  XYB, then D = XYB - LF, then HF_pre (X, Y) in place
-    P_LFV = 12,   // 12..17 LF vals
-    P_MF = 18,    // 18..23 MF
-    P_HF = 24,    // 24..27 HF (image*2 + c)
-    P_UHF = 28,   // 28..31 UHF
-    P_DIFF = 32,  // 32     diffmap of this scale
-    NPLANES = 33
+    I_LIN = 0,    // 0..2   linear RGB; dead after opsin
+    I_TMP = 0,    // 0..2   horizontal-pass output (reuses LIN); dead after mf_v
+    I_XYB = 3,    // 3..5   XYB, then D = XYB - LF, then HF_pre (X, Y) in place; dead after hf
+    I_LFV = 6,    // 6..8   LF vals
+    I_MF = 9,     // 9..11  MF
+    I_HF = 12,    // 12..13 HF (X, Y)
+    I_UHF = 14,   // 14..15 UHF (X, Y)
+    NIMG = 16,
+    // pair planes, inside the distorted image's dead TMP and XYB planes
+    Q_SAC = 0,    // sum of AC terms            } written by diff
+    Q_SDC = 1,    // sum of DC terms            }
+    Q_PRE0 = 2,   // mask precompute, image 0   }
+    Q_PRE1 = 3,   // mask precompute, image 1   }
+    Q_B0 = 4,     // blurred mask of image 0 (mask_blur)
+    Q_DIFF = 5    // diffmap of this scale (diffmap)
 };
 
 struct BScaleDev {
     int w, h, p;
     int64_t n;     // p*h
-    int64_t base;  // offset inside the pair's workspace
+    int64_t base;  // offset inside the image's workspace
 };
 struct BGeom {
     BScaleDev s[2];  // 0 = full, 1 = half
-    int64_t pair_floats;
+    int64_t img_floats;
     int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x8) at full scale
 };
 
-__device__ __forceinline__ float* bplane(float* work, const BGeom& g, const BScaleDev& S, int pair, int id) {
-    return work + (int64_t)pair * g.pair_floats + S.base + (int64_t)id * S.n;
+__device__ __forceinline__ float* iplane(float* work, const BGeom& g, const BScaleDev& S, int img, int id) {
+    return work + (int64_t)img * g.img_floats + S.base + (int64_t)id * S.n;
 }
 // Select a scale with constant indices only, so the parameter struct is never copied to the
 // stack for a dynamic index.
@@ -103,13 +107,13 @@ __device__ __forceinline__ BScaleDev pick_scale(const BGeom& g, int s) { return 
 
 // ------------------------------------------------------------------------------------------
 // Kernel: decode + linearise at full resolution + 2x2 box to half resolution.
-// grid (ceil(w/32), ceil(h/32), 2*npairs), 256 threads.
+// grid (ceil(w/32), ceil(h/32), nimages), 256 threads; frames[image].
 template <int IT>
 __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __restrict__ frames,
                                                             float* __restrict__ work, BGeom g) {
     __shared__ float sm[3][32][33];
-    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
-    const FrameDesc fd = frames[blockIdx.z];
+    const int img = blockIdx.z;
+    const FrameDesc fd = frames[img];
     const BScaleDev F = g.s[0], Hs = g.s[1];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 #pragma unroll
@@ -122,7 +126,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 v[c] = to_linear_fast(v[c]);
-                bplane(work, g, F, pair, P_LIN + img * 3 + c)[(int64_t)gy * F.p + gx] = v[c];
+                iplane(work, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
             }
         }
 #pragma unroll
@@ -141,7 +145,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
             s += sm[c][y1][x0];
             s += sm[c][y0][x1];
             s += sm[c][y1][x1];
-            bplane(work, g, Hs, pair, P_LIN + img * 3 + c)[(int64_t)gy * Hs.p + gx] = s * 0.25f;
+            iplane(work, g, Hs, img, I_LIN + c)[(int64_t)gy * Hs.p + gx] = s * 0.25f;
         }
     }
 }
@@ -235,26 +239,26 @@ __device__ __forceinline__ float b_gamma(float v) {
     return fmaf(19.245013259874995f, lg2_approx(add_dc(v, kOff)) * 0.69314718055994531f, -23.16046239805755f);
 }
 
-// grid (ceil(w/32), ceil(h/48), 2*npairs); the three channels' tiles are double-buffered.
+// grid (ceil(w/32), ceil(h/48), nimages); the three channels' tiles are double-buffered.
 __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict__ work, BGeom g, int s,
                                                               float intensity) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
-    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const int img = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
     float rxy[6];
     tile_masses_r8<0>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float src[3][6], blr[3][6];
-    tile_stage_r8(sm, bplane(work, g, S, pair, P_LIN + img * 3), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(work, g, S, img, I_LIN), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         float* in = sm + (c & 1) * TB_RAW;
         if (c < 2) {
-            tile_stage_r8(sm + ((c + 1) & 1) * TB_RAW, bplane(work, g, S, pair, P_LIN + img * 3 + c + 1), S.p, S.w,
-                          S.h, x0, y0);
+            tile_stage_r8(sm + ((c + 1) & 1) * TB_RAW, iplane(work, g, S, img, I_LIN + c + 1), S.p, S.w, S.h, x0,
+                          y0);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -266,9 +270,9 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
         for (int o = 0; o < 6; o++) src[c][o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
     }
-    float* ox = bplane(work, g, S, pair, P_XYB + img * 3 + 0);
-    float* oy = bplane(work, g, S, pair, P_XYB + img * 3 + 1);
-    float* oz = bplane(work, g, S, pair, P_XYB + img * 3 + 2);
+    float* ox = iplane(work, g, S, img, I_XYB + 0);
+    float* oy = iplane(work, g, S, img, I_XYB + 1);
+    float* oz = iplane(work, g, S, img, I_XYB + 2);
 #pragma unroll
     for (int o = 0; o < 6; o++) {
         const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -302,7 +306,7 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
 // consecutive outputs. The input rows start at x0 - RA (RA = R rounded up to a multiple of 4, so
 // the cp.async chunks are 16-byte aligned) and are read back as float4 (pitch 180 = 45 quads:
 // conflict-free); the thread's window starts RA - R floats into its first quad.
-// grid (ceil(w/128), ceil(h/16), 6*npairs): z -> pair = z/6, plane = src_id + z%6.
+// grid (ceil(w/128), ceil(h/16), 3*nimages): z -> image = z/3, plane = src_id + z%3.
 constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180;
 
 template <int KI, int R>
@@ -314,10 +318,10 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ w
     constexpr int OFF = RA - R;
     constexpr int NV4 = (OFF + 8 + 2 * R + 3) / 4;
     static_assert(IW <= HB_P && 120 + 4 * NV4 <= HB_P, "hblur tile");
-    const int pair = blockIdx.z / 6, pl = blockIdx.z % 6;
+    const int img = blockIdx.z / 3, pl = blockIdx.z % 3;
     const BScaleDev S = pick_scale(g, s);
-    const float* src = bplane(work, g, S, pair, src_id + pl);
-    float* dst = bplane(work, g, S, pair, dst_id + pl);
+    const float* src = iplane(work, g, S, img, src_id + pl);
+    float* dst = iplane(work, g, S, img, dst_id + pl);
     const int x0 = blockIdx.x * HB_TW, y0 = blockIdx.y * HB_TH;
     stage_rows<256>(in, HB_P, src, S.p, S.w, S.h, x0 - RA, y0, HB_TH, IW / 4);
     cp_async_commit();
@@ -354,22 +358,22 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ w
 
 // Separable vertical pass over the three channels of one image: 32x64 tile, each thread makes
 // 8 consecutive rows of one column for every channel, then runs the fused epilogue.
-// grid (ceil(w/32), ceil(h/64), 2*npairs).
+// grid (ceil(w/32), ceil(h/64), nimages).
 constexpr int VB_TW = 32, VB_TH = 64;
 
 template <int KI, int R>
-__device__ __forceinline__ void vblur3(float* in, float* ctr, float* __restrict__ work, const BGeom& g, int pair,
+__device__ __forceinline__ void vblur3(float* in, float* ctr, float* __restrict__ work, const BGeom& g, int img,
                                        int s, int src_id, int ctr_id, int nctr, float out[3][8]) {
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * VB_TW, y0 = blockIdx.y * VB_TH;
     constexpr int IH = VB_TH + 2 * R;
 #pragma unroll
     for (int c = 0; c < 3; c++)
-        stage_rows<256>(in + c * IH * VB_TW, VB_TW, bplane(work, g, S, pair, src_id + c), S.p, S.w, S.h, x0, y0 - R,
+        stage_rows<256>(in + c * IH * VB_TW, VB_TW, iplane(work, g, S, img, src_id + c), S.p, S.w, S.h, x0, y0 - R,
                         IH, VB_TW / 4);
     // the epilogue's own-pixel planes, staged with the blur input so their latency overlaps
     for (int c = 0; c < nctr; c++)
-        stage_rows<256>(ctr + c * VB_TH * VB_TW, VB_TW, bplane(work, g, S, pair, ctr_id + c), S.p, S.w, S.h, x0, y0,
+        stage_rows<256>(ctr + c * VB_TH * VB_TW, VB_TW, iplane(work, g, S, img, ctr_id + c), S.p, S.w, S.h, x0, y0,
                         VB_TH, VB_TW / 4);
     cp_async_commit();
     cp_async_wait<0>();
@@ -399,9 +403,9 @@ constexpr int kVLfSmem = (3 * (VB_TH + 42) * VB_TW + 3 * VB_TH * VB_TW) * 4;
 __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ work, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* ctr = sm + 3 * (VB_TH + 42) * VB_TW;
-    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const int img = blockIdx.z;
     float lf[3][8];
-    vblur3<4, 21>(sm, ctr, work, g, pair, s, P_TMP + img * 3, P_XYB + img * 3, 3, lf);
+    vblur3<4, 21>(sm, ctr, work, g, img, s, I_TMP, I_XYB, 3, lf);
     const BScaleDev S = pick_scale(g, s);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     const int x = blockIdx.x * VB_TW + vc;
@@ -411,8 +415,8 @@ __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ wo
     float* lfv[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        xyb[c] = bplane(work, g, S, pair, P_XYB + img * 3 + c);
-        lfv[c] = bplane(work, g, S, pair, P_LFV + img * 3 + c);
+        xyb[c] = iplane(work, g, S, img, I_XYB + c);
+        lfv[c] = iplane(work, g, S, img, I_LFV + c);
     }
 #pragma unroll
     for (int o = 0; o < 8; o++) {
@@ -455,19 +459,19 @@ constexpr int kVMfSmem = (3 * (VB_TH + 18) * VB_TW + 2 * VB_TH * VB_TW) * 4;
 __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ work, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* ctr = sm + 3 * (VB_TH + 18) * VB_TW;
-    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const int img = blockIdx.z;
     float mf[3][8];
-    vblur3<3, 9>(sm, ctr, work, g, pair, s, P_TMP + img * 3, P_XYB + img * 3, 2, mf);
+    vblur3<3, 9>(sm, ctr, work, g, img, s, I_TMP, I_XYB, 2, mf);
     const BScaleDev S = pick_scale(g, s);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     const int x = blockIdx.x * VB_TW + vc;
     const int yb = blockIdx.y * VB_TH + 8 * vg;
     if (x >= S.w) return;
-    float* d0 = bplane(work, g, S, pair, P_XYB + img * 3 + 0);
-    float* d1 = bplane(work, g, S, pair, P_XYB + img * 3 + 1);
-    float* m0 = bplane(work, g, S, pair, P_MF + img * 3 + 0);
-    float* m1 = bplane(work, g, S, pair, P_MF + img * 3 + 1);
-    float* m2 = bplane(work, g, S, pair, P_MF + img * 3 + 2);
+    float* d0 = iplane(work, g, S, img, I_XYB + 0);
+    float* d1 = iplane(work, g, S, img, I_XYB + 1);
+    float* m0 = iplane(work, g, S, img, I_MF + 0);
+    float* m1 = iplane(work, g, S, img, I_MF + 1);
+    float* m2 = iplane(work, g, S, img, I_MF + 2);
     const float sx = 0.653020556257f, yw = 46.0f;
 #pragma unroll
     for (int o = 0; o < 8; o++) {
@@ -487,18 +491,18 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ wo
     }
 }
 
-// HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), 2*npairs)
+// HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), nimages)
 __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ work, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
-    const int img = blockIdx.z & 1, pair = blockIdx.z >> 1;
+    const int img = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
     float rxy[6];
     tile_masses_r8<1>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    tile_stage_r8(sm, bplane(work, g, S, pair, P_XYB + img * 3), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, bplane(work, g, S, pair, P_XYB + img * 3 + 1), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(work, g, S, img, I_XYB), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, iplane(work, g, S, img, I_XYB + 1), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -510,8 +514,8 @@ __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ w
 #pragma unroll
         for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
-        float* hfp = bplane(work, g, S, pair, P_HF + img * 2 + c);
-        float* uhfp = bplane(work, g, S, pair, P_UHF + img * 2 + c);
+        float* hfp = iplane(work, g, S, img, I_HF + c);
+        float* uhfp = iplane(work, g, S, img, I_UHF + c);
 #pragma unroll
         for (int o = 0; o < 6; o++) {
             const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -642,16 +646,19 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 #undef SQ
 
 // grid (ceil(w/32), ceil(h/64), npairs), 256 threads; column tid&31, rows 8*(tid>>5)..+7.
+// pimg[pair] = (reference image, distorted image).
 // The six maps' raw (l0, l1) tiles are staged with cp.async, double-buffered across maps;
 // samples outside the image arrive as zeros, for which malta_pre returns exactly 0, the
 // reference's padding value (maltaDiff.hpp:549-553).
 constexpr int DF_RAW = DF_IH * DF_IW;
 constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW) * 4;
 
-__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__ work, BGeom g, int s) {
+__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__ work, const int2* __restrict__ pimg,
+                                                             BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* Dt = sm + 4 * DF_RAW;
-    const int pair = blockIdx.z;
+    const int2 pi = pimg[blockIdx.z];
+    const int i0 = pi.x, i1 = pi.y;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * DF_TW, y0 = blockIdx.y * DF_TH;
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
@@ -661,14 +668,12 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
         acX[o] = 0.f;
         acY[o] = 0.f;
     }
-    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X; image 1's plane is
-    // `per_img` ids after image 0's.
-    auto plane_id = [](int m) { return (m < 2 ? P_UHF : m < 4 ? P_HF : P_MF) + 1 - (m & 1); };
-    auto per_img = [](int m) { return m < 4 ? 2 : 3; };
-    stage_rows<256>(sm, DF_IW, bplane(work, g, S, pair, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X
+    auto plane_id = [](int m) { return (m < 2 ? I_UHF : m < 4 ? I_HF : I_MF) + 1 - (m & 1); };
+    stage_rows<256>(sm, DF_IW, iplane(work, g, S, i0, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
                     DF_IW / 4);
-    stage_rows<256>(sm + DF_RAW, DF_IW, bplane(work, g, S, pair, plane_id(0) + per_img(0)), S.p, S.w, S.h,
-                    x0 - DF_H, y0 - DF_H, DF_IH, DF_IW / 4);
+    stage_rows<256>(sm + DF_RAW, DF_IW, iplane(work, g, S, i1, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
+                    DF_IH, DF_IW / 4);
     cp_async_commit();
 #pragma unroll 1
     for (int m = 0; m < 6; m++) {
@@ -677,10 +682,10 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
         if (m < 5) {
             float* n0 = sm + ((m + 1) & 1) * 2 * DF_RAW;
             const int id = plane_id(m + 1);
-            stage_rows<256>(n0, DF_IW, bplane(work, g, S, pair, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+            stage_rows<256>(n0, DF_IW, iplane(work, g, S, i0, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
                             DF_IW / 4);
-            stage_rows<256>(n0 + DF_RAW, DF_IW, bplane(work, g, S, pair, id + per_img(m + 1)), S.p, S.w, S.h,
-                            x0 - DF_H, y0 - DF_H, DF_IH, DF_IW / 4);
+            stage_rows<256>(n0 + DF_RAW, DF_IW, iplane(work, g, S, i1, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
+                            DF_IH, DF_IW / 4);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -722,15 +727,16 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
             float hf[2][2], uhf[2][2], mf[2][3], lf[2][3];
 #pragma unroll
             for (int m = 0; m < 2; m++) {
+                const int im = m ? i1 : i0;
 #pragma unroll
                 for (int c = 0; c < 2; c++) {
-                    hf[m][c] = __ldg(bplane(work, g, S, pair, P_HF + m * 2 + c) + i);
-                    uhf[m][c] = __ldg(bplane(work, g, S, pair, P_UHF + m * 2 + c) + i);
+                    hf[m][c] = __ldg(iplane(work, g, S, im, I_HF + c) + i);
+                    uhf[m][c] = __ldg(iplane(work, g, S, im, I_UHF + c) + i);
                 }
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    mf[m][c] = __ldg(bplane(work, g, S, pair, P_MF + m * 3 + c) + i);
-                    lf[m][c] = __ldg(bplane(work, g, S, pair, P_LFV + m * 3 + c) + i);
+                    mf[m][c] = __ldg(iplane(work, g, S, im, I_MF + c) + i);
+                    lf[m][c] = __ldg(iplane(work, g, S, im, I_LFV + c) + i);
                 }
             }
 #pragma unroll
@@ -755,8 +761,8 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
                 const float dl = lf[0][c] - lf[1][c];
                 dc[c] += P.wlf[c] * dl * dl;
             }
-            bplane(work, g, S, pair, P_SAC)[i] = ac[0] + ac[1] + ac[2];
-            bplane(work, g, S, pair, P_SDC)[i] = dc[0] + dc[1] + dc[2];
+            iplane(work, g, S, i1, Q_SAC)[i] = ac[0] + ac[1] + ac[2];
+            iplane(work, g, S, i1, Q_SDC)[i] = dc[0] + dc[1] + dc[2];
             // maskinit + diffPrecompute (maskPsycho.hpp:3-40). sqrt(m + b) - sqrt(b) is evaluated
             // as m / (sqrt(m + b) + sqrt(b)): the same value without the cancellation.
 #pragma unroll
@@ -764,7 +770,7 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
                 const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
                 const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
                 const float mk = mul * sqrtf(xd * xd + yd * yd);
-                bplane(work, g, S, pair, P_PRE0 + m)[i] = mk / (sqrtf(mk + bias) + sqb);
+                iplane(work, g, S, i1, Q_PRE0 + m)[i] = mk / (sqrtf(mk + bias) + sqb);
             }
         }
     }
@@ -772,16 +778,17 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
 
 // Blur both mask planes (sigma 2.7); store B0 and add 10*(B0-B1)^2 to the AC sum.
 // grid (ceil(w/32), ceil(h/48), npairs)
-__global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restrict__ work, BGeom g, int s) {
+__global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restrict__ work,
+                                                                  const int2* __restrict__ pimg, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
-    const int pair = blockIdx.z;
+    const int i1 = pimg[blockIdx.z].y;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
     float rxy[6];
     tile_masses_r8<2>(x0, y0, S.w, S.h, rxy);
-    tile_stage_r8(sm, bplane(work, g, S, pair, P_PRE0), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, bplane(work, g, S, pair, P_PRE1), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(work, g, S, i1, Q_PRE0), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, iplane(work, g, S, i1, Q_PRE1), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -792,8 +799,8 @@ __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restr
         __syncthreads();
     }
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    float* b0 = bplane(work, g, S, pair, P_B0);
-    float* sac = bplane(work, g, S, pair, P_SAC);
+    float* b0 = iplane(work, g, S, i1, Q_B0);
+    float* sac = iplane(work, g, S, i1, Q_SAC);
 #pragma unroll
     for (int o = 0; o < 6; o++) {
         const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -841,17 +848,19 @@ __device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float&
 }
 
 // Fuzzy erosion + diffmap; FINAL also folds in the half-scale map, stores the distortion map
-// and emits norm partials. grid (ceil(w/32), ceil(h/8), npairs), block (32, 8).
+// (when distmap is not null) and emits norm partials. grid (ceil(w/32), ceil(h/8), npairs),
+// block (32, 8).
 template <bool FINAL>
-__global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__ work, BGeom g, int s,
-                                                             float* __restrict__ distmap, float* __restrict__ partials,
-                                                             float qnorm) {
+__global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__ work, const int2* __restrict__ pimg,
+                                                             BGeom g, int s, float* __restrict__ distmap,
+                                                             float* __restrict__ partials, float qnorm) {
     const int pair = blockIdx.z;
+    const int i1 = pimg[pair].y;
     const BScaleDev S = pick_scale(g, s);
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     float sq = 0.f, s3 = 0.f, mx = 0.f;
     if (x < S.w && y < S.h) {
-        const float* b0 = bplane(work, g, S, pair, P_B0);
+        const float* b0 = iplane(work, g, S, i1, Q_B0);
         const int k = 3;
         const int W = S.w, H = S.h, p = S.p;
         float m0 = b0[(int64_t)y * p + x], m1 = 2.0f * m0, m2 = m1;
@@ -869,16 +878,16 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__
         if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x], m0, m1, m2);
         const float mask = 0.45f * m0 + 0.3f * m1 + 0.25f * m2;
         const int64_t i = (int64_t)y * p + x;
-        float d = sqrtf(mask_y(mask) * bplane(work, g, S, pair, P_SAC)[i] +
-                        mask_dc_y(mask) * bplane(work, g, S, pair, P_SDC)[i]);
+        float d = sqrtf(mask_y(mask) * iplane(work, g, S, i1, Q_SAC)[i] +
+                        mask_dc_y(mask) * iplane(work, g, S, i1, Q_SDC)[i]);
         if (!FINAL) {
-            bplane(work, g, S, pair, P_DIFF)[i] = d;
+            iplane(work, g, S, i1, Q_DIFF)[i] = d;
         } else {
             constexpr DConst k085 = dconst(1.0 - 0.3 * (double)0.5f);
             const BScaleDev Hs = g.s[1];
-            const float small = bplane(work, g, Hs, pair, P_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
+            const float small = iplane(work, g, Hs, i1, Q_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
             d = fmaf(0.5f, small, mul_dc(d, k085));
-            distmap[(int64_t)pair * W * H + (int64_t)y * W + x] = d;
+            if (distmap) distmap[(int64_t)pair * W * H + (int64_t)y * W + x] = d;
             sq = powf(d, qnorm);
             s3 = fabsf(d) * d * d;
             mx = fabsf(d);
@@ -965,11 +974,11 @@ static BGeom make_bgeom(int64_t w, int64_t h) {
         S.p = (int)round_up(cw, 8);
         S.n = round_up((int64_t)S.p * ch, 64);
         S.base = off;
-        off += S.n * NPLANES;
+        off += S.n * NIMG;
         cw = half_dim(cw);
         ch = half_dim(ch);
     }
-    g.pair_floats = off;
+    g.img_floats = off;
     g.norm_tiles_x = (int)ceil_div(w, 32);
     g.norm_tiles = g.norm_tiles_x * (int)ceil_div(h, 8);
     return g;
@@ -1016,19 +1025,37 @@ static DiffParams make_diff_params() {
 
 constexpr int kTileSmem = (2 * TB_RAW + TB_HPL) * 4;
 
+__global__ void butter_identity_pairs_kernel(int2* pimg, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pimg[i] = make_int2(2 * i, 2 * i + 1);
+}
+
 int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensity_, int max_pairs_) {
+    int rc = init_images(width, height, qnorm_, intensity_, 2 * max_pairs_, max_pairs_, true);
+    if (rc) return rc;
+    VSHIP_CUDA_TRY(cudaMalloc(&pimg_identity, sizeof(int2) * max_pairs));
+    butter_identity_pairs_kernel<<<(unsigned)ceil_div(max_pairs, 256), 256>>>(pimg_identity, max_pairs);
+    VSHIP_CUDA_TRY(cudaGetLastError());
+    VSHIP_CUDA_TRY(cudaDeviceSynchronize());
+    return E_OK;
+}
+
+int ButterEngine::init_images(int64_t width, int64_t height, int qnorm_, float intensity_, int max_images_,
+                              int max_pairs_, bool keep_distmap) {
     w = width;
     h = height;
     qnorm = qnorm_;
     intensity = intensity_;
+    max_images = max_images_;
     max_pairs = max_pairs_;
+    if (max_images <= 0 || max_pairs <= 0) return E_BAD_POINTER;
     BGeom g = make_bgeom(w, h);
     for (int s = 0; s < 2; s++) {
         sc[s].w = g.s[s].w;
         sc[s].h = g.s[s].h;
         sc[s].n = g.s[s].n;
     }
-    work_floats = g.pair_floats;
+    img_floats = g.img_floats;
     norm_blocks = g.norm_tiles;
     int rc = upload_butter_tables();
     if (rc) return rc;
@@ -1039,9 +1066,9 @@ int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensit
         const DiffParams P = make_diff_params();
         VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
     }
-    VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * work_floats * max_pairs));
+    VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * img_floats * max_images));
     VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
-    VSHIP_CUDA_TRY(cudaMalloc(&distmap, sizeof(float) * (size_t)w * h * max_pairs));
+    if (keep_distmap) VSHIP_CUDA_TRY(cudaMalloc(&distmap, sizeof(float) * (size_t)w * h * max_pairs));
     VSHIP_CUDA_TRY(cudaMalloc(&norms, sizeof(double) * 3 * max_pairs));
     return E_OK;
 }
@@ -1051,25 +1078,35 @@ void ButterEngine::destroy() {
     if (partials) cudaFree(partials);
     if (distmap) cudaFree(distmap);
     if (norms) cudaFree(norms);
+    if (pimg_identity) cudaFree(pimg_identity);
     work = nullptr;
     partials = nullptr;
     distmap = nullptr;
     norms = nullptr;
+    pimg_identity = nullptr;
 }
+
+size_t ButterEngine::image_bytes(int64_t w, int64_t h) { return sizeof(float) * (size_t)make_bgeom(w, h).img_floats; }
 
 size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs) {
     BGeom g = make_bgeom(w, h);
-    return (sizeof(float) * (size_t)g.pair_floats + sizeof(float) * 3 * (size_t)g.norm_tiles +
-            sizeof(float) * (size_t)w * h + sizeof(double) * 3) *
+    return (sizeof(float) * 2 * (size_t)g.img_floats + sizeof(float) * 3 * (size_t)g.norm_tiles +
+            sizeof(float) * (size_t)w * h + sizeof(double) * 3 + sizeof(int2)) *
            pairs;
 }
 
 int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st) {
-    if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
+    if (npairs <= 0 || npairs > max_pairs || !pimg_identity) return E_BAD_POINTER;
+    return launch_images(frames_dev, 2 * npairs, pimg_identity, npairs, intype, norms_out, distmap, st);
+}
+
+int ButterEngine::launch_images(const FrameDesc* frames_dev, int nimages, const int2* pimg, int npairs, int intype,
+                                double* norms_out, float* distmap_out, cudaStream_t st) {
+    if (nimages <= 0 || nimages > max_images || npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
     const BGeom g = make_bgeom(w, h);
-    const unsigned np = (unsigned)npairs;
+    const unsigned ni = (unsigned)nimages, np = (unsigned)npairs;
     {
-        dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), 2 * np);
+        dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), ni);
         ProfScope ps_("butter_decode", st);
         switch (intype) {
             case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
@@ -1081,24 +1118,24 @@ int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
     }
     for (int s = 1; s >= 0; s--) {
         const int64_t sw = g.s[s].w, sh = g.s[s].h;
-        const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), 2 * np);
-        const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 6 * np);
-        const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), 2 * np);
+        const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), ni);
+        const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 3 * ni);
+        const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), ni);
         { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s, intensity); }
-        { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(work, g, s, P_XYB, P_TMP); }
+        { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(work, g, s, I_XYB, I_TMP); }
         { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(work, g, s); }
-        { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(work, g, s, P_XYB, P_TMP); }
+        { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(work, g, s, I_XYB, I_TMP); }
         { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(work, g, s); }
         { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s); }
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
-        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(work, g, s); }
+        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(work, pimg, g, s); }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
-        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(work, g, s); }
+        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(work, pimg, g, s); }
         const dim3 gf((unsigned)ceil_div(sw, 32), (unsigned)ceil_div(sh, 8), np);
         if (s == 1)
-            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, dim3(32, 8), 0, st>>>(work, g, s, distmap, partials, (float)qnorm); }
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, dim3(32, 8), 0, st>>>(work, pimg, g, s, nullptr, partials, (float)qnorm); }
         else
-            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, dim3(32, 8), 0, st>>>(work, g, s, distmap, partials, (float)qnorm); }
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, dim3(32, 8), 0, st>>>(work, pimg, g, s, distmap_out, partials, (float)qnorm); }
     }
     { ProfScope ps_("butter_finalize", st); butter_finalize_kernel<<<np, 256, 0, st>>>(partials, norms_out ? norms_out : norms, g, qnorm); }
     VSHIP_CUDA_TRY(cudaGetLastError());

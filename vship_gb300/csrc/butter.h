@@ -15,28 +15,41 @@ struct ButterScale {
     int64_t n;  // w*h
 };
 
-// Device workspace and launch sequence for up to `max_pairs` frame pairs of one resolution.
+// Device workspace and launch sequence of one resolution. The workspace holds up to max_images
+// images (each its planes at both scales); a launch runs every image's own stage once, then
+// every pair's stage on (reference image, distorted image) index pairs, so an image can serve
+// as the reference of several pairs.
 class ButterEngine {
 public:
     int64_t w = 0, h = 0;
     int qnorm = 2;
     float intensity = 203.f;
-    int max_pairs = 0;
+    int max_pairs = 0, max_images = 0;
     ButterScale sc[2]{};
-    float* work = nullptr;       // all intermediate planes
-    size_t work_floats = 0;      // per pair
-    float* partials = nullptr;   // norm partial sums
+    float* work = nullptr;          // all intermediate planes, [image][scale][plane]
+    size_t img_floats = 0;          // per image
+    float* partials = nullptr;      // norm partial sums
     int norm_blocks = 0;
-    float* distmap = nullptr;    // [pair][h][w]
-    double* norms = nullptr;     // [pair][3]
+    float* distmap = nullptr;       // [pair][h][w] (paired form)
+    double* norms = nullptr;        // [pair][3]
+    int2* pimg_identity = nullptr;  // (2p, 2p + 1): the paired form's pair table
 
+    // Paired form: images 2p and 2p + 1 are pair p's reference and distorted frames.
     int init(int64_t width, int64_t height, int qnorm, float intensity, int max_pairs);
+    // Image/pair form; keep_distmap allocates this->distmap for max_pairs maps.
+    int init_images(int64_t width, int64_t height, int qnorm, float intensity, int max_images, int max_pairs,
+                    bool keep_distmap);
     void destroy();
     // frames_dev: 2*npairs FrameDesc in device memory (pair-major: reference, distorted).
     // Writes the final distortion maps to this->distmap and {Qnorm, 3-norm, inf-norm} to
     // norms_out (device, 3 doubles per pair) or to this->norms when norms_out is null.
     int launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st);
+    // frames_dev: nimages FrameDesc (device); pimg: npairs (reference, distorted) image indices
+    // (device); distmap_out: null or npairs maps.
+    int launch_images(const FrameDesc* frames_dev, int nimages, const int2* pimg, int npairs, int intype,
+                      double* norms_out, float* distmap_out, cudaStream_t st);
     static size_t device_bytes(int64_t w, int64_t h, int pairs);
+    static size_t image_bytes(int64_t w, int64_t h);
 };
 
 }  // namespace vship

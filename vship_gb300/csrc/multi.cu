@@ -4,8 +4,9 @@
 //   SSIMU2     source pyramids   max_src[r]   x 3 x plane_elems FP32
 //              candidate pyramids max_pairs[r] x 3 x plane_elems FP32, or FP16 deltas
 //              partial sums      max_pairs[r] x 18 x tiles_total FP32
-//   Butteraugli one ButterEngine holding b_chunk[r] pair workspaces; a batch of that resolution
-//              runs as ceil(count / b_chunk[r]) chunks
+//   Butteraugli one ButterEngine holding b_cap_img[r] image workspaces; a batch of that resolution
+//              runs as chunks of whole (source, candidates) groups that fit, a source's image
+//              stage running once per chunk it appears in
 // plus the small tables the kernels walk: image descriptors (re-uploaded every call from pinned
 // staging, since the frame pointers change), pair table and work items (uploaded when the batch
 // layout changes).
@@ -31,7 +32,21 @@ __global__ void multi_scatter_norms_kernel(const double* __restrict__ grouped, c
     }
 }
 
-static constexpr size_t kButterChunkBudget = (size_t)6 << 30;  // bytes of pair workspace per resolution
+// Bytes of Butteraugli image workspace per resolution: 6 GiB, or $VSHIP_BUTTER_CHUNK_BYTES.
+static size_t butter_chunk_budget() {
+    if (const char* e = getenv("VSHIP_BUTTER_CHUNK_BYTES")) {
+        const long long v = atoll(e);
+        if (v > 0) return (size_t)v;
+    }
+    return (size_t)6 << 30;
+}
+
+static void butter_caps(int64_t w, int64_t h, int max_src, int max_pairs, int* cap_img, int* cap_pair) {
+    const size_t one = ButterEngine::image_bytes(w, h);
+    const int fit = (int)std::min<size_t>(1 << 20, std::max<size_t>(2, butter_chunk_budget() / one));
+    *cap_img = std::min(fit, std::max(2, max_src + max_pairs));
+    *cap_pair = std::max(1, std::min(max_pairs, *cap_img - 1));
+}
 
 size_t MultiEngine::device_bytes(int nres, const int* widths, const int* heights, const int* max_sources,
                                  const int* max_pairs, int flags) {
@@ -48,9 +63,10 @@ size_t MultiEngine::device_bytes(int nres, const int* widths, const int* heights
             total += (size_t)max_pairs[r] * g.tiles_total * sizeof(int2);
         }
         if ((flags & MULTI_BUTTERAUGLI) && max_pairs[r] > 0) {
-            const size_t one = ButterEngine::device_bytes(widths[r], heights[r], 1);
-            const int chunk = (int)std::min<size_t>((size_t)max_pairs[r], std::max<size_t>(1, kButterChunkBudget / one));
-            total += one * chunk;
+            int ci = 0, cp = 0;
+            butter_caps(widths[r], heights[r], max_sources[r], max_pairs[r], &ci, &cp);
+            total += ButterEngine::image_bytes(widths[r], heights[r]) * ci +
+                     (size_t)cp * (3 * 4 * (size_t)ceil_div(widths[r], 32) * (size_t)ceil_div(heights[r], 8) + 24);
         }
     }
     return total;
@@ -118,13 +134,14 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
     if (flags & MULTI_BUTTERAUGLI) {
         for (int r = 0; r < nres; r++) {
             if (!max_pairs[r]) continue;
-            const size_t one = ButterEngine::device_bytes(rw[r], rh[r], 1);
-            b_chunk[r] = (int)std::min<size_t>((size_t)max_pairs[r], std::max<size_t>(1, kButterChunkBudget / one));
-            int rc = b_eng[r].init(rw[r], rh[r], qnorm, intensity, b_chunk[r]);
+            butter_caps(rw[r], rh[r], max_src[r], max_pairs[r], &b_cap_img[r], &b_cap_pair[r]);
+            int rc = b_eng[r].init_images(rw[r], rh[r], qnorm, intensity, b_cap_img[r], b_cap_pair[r], false);
             if (rc) return rc;
         }
+        // a chunk image per pair plus its source at worst
         VSHIP_CUDA_TRY(cudaMalloc(&b_frames_d, sizeof(FrameDesc) * 2 * pair_cap));
         VSHIP_CUDA_TRY(cudaMallocHost(&b_frames_h, sizeof(FrameDesc) * 2 * pair_cap));
+        VSHIP_CUDA_TRY(cudaMalloc(&b_pimg_d, sizeof(int2) * pair_cap));
         VSHIP_CUDA_TRY(cudaMalloc(&b_norms_d, sizeof(double) * 3 * pair_cap * 2));
         VSHIP_CUDA_TRY(cudaMalloc(&b_perm_d, sizeof(int) * pair_cap));
     }
@@ -152,6 +169,7 @@ void MultiEngine::destroy() {
     if (s_sitems_d) cudaFree(s_sitems_d);
     if (b_frames_d) cudaFree(b_frames_d);
     if (b_frames_h) cudaFreeHost(b_frames_h);
+    if (b_pimg_d) cudaFree(b_pimg_d);
     if (b_norms_d) cudaFree(b_norms_d);
     if (b_perm_d) cudaFree(b_perm_d);
     geoms_d = nullptr;
@@ -163,6 +181,7 @@ void MultiEngine::destroy() {
     s_sitems_d = nullptr;
     b_frames_d = nullptr;
     b_frames_h = nullptr;
+    b_pimg_d = nullptr;
     b_norms_d = nullptr;
     b_perm_d = nullptr;
     if (staging_free) cudaEventDestroy(staging_free);
@@ -234,13 +253,46 @@ int MultiEngine::build_plan(int nsrc, const int* src_res, int npairs, const int*
         VSHIP_CUDA_TRY(cudaMemcpyAsync(s_pitems_d, pit.data(), sizeof(int4) * pit.size(), cudaMemcpyHostToDevice, st));
     }
     if (flags & MULTI_BUTTERAUGLI) {
+        // chunks of whole (source, candidates) groups, split only where one group alone exceeds
+        // the resolution's workspace
+        std::vector<std::vector<int>> by_src(nsrc);
+        for (int j = 0; j < npairs; j++) by_src[cand_src[j]].push_back(j);
         std::vector<int> perm;
+        std::vector<int2> pimg;
+        b_chunks.clear();
+        b_img_of.clear();
         for (int r = 0; r < nres; r++) {
-            b_first[r] = (int)perm.size();
-            for (int j = 0; j < npairs; j++)
-                if (src_res[cand_src[j]] == r) perm.push_back(j);
-            b_count[r] = (int)perm.size() - b_first[r];
+            BChunk cur{r, (int)b_img_of.size(), 0, (int)perm.size(), 0};
+            auto flush = [&]() {
+                if (cur.npairs) b_chunks.push_back(cur);
+                cur = BChunk{r, (int)b_img_of.size(), 0, (int)perm.size(), 0};
+            };
+            for (int s = 0; s < nsrc; s++) {
+                if (src_res[s] != r) continue;
+                int src_local = -1;
+                for (size_t k = 0; k < by_src[s].size();) {
+                    const int need = (src_local < 0 ? 1 : 0) + 1;
+                    if (cur.nimg + need > b_cap_img[r] || cur.npairs + 1 > b_cap_pair[r]) {
+                        flush();
+                        src_local = -1;
+                        continue;
+                    }
+                    if (src_local < 0) {
+                        src_local = cur.nimg++;
+                        b_img_of.push_back(s);
+                    }
+                    const int j = by_src[s][k++];
+                    const int cand_local = cur.nimg++;
+                    b_img_of.push_back(-1 - j);
+                    pimg.push_back(make_int2(src_local, cand_local));
+                    perm.push_back(j);
+                    cur.npairs++;
+                }
+            }
+            flush();
         }
+        if ((int)b_img_of.size() > 2 * pair_cap) return E_BAD_POINTER;
+        VSHIP_CUDA_TRY(cudaMemcpyAsync(b_pimg_d, pimg.data(), sizeof(int2) * pimg.size(), cudaMemcpyHostToDevice, st));
         VSHIP_CUDA_TRY(cudaMemcpyAsync(b_perm_d, perm.data(), sizeof(int) * npairs, cudaMemcpyHostToDevice, st));
     }
     plan_valid = true;
@@ -301,14 +353,10 @@ void MultiEngine::fill_images(int nsrc, const FrameDesc* src, int npairs, const 
         }
     }
     if (flags & MULTI_BUTTERAUGLI) {
-        int g = 0;
-        for (int r = 0; r < nres; r++)
-            for (int j = 0; j < npairs; j++)
-                if (plan_src_res[plan_cand_src[j]] == r) {
-                    b_frames_h[2 * g] = src[plan_cand_src[j]];
-                    b_frames_h[2 * g + 1] = cand[j];
-                    g++;
-                }
+        for (size_t k = 0; k < b_img_of.size(); k++) {
+            const int f = b_img_of[k];
+            b_frames_h[k] = f >= 0 ? src[f] : cand[-1 - f];
+        }
     }
 }
 
@@ -326,14 +374,11 @@ int MultiEngine::enqueue(int npairs, cudaStream_t st) {
         if (rc) return rc;
     }
     if (flags & MULTI_BUTTERAUGLI) {
-        for (int r = 0; r < nres && !rc; r++) {
-            for (int c0 = 0; c0 < b_count[r] && !rc; c0 += b_chunk[r]) {
-                const int n = std::min(b_chunk[r], b_count[r] - c0);
-                const int g = b_first[r] + c0;
-                rc = b_eng[r].launch(b_frames_d + 2 * g, plan_intype, n, b_norms_d + 3 * g, st);
-            }
+        for (const BChunk& c : b_chunks) {
+            rc = b_eng[c.res].launch_images(b_frames_d + c.img_off, c.nimg, b_pimg_d + c.pair_off, c.npairs,
+                                            plan_intype, b_norms_d + 3 * c.pair_off, nullptr, st);
+            if (rc) return rc;
         }
-        if (rc) return rc;
         multi_scatter_norms_kernel<<<(unsigned)ceil_div(3 * npairs, 256), 256, 0, st>>>(
             b_norms_d, b_perm_d, b_norms_d + 3 * pair_cap, npairs);
         VSHIP_CUDA_TRY(cudaGetLastError());
@@ -499,7 +544,7 @@ int MultiEngine::compute(int nsrc, const FrameDesc* src, const int* src_res, int
         VSHIP_CUDA_TRY(cudaMemcpyAsync(s_imgs_d, s_imgs_h, sizeof(Ssimu2MultiImage) * (nsrc + npairs),
                                        cudaMemcpyHostToDevice, st));
     if (flags & MULTI_BUTTERAUGLI)
-        VSHIP_CUDA_TRY(cudaMemcpyAsync(b_frames_d, b_frames_h, sizeof(FrameDesc) * 2 * npairs,
+        VSHIP_CUDA_TRY(cudaMemcpyAsync(b_frames_d, b_frames_h, sizeof(FrameDesc) * b_img_of.size(),
                                        cudaMemcpyHostToDevice, st));
     VSHIP_CUDA_TRY(cudaEventRecord(staging_free, st));
     if (tune_now) {

@@ -7,7 +7,9 @@
 //                   per source), one for the candidates (FP32, or FP16 deltas against their
 //                   source's pyramid), one persistent stats launch over (pair, tile) items of all
 //                   resolutions, one finalize launch;
-//   Butteraugli  -- the per-resolution batch pipeline over chunks of pairs.
+//   Butteraugli  -- per resolution, chunks of (source, its candidates) groups: every image's own
+//                   stage (decode, opsin, frequency bands) once per chunk, then every pair's
+//                   stage against its source's planes.
 // The launch sequence of a given batch layout is captured once in a CUDA graph and replayed
 // while the layout (resolution of each source, source of each candidate, sample type) repeats.
 // Launch knobs (persistent grid, work order) come from a small autotuner whose choices are
@@ -81,14 +83,19 @@ private:
     int n_pitems_src = 0, n_pitems_cand = 0, n_sitems = 0;
     size_t cap_pitems = 0, cap_sitems = 0;
     int stats_blocks_per_sm = 1;
-    // Butteraugli state: one chunked batch engine per resolution
+    // Butteraugli state: one image/pair engine per resolution, run over chunks
+    struct BChunk {
+        int res, img_off, nimg, pair_off, npairs;
+    };
     ButterEngine b_eng[kMaxRes];
-    int b_chunk[kMaxRes]{};
-    FrameDesc* b_frames_d = nullptr;  // [pair_cap][2] grouped by resolution
+    int b_cap_img[kMaxRes]{}, b_cap_pair[kMaxRes]{};
+    std::vector<BChunk> b_chunks;
+    std::vector<int> b_img_of;        // chunk image -> caller frame (source i >= 0, candidate j as -1 - j)
+    FrameDesc* b_frames_d = nullptr;  // chunk images' descriptors, all chunks back to back
     FrameDesc* b_frames_h = nullptr;  // pinned staging
-    double* b_norms_d = nullptr;      // grouped by resolution
-    int* b_perm_d = nullptr;          // grouped index -> caller's pair index
-    int b_count[kMaxRes]{}, b_first[kMaxRes]{};
+    int2* b_pimg_d = nullptr;         // per grouped pair: (source, candidate) image inside its chunk
+    double* b_norms_d = nullptr;      // grouped norms, then the caller-ordered copy
+    int* b_perm_d = nullptr;          // grouped pair -> caller's pair index
 
     // current layout
     bool plan_valid = false;
