@@ -653,6 +653,182 @@ def bench_multi(v, args, ws, rank):
     return res
 
 
+# ------------------------------------------------------------------------------------------
+# serving loop: Poisson arrivals, 70 % SSIMU2 / 30 % Butteraugli, 1..16 pairs per request,
+# source reuse probability 0.8, 64 GB admission budget
+
+SERVE_RATES = [50, 100, 200, 500, 1000, 2000]
+
+
+def wait_until(t0, ta):
+    """Sleep, then spin the last millisecond, until ta seconds after t0 (the spin is short, so
+    worker threads keep getting the interpreter)."""
+    while True:
+        dt = ta - (time.perf_counter() - t0)
+        if dt <= 0:
+            return
+        if dt > 0.002:
+            time.sleep(dt - 0.001)
+
+
+def serve_stream(rate, nreq, nsrc_pool, seed):
+    """Seeded request stream: (arrival_s, metric, npairs, source_key, pool_source, candidate idx)."""
+    import numpy as np
+    rs = np.random.default_rng(seed)
+    t = np.cumsum(rs.exponential(1.0 / rate, nreq))
+    out, used, next_key = [], [], 1
+    for i in range(nreq):
+        metric = 0 if rs.random() < 0.7 else 1
+        npairs = int(rs.integers(1, 17))
+        if used and rs.random() < 0.8:
+            key, ps = used[int(rs.integers(0, len(used)))]
+        else:
+            key, ps = next_key, int(rs.integers(0, nsrc_pool))
+            next_key += 1
+            used.append((key, ps))
+        cand = [int(x) for x in rs.integers(0, len(MULTI_DCT_STEPS), npairs)]
+        out.append((float(t[i]), metric, npairs, key, ps, cand))
+    return out
+
+
+def run_serving(v, stream, pool_frames, res_index, admission, cache):
+    """Drive the serving runtime with the stream; returns (latencies s, wall s, stats)."""
+    import numpy as np
+    srv = v.Server([pool_frames["size"]], v.IN_YUV420P10, admission_bytes=admission, cache_bytes=cache,
+                   max_batch_pairs=256)
+    done = {}
+    stop = threading.Event()
+
+    def poller():
+        while not stop.is_set() or len(done) < len(stream):
+            for rid, status, lat in srv.poll(256, 0.05):
+                done[rid] = (status, lat)
+            if stop.is_set() and len(done) >= len(stream):
+                break
+
+    th = threading.Thread(target=poller)
+    th.start()
+    outs = []
+    t0 = time.perf_counter()
+    for i, (ta, metric, npairs, key, ps, cand) in enumerate(stream):
+        wait_until(t0, ta)
+        src, cands = pool_frames["src"][ps], pool_frames["cands"][ps]
+        out = np.zeros(npairs * (1 if metric == 0 else 3))
+        outs.append(out)
+        srv.submit(i, metric, res_index, key, src, [cands[c] for c in cand], out)
+    srv.drain()
+    wall = time.perf_counter() - t0
+    stop.set()
+    th.join()
+    stats = srv.stats()
+    srv.free()
+    bad = [r for r, (s, _) in done.items() if s != 0]
+    if bad:
+        raise RuntimeError(f"serving: {len(bad)} requests failed")
+    return np.array([done[i][1] for i in range(len(stream))]), wall, stats
+
+
+def run_plain_serving(v, stream, pool_frames):
+    """The same stream through the plain per-pair path: one batch handler per metric, requests in
+    arrival order, one call each (no cache, no cross-request batching)."""
+    import numpy as np
+    import queue as _q
+    import torch
+    w, h = pool_frames["size"]
+    e_s = v.SSIMU2Batch(w, h, 16)
+    e_b = v.ButteraugliBatch(w, h, 16, 2, 203.0)
+    o_s = torch.zeros(16, dtype=torch.float64, device="cuda")
+    o_b = torch.zeros(48, dtype=torch.float64, device="cuda")
+    tables = {}
+    q = _q.Queue()
+    lat = np.zeros(len(stream))
+    stream_ = torch.cuda.current_stream()
+
+    def worker():
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            i, t_sub = item
+            _, metric, npairs, key, ps, cand = stream[i]
+            fr = []
+            for c in cand:
+                fr += [pool_frames["src"][ps], pool_frames["cands"][ps][c]]
+            tb = v.device_frames_table(fr)
+            if metric == 0:
+                e_s.compute_async(tb.data_ptr(), npairs, v.IN_YUV420P10, o_s.data_ptr(), stream_.cuda_stream)
+                o_s[:npairs].cpu()
+            else:
+                e_b.compute_async(tb.data_ptr(), npairs, v.IN_YUV420P10, o_b.data_ptr(), 0, stream_.cuda_stream)
+                o_b[:3 * npairs].cpu()
+            lat[i] = time.perf_counter() - t_sub
+
+    th = threading.Thread(target=worker)
+    th.start()
+    t0 = time.perf_counter()
+    for i, (ta, *_rest) in enumerate(stream):
+        wait_until(t0, ta)
+        q.put((i, time.perf_counter()))
+    q.put(None)
+    th.join()
+    wall = time.perf_counter() - t0
+    e_s.free()
+    e_b.free()
+    return lat, wall
+
+
+def bench_serving(v, args, ws, rank):
+    import numpy as np
+    import torch
+    w, h = parse_size(args.serve_size)
+    nsrc_pool = 8
+    buf, metas, src_res, cand_src, src_frame, cand_frame = make_multi_inputs_one(w, h, nsrc_pool)
+    pool_frames = {"size": (w, h), "src": multi_descs(buf, metas, src_frame),
+                   "cands": [multi_descs(buf, metas, cand_frame[8 * s: 8 * s + 8]) for s in range(nsrc_pool)]}
+    admission, cache = 64 << 30, 16 << 30
+    sys.setswitchinterval(1e-4)
+    # warm-up: builds the pool's blocks, loads kernels
+    run_serving(v, serve_stream(50, 20, nsrc_pool, 99), pool_frames, 0, admission, cache)
+    rows = []
+    for rate in SERVE_RATES:
+        nreq = int(min(max(rate * args.serve_seconds, 40), args.serve_max_requests))
+        stream = serve_stream(rate, nreq, nsrc_pool, 1000 + rate)
+        lat, wall, stats = run_serving(v, stream, pool_frames, 0, admission, cache)
+        pairs = sum(x[2] for x in stream)
+        row = {"offered_req_s": rate, "requests": nreq, "pairs": pairs,
+               "throughput_req_s": nreq / wall, "throughput_pairs_s": pairs / wall,
+               "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+               "cache_hit_rate": stats["cache_hits"] / max(1, stats["cache_hits"] + stats["cache_misses"]),
+               "batches": stats["batches"], "mean_batch_pairs": pairs / max(1, stats["batches"]),
+               "admission_peak_gb": stats["admission_peak_bytes"] / 1e9}
+        if rate <= args.serve_plain_max_rate:
+            plat, pwall = run_plain_serving(v, stream, pool_frames)
+            row["plain"] = {"throughput_req_s": nreq / pwall, "throughput_pairs_s": pairs / pwall,
+                            "p50_ms": float(np.percentile(plat, 50) * 1e3),
+                            "p99_ms": float(np.percentile(plat, 99) * 1e3)}
+        rows.append(row)
+    del buf
+    torch.cuda.empty_cache()
+    return {"workload": f"serving: {w}x{h} YUV420P10, Poisson arrivals, 70% SSIMU2 / 30% Butteraugli, "
+                        f"1-16 pairs per request, source reuse p=0.8 over a pool of {nsrc_pool} sources x 8 "
+                        f"DCT candidates, admission 64 GB (48N / 124N B per pair), source cache 16 GB",
+            "latency": "host submit -> results in the request's host buffer",
+            "plain": "same stream, one request at a time through the per-resolution batch handlers "
+                     "(no cache, no cross-request batching)",
+            "rates": rows}
+
+
+def make_multi_inputs_one(w, h, nsrc):
+    """nsrc sources of one resolution, each with the 8 DCT candidates (make_multi_inputs layout)."""
+    global MULTI_RES
+    saved = MULTI_RES
+    try:
+        MULTI_RES = [(w, h)]
+        return make_multi_inputs("cuda", [nsrc])
+    finally:
+        MULTI_RES = saved
+
+
 def main_ours(args):
     import torch
     ws, rank, local = dist_setup(args)
@@ -695,6 +871,8 @@ def main_ours(args):
         m = bench_multi(v, args, ws, rank)
         out["batched_multi"] = m
         out["gpu_launches"] += m["gpu_launches"]
+    if not args.skip_serving:
+        out["serving"] = bench_serving(v, args, ws, rank)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -757,6 +935,11 @@ def main():
     ap.add_argument("--skip-butter", action="store_true")
     ap.add_argument("--skip-ssimu2", action="store_true")
     ap.add_argument("--skip-multi", action="store_true")
+    ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--serve-size", default=f"{W4K}x{H4K}")
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-max-requests", type=int, default=400)
+    ap.add_argument("--serve-plain-max-rate", type=float, default=2000)
     ap.add_argument("--multi-scale", type=float, default=1.0, help="fraction of the 64 sources (small runs)")
     ap.add_argument("--ssimu2-size", default=f"{W1080}x{H1080}")
     ap.add_argument("--butter-size", default=f"{W4K}x{H4K}")

@@ -305,6 +305,59 @@ EXPORTPREPROCESS int Vship_MultiKnobs(Vship_MultiHandler handler, char* out_json
 EXPORTPREPROCESS uint64_t Vship_MultiDeviceBytes(int nres, const int* widths, const int* heights,
                                                  const int* max_sources, const int* max_pairs, int flags);
 
+/* Serving runtime -- no counterpart in the reference (whose front-ends score frames in order).
+ *
+ * A server owns one GPU stream. Requests (one source frame scored against 1..max_batch_pairs
+ * candidates, by SSIMULACRA2 or Butteraugli, at one of the resolutions given at creation) are
+ * queued by Vship_ServeSubmit and return at once. A scheduler thread gathers queued requests
+ * into batches in arrival order whenever fewer than two batches are on the GPU, admitting a
+ * request only while the charges of the requests on the GPU stay within admission_bytes
+ * (48 x width x height bytes per SSIMULACRA2 pair, 124 x width x height per Butteraugli pair).
+ * Per-source device state (the SSIMULACRA2 XYB pyramid, the Butteraugli opsin and frequency
+ * planes) is kept in an LRU cache of cache_bytes keyed by (metric, resolution, source_key), so
+ * a source that comes back skips its own stage; source_key 0 is never cached. Results go to the
+ * request's host buffer `results` (npairs scores, or 3 doubles per pair {Qnorm, 3-norm,
+ * inf-norm}) before Vship_ServePoll reports the request with its latency (submit to results).
+ * Frames (device planes of input_type) and `results` must stay valid until then; the candidate
+ * descriptor array is copied at submit. flags: Vship_ServeFp32Candidates keeps SSIMULACRA2
+ * candidate pyramids in FP32 (default: FP16 differences from the source's). */
+typedef struct {
+    int id;
+} Vship_ServeHandler;
+typedef enum { Vship_ServeSSIMU2 = 0, Vship_ServeButteraugli = 1 } Vship_ServeMetric;
+#define Vship_ServeFp32Candidates 1
+typedef struct {
+    uint64_t request_id;
+    int metric;      /* Vship_ServeMetric */
+    int resolution;  /* index into the creation's widths / heights */
+    uint64_t source_key;
+    Vship_DeviceFrame source;
+    int npairs;
+    const Vship_DeviceFrame* candidates; /* host array of npairs descriptors */
+    double* results;                     /* host */
+} Vship_ServeRequest;
+typedef struct {
+    uint64_t request_id;
+    int status; /* Vship_Exception */
+    double latency_seconds;
+} Vship_ServeCompletion;
+EXPORTPREPROCESS Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, int nres, const int* widths,
+                                                   const int* heights, Vship_InputType input_type,
+                                                   uint64_t admission_bytes, uint64_t cache_bytes,
+                                                   int max_batch_pairs, int flags, int Qnorm,
+                                                   float intensity_multiplier);
+/* Vship_OutOfVRAM: the request's charge alone exceeds admission_bytes. */
+EXPORTPREPROCESS Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* request);
+/* Up to max completions, waiting up to timeout_seconds for the first; returns how many. */
+EXPORTPREPROCESS int Vship_ServePoll(Vship_ServeHandler handler, Vship_ServeCompletion* out, int max,
+                                     double timeout_seconds);
+/* Blocks until every submitted request has completed. */
+EXPORTPREPROCESS Vship_Exception Vship_ServeDrain(Vship_ServeHandler handler);
+/* Counters as JSON (same size/truncation contract as Vship_GetErrorMessage). */
+EXPORTPREPROCESS int Vship_ServeStats(Vship_ServeHandler handler, char* out_json, int len);
+/* Drains, stops the threads and frees everything. */
+EXPORTPREPROCESS Vship_Exception Vship_ServeDestroy(Vship_ServeHandler handler);
+
 /* Instrumentation: when enabled, every kernel launch is bracketed by CUDA events on its stream.
  * Vship_ProfileReport synchronises those events and writes a JSON object
  * {"kernel": [launches, total_ms], ...} (same size/truncation contract as

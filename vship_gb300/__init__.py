@@ -65,6 +65,17 @@ _H = Handler
 _E = ctypes.c_int
 _IP = ctypes.POINTER(ctypes.c_int)
 
+
+class ServeRequest(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("metric", ctypes.c_int), ("resolution", ctypes.c_int),
+                ("source_key", ctypes.c_uint64), ("source", DeviceFrame), ("npairs", ctypes.c_int),
+                ("candidates", ctypes.POINTER(DeviceFrame)), ("results", ctypes.POINTER(ctypes.c_double))]
+
+
+class ServeCompletion(ctypes.Structure):
+    _fields_ = [("request_id", ctypes.c_uint64), ("status", ctypes.c_int), ("latency_seconds", ctypes.c_double)]
+
+
 SIGNATURES = {
     "Vship_GetVersion": (Version, []),
     "Vship_GetDeviceCount": (_E, [ctypes.POINTER(ctypes.c_int)]),
@@ -121,6 +132,13 @@ SIGNATURES = {
                                            ctypes.c_void_p, ctypes.c_void_p]),
     "Vship_MultiKnobs": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
     "Vship_MultiDeviceBytes": (ctypes.c_uint64, [ctypes.c_int, _IP, _IP, _IP, _IP, ctypes.c_int]),
+    "Vship_ServeCreate": (_E, [ctypes.POINTER(_H), ctypes.c_int, _IP, _IP, ctypes.c_int, ctypes.c_uint64,
+                               ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+    "Vship_ServeSubmit": (_E, [_H, ctypes.POINTER(ServeRequest)]),
+    "Vship_ServePoll": (ctypes.c_int, [_H, ctypes.POINTER(ServeCompletion), ctypes.c_int, ctypes.c_double]),
+    "Vship_ServeDrain": (_E, [_H]),
+    "Vship_ServeStats": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
+    "Vship_ServeDestroy": (_E, [_H]),
     "Vship_ProfileSetEnabled": (None, [ctypes.c_int]),
     "Vship_ProfileReport": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }
@@ -451,6 +469,76 @@ class MultiScorer:
         if self._h is not None:
             _check(lib().Vship_MultiFree(self._h), "Vship_MultiFree")
             self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+SERVE_SSIMU2, SERVE_BUTTERAUGLI = 0, 1
+SERVE_FP32_CANDIDATES = 1
+
+
+class Server:
+    """Serving runtime (Vship_ServeCreate / Submit / Poll). ``resolutions`` is a list of
+    (width, height). Results land in numpy float64 arrays the caller passes to submit (kept
+    referenced here until their completion is polled)."""
+
+    def __init__(self, resolutions, input_type=4, admission_bytes=64 << 30, cache_bytes=16 << 30,
+                 max_batch_pairs=256, flags=0, qnorm=2, intensity_multiplier=203.0):
+        self.resolutions = [(int(w), int(h)) for w, h in resolutions]
+        self._h = Handler()
+        self._live = {}
+        _check(lib().Vship_ServeCreate(ctypes.byref(self._h), len(self.resolutions),
+                                       _ints([w for w, _ in self.resolutions]), _ints([h for _, h in self.resolutions]),
+                                       int(input_type), int(admission_bytes), int(cache_bytes), int(max_batch_pairs),
+                                       int(flags), int(qnorm), ctypes.c_float(intensity_multiplier)),
+               "Vship_ServeCreate")
+
+    def submit(self, request_id, metric, resolution, source_key, source, candidates, out):
+        """source / candidates: (planes, stride_bytes[, chroma_stride_bytes]) of device pointers;
+        out: C-contiguous float64 numpy array of npairs (SSIMU2) or 3*npairs (Butteraugli)."""
+        import numpy as np
+        assert out.dtype == np.float64 and out.flags["C_CONTIGUOUS"]
+        src = _frames([source])
+        cands = _frames(candidates)
+        q = ServeRequest(int(request_id), int(metric), int(resolution), int(source_key), src[0], len(candidates),
+                         ctypes.cast(cands, ctypes.POINTER(DeviceFrame)),
+                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        self._live[int(request_id)] = out
+        rc = lib().Vship_ServeSubmit(self._h, ctypes.byref(q))
+        if rc:
+            self._live.pop(int(request_id), None)
+            _check(rc, "Vship_ServeSubmit")
+
+    def poll(self, max_n=256, timeout=0.0):
+        """[(request_id, status, latency_seconds), ...] of requests completed since the last poll."""
+        buf = (ServeCompletion * max_n)()
+        n = lib().Vship_ServePoll(self._h, buf, max_n, float(timeout))
+        out = []
+        for i in range(n):
+            rid = int(buf[i].request_id)
+            self._live.pop(rid, None)
+            out.append((rid, int(buf[i].status), float(buf[i].latency_seconds)))
+        return out
+
+    def drain(self):
+        _check(lib().Vship_ServeDrain(self._h), "Vship_ServeDrain")
+
+    def stats(self) -> dict:
+        import json
+        n = lib().Vship_ServeStats(self._h, None, 0)
+        buf = ctypes.create_string_buffer(n)
+        lib().Vship_ServeStats(self._h, buf, n)
+        return json.loads(buf.value.decode())
+
+    def free(self):
+        if self._h is not None:
+            _check(lib().Vship_ServeDestroy(self._h), "Vship_ServeDestroy")
+            self._h = None
+            self._live.clear()
 
     def __del__(self):
         try:

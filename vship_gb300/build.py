@@ -23,7 +23,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
     "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
 ]
-SOURCES = ["ssimu2.cu", "butter.cu", "api.cu", "profile.cu", "noalloc.cu", "multi.cu"]
+SOURCES = ["ssimu2.cu", "butter.cu", "api.cu", "profile.cu", "noalloc.cu", "multi.cu", "serve.cu"]
 CLI = os.path.join(HERE, "ffvship")
 
 

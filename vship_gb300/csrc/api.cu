@@ -15,6 +15,7 @@
 #include "common.cuh"
 #include "ssimu2.h"
 #include "multi.h"
+#include "serve.h"
 #include "profile.h"
 
 #include <cuda_runtime.h>
@@ -229,6 +230,12 @@ struct MultiHandle {
     }
 };
 HandleTable<MultiHandle> g_multi;
+
+struct ServeHandle {
+    Server srv;
+    ~ServeHandle() { srv.destroy(); }
+};
+HandleTable<ServeHandle> g_serve;
 
 // Device guard: make the handler's device current for the duration of a call.
 struct DeviceGuard {
@@ -660,6 +667,75 @@ uint64_t Vship_MultiDeviceBytes(int nres, const int* widths, const int* heights,
                                 const int* max_pairs, int flags) {
     if (nres <= 0 || nres > kMaxRes || !widths || !heights || !max_sources || !max_pairs) return 0;
     return (uint64_t)MultiEngine::device_bytes(nres, widths, heights, max_sources, max_pairs, flags);
+}
+
+// ----- serving runtime ---------------------------------------------------------------------
+
+Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, int nres, const int* widths, const int* heights,
+                                  Vship_InputType input_type, uint64_t admission_bytes, uint64_t cache_bytes,
+                                  int max_batch_pairs, int flags, int Qnorm, float intensity_multiplier) {
+    if (!handler) return Vship_BadPointer;
+    int c = 0;
+    int rc = check_gpu_count(&c);
+    if (rc) return to_exc(rc);
+    std::unique_ptr<ServeHandle> h(new ServeHandle());
+    rc = h->srv.create(nres, widths, heights, (int)input_type, admission_bytes, cache_bytes, max_batch_pairs, flags,
+                       Qnorm, intensity_multiplier);
+    if (rc) return to_exc(rc);
+    handler->id = g_serve.put(std::move(h));
+    return Vship_NoError;
+}
+
+Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* q) {
+    ServeHandle* h = g_serve.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    if (!q || !q->candidates || q->npairs <= 0 || !q->results) return Vship_BadPointer;
+    ServeReq* r = new ServeReq();
+    r->id = q->request_id;
+    r->metric = q->metric;
+    r->res = q->resolution;
+    r->key = q->source_key;
+    std::memcpy(&r->src, &q->source, sizeof(FrameDesc));
+    r->cands.resize(q->npairs);
+    std::memcpy(r->cands.data(), q->candidates, sizeof(FrameDesc) * q->npairs);
+    r->out = q->results;
+    return to_exc(h->srv.submit(r));
+}
+
+int Vship_ServePoll(Vship_ServeHandler handler, Vship_ServeCompletion* out, int max, double timeout_seconds) {
+    ServeHandle* h = g_serve.get(handler.id);
+    if (!h || !out || max <= 0) return 0;
+    std::vector<ServeDone> d(max);
+    const int n = h->srv.poll(d.data(), max, timeout_seconds);
+    for (int i = 0; i < n; i++) {
+        out[i].request_id = d[i].id;
+        out[i].status = d[i].status;
+        out[i].latency_seconds = d[i].latency;
+    }
+    return n;
+}
+
+Vship_Exception Vship_ServeDrain(Vship_ServeHandler handler) {
+    ServeHandle* h = g_serve.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    return to_exc(h->srv.drain());
+}
+
+int Vship_ServeStats(Vship_ServeHandler handler, char* out_json, int len) {
+    ServeHandle* h = g_serve.get(handler.id);
+    const std::string s = h ? h->srv.stats_json() : std::string("{}");
+    const int need = (int)s.size() + 1;
+    if (len <= 0 || !out_json) return need;
+    const int ncopy = std::min(len - 1, need - 1);
+    std::memcpy(out_json, s.data(), ncopy);
+    out_json[ncopy] = '\0';
+    return need;
+}
+
+Vship_Exception Vship_ServeDestroy(Vship_ServeHandler handler) {
+    std::unique_ptr<ServeHandle> h = g_serve.take(handler.id);
+    if (!h) return Vship_BadHandler;
+    return Vship_NoError;
 }
 
 }  // extern "C"

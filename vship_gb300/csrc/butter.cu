@@ -26,6 +26,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 namespace vship {
 
@@ -98,8 +99,9 @@ struct BGeom {
     int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x8) at full scale
 };
 
-__device__ __forceinline__ float* iplane(float* work, const BGeom& g, const BScaleDev& S, int img, int id) {
-    return work + (int64_t)img * g.img_floats + S.base + (int64_t)id * S.n;
+// ib[img] = that image's workspace (both scales); the launch's image list indexes it
+__device__ __forceinline__ float* iplane(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id) {
+    return ib[img] + S.base + (int64_t)id * S.n;
 }
 // Select a scale with constant indices only, so the parameter struct is never copied to the
 // stack for a dynamic index.
@@ -110,7 +112,7 @@ __device__ __forceinline__ BScaleDev pick_scale(const BGeom& g, int s) { return 
 // grid (ceil(w/32), ceil(h/32), nimages), 256 threads; frames[image].
 template <int IT>
 __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __restrict__ frames,
-                                                            float* __restrict__ work, BGeom g) {
+                                                            float* const* __restrict__ ib, BGeom g) {
     __shared__ float sm[3][32][33];
     const int img = blockIdx.z;
     const FrameDesc fd = frames[img];
@@ -126,7 +128,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 v[c] = to_linear_fast(v[c]);
-                iplane(work, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
+                iplane(ib, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
             }
         }
 #pragma unroll
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
             s += sm[c][y1][x0];
             s += sm[c][y0][x1];
             s += sm[c][y1][x1];
-            iplane(work, g, Hs, img, I_LIN + c)[(int64_t)gy * Hs.p + gx] = s * 0.25f;
+            iplane(ib, g, Hs, img, I_LIN + c)[(int64_t)gy * Hs.p + gx] = s * 0.25f;
         }
     }
 }
@@ -240,7 +242,7 @@ __device__ __forceinline__ float b_gamma(float v) {
 }
 
 // grid (ceil(w/32), ceil(h/48), nimages); the three channels' tiles are double-buffered.
-__global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict__ work, BGeom g, int s,
+__global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* const* __restrict__ ib, BGeom g, int s,
                                                               float intensity) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
@@ -251,13 +253,13 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
     tile_masses_r8<0>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float src[3][6], blr[3][6];
-    tile_stage_r8(sm, iplane(work, g, S, img, I_LIN), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(ib, g, S, img, I_LIN), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         float* in = sm + (c & 1) * TB_RAW;
         if (c < 2) {
-            tile_stage_r8(sm + ((c + 1) & 1) * TB_RAW, iplane(work, g, S, img, I_LIN + c + 1), S.p, S.w, S.h, x0,
+            tile_stage_r8(sm + ((c + 1) & 1) * TB_RAW, iplane(ib, g, S, img, I_LIN + c + 1), S.p, S.w, S.h, x0,
                           y0);
             cp_async_commit();
             cp_async_wait<1>();
@@ -270,9 +272,9 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
         for (int o = 0; o < 6; o++) src[c][o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
     }
-    float* ox = iplane(work, g, S, img, I_XYB + 0);
-    float* oy = iplane(work, g, S, img, I_XYB + 1);
-    float* oz = iplane(work, g, S, img, I_XYB + 2);
+    float* ox = iplane(ib, g, S, img, I_XYB + 0);
+    float* oy = iplane(ib, g, S, img, I_XYB + 1);
+    float* oz = iplane(ib, g, S, img, I_XYB + 2);
 #pragma unroll
     for (int o = 0; o < 6; o++) {
         const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -310,7 +312,7 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* __restrict_
 constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180;
 
 template <int KI, int R>
-__global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ work, BGeom g, int s, int src_id,
+__global__ void __launch_bounds__(256) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s, int src_id,
                                                            int dst_id) {
     __shared__ __align__(16) float in[HB_TH * HB_P];
     constexpr int RA = (R + 3) & ~3;
@@ -320,8 +322,8 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ w
     static_assert(IW <= HB_P && 120 + 4 * NV4 <= HB_P, "hblur tile");
     const int img = blockIdx.z / 3, pl = blockIdx.z % 3;
     const BScaleDev S = pick_scale(g, s);
-    const float* src = iplane(work, g, S, img, src_id + pl);
-    float* dst = iplane(work, g, S, img, dst_id + pl);
+    const float* src = iplane(ib, g, S, img, src_id + pl);
+    float* dst = iplane(ib, g, S, img, dst_id + pl);
     const int x0 = blockIdx.x * HB_TW, y0 = blockIdx.y * HB_TH;
     stage_rows<256>(in, HB_P, src, S.p, S.w, S.h, x0 - RA, y0, HB_TH, IW / 4);
     cp_async_commit();
@@ -362,18 +364,18 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* __restrict__ w
 constexpr int VB_TW = 32, VB_TH = 64;
 
 template <int KI, int R>
-__device__ __forceinline__ void vblur3(float* in, float* ctr, float* __restrict__ work, const BGeom& g, int img,
+__device__ __forceinline__ void vblur3(float* in, float* ctr, float* const* __restrict__ ib, const BGeom& g, int img,
                                        int s, int src_id, int ctr_id, int nctr, float out[3][8]) {
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * VB_TW, y0 = blockIdx.y * VB_TH;
     constexpr int IH = VB_TH + 2 * R;
 #pragma unroll
     for (int c = 0; c < 3; c++)
-        stage_rows<256>(in + c * IH * VB_TW, VB_TW, iplane(work, g, S, img, src_id + c), S.p, S.w, S.h, x0, y0 - R,
+        stage_rows<256>(in + c * IH * VB_TW, VB_TW, iplane(ib, g, S, img, src_id + c), S.p, S.w, S.h, x0, y0 - R,
                         IH, VB_TW / 4);
     // the epilogue's own-pixel planes, staged with the blur input so their latency overlaps
     for (int c = 0; c < nctr; c++)
-        stage_rows<256>(ctr + c * VB_TH * VB_TW, VB_TW, iplane(work, g, S, img, ctr_id + c), S.p, S.w, S.h, x0, y0,
+        stage_rows<256>(ctr + c * VB_TH * VB_TW, VB_TW, iplane(ib, g, S, img, ctr_id + c), S.p, S.w, S.h, x0, y0,
                         VB_TH, VB_TW / 4);
     cp_async_commit();
     cp_async_wait<0>();
@@ -400,12 +402,12 @@ __device__ __forceinline__ void vblur3(float* in, float* ctr, float* __restrict_
 
 // LF vertical pass: D = XYB - LF (in place over XYB) and LF vals (separatefrequencies.hpp:3-12)
 constexpr int kVLfSmem = (3 * (VB_TH + 42) * VB_TW + 3 * VB_TH * VB_TW) * 4;
-__global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ work, BGeom g, int s) {
+__global__ void __launch_bounds__(256) butter_lf_v_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* ctr = sm + 3 * (VB_TH + 42) * VB_TW;
     const int img = blockIdx.z;
     float lf[3][8];
-    vblur3<4, 21>(sm, ctr, work, g, img, s, I_TMP, I_XYB, 3, lf);
+    vblur3<4, 21>(sm, ctr, ib, g, img, s, I_TMP, I_XYB, 3, lf);
     const BScaleDev S = pick_scale(g, s);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     const int x = blockIdx.x * VB_TW + vc;
@@ -415,8 +417,8 @@ __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* __restrict__ wo
     float* lfv[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
-        xyb[c] = iplane(work, g, S, img, I_XYB + c);
-        lfv[c] = iplane(work, g, S, img, I_LFV + c);
+        xyb[c] = iplane(ib, g, S, img, I_XYB + c);
+        lfv[c] = iplane(ib, g, S, img, I_LFV + c);
     }
 #pragma unroll
     for (int o = 0; o < 8; o++) {
@@ -456,22 +458,22 @@ __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
 // MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
 // written over the D planes (separatefrequencies.hpp:37-99,160-187).
 constexpr int kVMfSmem = (3 * (VB_TH + 18) * VB_TW + 2 * VB_TH * VB_TW) * 4;
-__global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ work, BGeom g, int s) {
+__global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* ctr = sm + 3 * (VB_TH + 18) * VB_TW;
     const int img = blockIdx.z;
     float mf[3][8];
-    vblur3<3, 9>(sm, ctr, work, g, img, s, I_TMP, I_XYB, 2, mf);
+    vblur3<3, 9>(sm, ctr, ib, g, img, s, I_TMP, I_XYB, 2, mf);
     const BScaleDev S = pick_scale(g, s);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     const int x = blockIdx.x * VB_TW + vc;
     const int yb = blockIdx.y * VB_TH + 8 * vg;
     if (x >= S.w) return;
-    float* d0 = iplane(work, g, S, img, I_XYB + 0);
-    float* d1 = iplane(work, g, S, img, I_XYB + 1);
-    float* m0 = iplane(work, g, S, img, I_MF + 0);
-    float* m1 = iplane(work, g, S, img, I_MF + 1);
-    float* m2 = iplane(work, g, S, img, I_MF + 2);
+    float* d0 = iplane(ib, g, S, img, I_XYB + 0);
+    float* d1 = iplane(ib, g, S, img, I_XYB + 1);
+    float* m0 = iplane(ib, g, S, img, I_MF + 0);
+    float* m1 = iplane(ib, g, S, img, I_MF + 1);
+    float* m2 = iplane(ib, g, S, img, I_MF + 2);
     const float sx = 0.653020556257f, yw = 46.0f;
 #pragma unroll
     for (int o = 0; o < 8; o++) {
@@ -492,7 +494,7 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* __restrict__ wo
 }
 
 // HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), nimages)
-__global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ work, BGeom g, int s) {
+__global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
     const int img = blockIdx.z;
@@ -501,8 +503,8 @@ __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ w
     float rxy[6];
     tile_masses_r8<1>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    tile_stage_r8(sm, iplane(work, g, S, img, I_XYB), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, iplane(work, g, S, img, I_XYB + 1), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(ib, g, S, img, I_XYB), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, img, I_XYB + 1), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -514,8 +516,8 @@ __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* __restrict__ w
 #pragma unroll
         for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
-        float* hfp = iplane(work, g, S, img, I_HF + c);
-        float* uhfp = iplane(work, g, S, img, I_UHF + c);
+        float* hfp = iplane(ib, g, S, img, I_HF + c);
+        float* uhfp = iplane(ib, g, S, img, I_UHF + c);
 #pragma unroll
         for (int o = 0; o < 6; o++) {
             const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -653,7 +655,7 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 constexpr int DF_RAW = DF_IH * DF_IW;
 constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW) * 4;
 
-__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__ work, const int2* __restrict__ pimg,
+__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
                                                              BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* Dt = sm + 4 * DF_RAW;
@@ -670,9 +672,9 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
     }
     // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X
     auto plane_id = [](int m) { return (m < 2 ? I_UHF : m < 4 ? I_HF : I_MF) + 1 - (m & 1); };
-    stage_rows<256>(sm, DF_IW, iplane(work, g, S, i0, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+    stage_rows<256>(sm, DF_IW, iplane(ib, g, S, i0, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
                     DF_IW / 4);
-    stage_rows<256>(sm + DF_RAW, DF_IW, iplane(work, g, S, i1, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
+    stage_rows<256>(sm + DF_RAW, DF_IW, iplane(ib, g, S, i1, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
                     DF_IH, DF_IW / 4);
     cp_async_commit();
 #pragma unroll 1
@@ -682,9 +684,9 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
         if (m < 5) {
             float* n0 = sm + ((m + 1) & 1) * 2 * DF_RAW;
             const int id = plane_id(m + 1);
-            stage_rows<256>(n0, DF_IW, iplane(work, g, S, i0, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+            stage_rows<256>(n0, DF_IW, iplane(ib, g, S, i0, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
                             DF_IW / 4);
-            stage_rows<256>(n0 + DF_RAW, DF_IW, iplane(work, g, S, i1, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
+            stage_rows<256>(n0 + DF_RAW, DF_IW, iplane(ib, g, S, i1, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
                             DF_IH, DF_IW / 4);
             cp_async_commit();
             cp_async_wait<1>();
@@ -730,13 +732,13 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
                 const int im = m ? i1 : i0;
 #pragma unroll
                 for (int c = 0; c < 2; c++) {
-                    hf[m][c] = __ldg(iplane(work, g, S, im, I_HF + c) + i);
-                    uhf[m][c] = __ldg(iplane(work, g, S, im, I_UHF + c) + i);
+                    hf[m][c] = __ldg(iplane(ib, g, S, im, I_HF + c) + i);
+                    uhf[m][c] = __ldg(iplane(ib, g, S, im, I_UHF + c) + i);
                 }
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    mf[m][c] = __ldg(iplane(work, g, S, im, I_MF + c) + i);
-                    lf[m][c] = __ldg(iplane(work, g, S, im, I_LFV + c) + i);
+                    mf[m][c] = __ldg(iplane(ib, g, S, im, I_MF + c) + i);
+                    lf[m][c] = __ldg(iplane(ib, g, S, im, I_LFV + c) + i);
                 }
             }
 #pragma unroll
@@ -761,8 +763,8 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
                 const float dl = lf[0][c] - lf[1][c];
                 dc[c] += P.wlf[c] * dl * dl;
             }
-            iplane(work, g, S, i1, Q_SAC)[i] = ac[0] + ac[1] + ac[2];
-            iplane(work, g, S, i1, Q_SDC)[i] = dc[0] + dc[1] + dc[2];
+            iplane(ib, g, S, i1, Q_SAC)[i] = ac[0] + ac[1] + ac[2];
+            iplane(ib, g, S, i1, Q_SDC)[i] = dc[0] + dc[1] + dc[2];
             // maskinit + diffPrecompute (maskPsycho.hpp:3-40). sqrt(m + b) - sqrt(b) is evaluated
             // as m / (sqrt(m + b) + sqrt(b)): the same value without the cancellation.
 #pragma unroll
@@ -770,7 +772,7 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
                 const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
                 const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
                 const float mk = mul * sqrtf(xd * xd + yd * yd);
-                iplane(work, g, S, i1, Q_PRE0 + m)[i] = mk / (sqrtf(mk + bias) + sqb);
+                iplane(ib, g, S, i1, Q_PRE0 + m)[i] = mk / (sqrtf(mk + bias) + sqb);
             }
         }
     }
@@ -778,7 +780,7 @@ __global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* __restrict__
 
 // Blur both mask planes (sigma 2.7); store B0 and add 10*(B0-B1)^2 to the AC sum.
 // grid (ceil(w/32), ceil(h/48), npairs)
-__global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restrict__ work,
+__global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* const* __restrict__ ib,
                                                                   const int2* __restrict__ pimg, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
@@ -787,8 +789,8 @@ __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restr
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
     float rxy[6];
     tile_masses_r8<2>(x0, y0, S.w, S.h, rxy);
-    tile_stage_r8(sm, iplane(work, g, S, i1, Q_PRE0), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, iplane(work, g, S, i1, Q_PRE1), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(ib, g, S, i1, Q_PRE0), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, i1, Q_PRE1), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -799,8 +801,8 @@ __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* __restr
         __syncthreads();
     }
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    float* b0 = iplane(work, g, S, i1, Q_B0);
-    float* sac = iplane(work, g, S, i1, Q_SAC);
+    float* b0 = iplane(ib, g, S, i1, Q_B0);
+    float* sac = iplane(ib, g, S, i1, Q_SAC);
 #pragma unroll
     for (int o = 0; o < 6; o++) {
         const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -851,7 +853,7 @@ __device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float&
 // (when distmap is not null) and emits norm partials. grid (ceil(w/32), ceil(h/8), npairs),
 // block (32, 8).
 template <bool FINAL>
-__global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__ work, const int2* __restrict__ pimg,
+__global__ void __launch_bounds__(256) butter_diffmap_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
                                                              BGeom g, int s, float* __restrict__ distmap,
                                                              float* __restrict__ partials, float qnorm) {
     const int pair = blockIdx.z;
@@ -860,7 +862,7 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__
     const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
     float sq = 0.f, s3 = 0.f, mx = 0.f;
     if (x < S.w && y < S.h) {
-        const float* b0 = iplane(work, g, S, i1, Q_B0);
+        const float* b0 = iplane(ib, g, S, i1, Q_B0);
         const int k = 3;
         const int W = S.w, H = S.h, p = S.p;
         float m0 = b0[(int64_t)y * p + x], m1 = 2.0f * m0, m2 = m1;
@@ -878,14 +880,14 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* __restrict__
         if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x], m0, m1, m2);
         const float mask = 0.45f * m0 + 0.3f * m1 + 0.25f * m2;
         const int64_t i = (int64_t)y * p + x;
-        float d = sqrtf(mask_y(mask) * iplane(work, g, S, i1, Q_SAC)[i] +
-                        mask_dc_y(mask) * iplane(work, g, S, i1, Q_SDC)[i]);
+        float d = sqrtf(mask_y(mask) * iplane(ib, g, S, i1, Q_SAC)[i] +
+                        mask_dc_y(mask) * iplane(ib, g, S, i1, Q_SDC)[i]);
         if (!FINAL) {
-            iplane(work, g, S, i1, Q_DIFF)[i] = d;
+            iplane(ib, g, S, i1, Q_DIFF)[i] = d;
         } else {
             constexpr DConst k085 = dconst(1.0 - 0.3 * (double)0.5f);
             const BScaleDev Hs = g.s[1];
-            const float small = iplane(work, g, Hs, i1, Q_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
+            const float small = iplane(ib, g, Hs, i1, Q_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
             d = fmaf(0.5f, small, mul_dc(d, k085));
             if (distmap) distmap[(int64_t)pair * W * H + (int64_t)y * W + x] = d;
             sq = powf(d, qnorm);
@@ -1030,6 +1032,20 @@ __global__ void butter_identity_pairs_kernel(int2* pimg, int n) {
     if (i < n) pimg[i] = make_int2(2 * i, 2 * i + 1);
 }
 
+int butter_prepare_device() {
+    int rc = upload_butter_tables();
+    if (rc) return rc;
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
+    const DiffParams P = make_diff_params();
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
+    return E_OK;
+}
+
+size_t butter_image_floats(int64_t w, int64_t h) { return (size_t)make_bgeom(w, h).img_floats; }
+int butter_norm_tiles(int64_t w, int64_t h) { return make_bgeom(w, h).norm_tiles; }
+
 int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensity_, int max_pairs_) {
     int rc = init_images(width, height, qnorm_, intensity_, 2 * max_pairs_, max_pairs_, true);
     if (rc) return rc;
@@ -1057,19 +1073,16 @@ int ButterEngine::init_images(int64_t width, int64_t height, int qnorm_, float i
     }
     img_floats = g.img_floats;
     norm_blocks = g.norm_tiles;
-    int rc = upload_butter_tables();
+    int rc = butter_prepare_device();
     if (rc) return rc;
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
-    {
-        const DiffParams P = make_diff_params();
-        VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
-    }
     VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * img_floats * max_images));
     VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
     if (keep_distmap) VSHIP_CUDA_TRY(cudaMalloc(&distmap, sizeof(float) * (size_t)w * h * max_pairs));
     VSHIP_CUDA_TRY(cudaMalloc(&norms, sizeof(double) * 3 * max_pairs));
+    std::vector<float*> bases(max_images);
+    for (int i = 0; i < max_images; i++) bases[i] = work + (size_t)i * img_floats;
+    VSHIP_CUDA_TRY(cudaMalloc(&ibase, sizeof(float*) * max_images));
+    VSHIP_CUDA_TRY(cudaMemcpy(ibase, bases.data(), sizeof(float*) * max_images, cudaMemcpyHostToDevice));
     return E_OK;
 }
 
@@ -1079,11 +1092,13 @@ void ButterEngine::destroy() {
     if (distmap) cudaFree(distmap);
     if (norms) cudaFree(norms);
     if (pimg_identity) cudaFree(pimg_identity);
+    if (ibase) cudaFree(ibase);
     work = nullptr;
     partials = nullptr;
     distmap = nullptr;
     norms = nullptr;
     pimg_identity = nullptr;
+    ibase = nullptr;
 }
 
 size_t ButterEngine::image_bytes(int64_t w, int64_t h) { return sizeof(float) * (size_t)make_bgeom(w, h).img_floats; }
@@ -1091,7 +1106,7 @@ size_t ButterEngine::image_bytes(int64_t w, int64_t h) { return sizeof(float) * 
 size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs) {
     BGeom g = make_bgeom(w, h);
     return (sizeof(float) * 2 * (size_t)g.img_floats + sizeof(float) * 3 * (size_t)g.norm_tiles +
-            sizeof(float) * (size_t)w * h + sizeof(double) * 3 + sizeof(int2)) *
+            sizeof(float) * (size_t)w * h + sizeof(double) * 3 + sizeof(int2) + 2 * sizeof(float*)) *
            pairs;
 }
 
@@ -1103,41 +1118,51 @@ int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
 int ButterEngine::launch_images(const FrameDesc* frames_dev, int nimages, const int2* pimg, int npairs, int intype,
                                 double* norms_out, float* distmap_out, cudaStream_t st) {
     if (nimages <= 0 || nimages > max_images || npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
+    return butter_enqueue(w, h, qnorm, intensity, ibase, frames_dev, nimages, pimg, npairs, intype, partials,
+                          norms_out ? norms_out : norms, distmap_out, st);
+}
+
+int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
+                   int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
+                   float* distmap_out, cudaStream_t st) {
+    if (npairs <= 0 || nstage < 0) return E_BAD_POINTER;
     const BGeom g = make_bgeom(w, h);
-    const unsigned ni = (unsigned)nimages, np = (unsigned)npairs;
-    {
+    const unsigned ni = (unsigned)nstage, np = (unsigned)npairs;
+    if (ni) {
         dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), ni);
         ProfScope ps_("butter_decode", st);
         switch (intype) {
-            case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
-            case IN_UINT16: butter_decode_kernel<IN_UINT16><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
-            case IN_HALF: butter_decode_kernel<IN_HALF><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
-            case IN_YUV420P10: butter_decode_kernel<IN_YUV420P10><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
-            default: butter_decode_kernel<IN_FLOAT><<<gr, 256, 0, st>>>(frames_dev, work, g); break;
+            case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
+            case IN_UINT16: butter_decode_kernel<IN_UINT16><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
+            case IN_HALF: butter_decode_kernel<IN_HALF><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
+            case IN_YUV420P10: butter_decode_kernel<IN_YUV420P10><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
+            default: butter_decode_kernel<IN_FLOAT><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
         }
     }
     for (int s = 1; s >= 0; s--) {
         const int64_t sw = g.s[s].w, sh = g.s[s].h;
-        const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), ni);
-        const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 3 * ni);
-        const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), ni);
-        { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s, intensity); }
-        { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(work, g, s, I_XYB, I_TMP); }
-        { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(work, g, s); }
-        { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(work, g, s, I_XYB, I_TMP); }
-        { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(work, g, s); }
-        { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(work, g, s); }
+        if (ni) {
+            const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), ni);
+            const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 3 * ni);
+            const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), ni);
+            { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s, intensity); }
+            { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
+            { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(ib, g, s); }
+            { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
+            { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(ib, g, s); }
+            { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s); }
+        }
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
-        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(work, pimg, g, s); }
+        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s); }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
-        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(work, pimg, g, s); }
+        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(ib, pimg, g, s); }
         const dim3 gf((unsigned)ceil_div(sw, 32), (unsigned)ceil_div(sh, 8), np);
         if (s == 1)
-            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, dim3(32, 8), 0, st>>>(work, pimg, g, s, nullptr, partials, (float)qnorm); }
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, dim3(32, 8), 0, st>>>(ib, pimg, g, s, nullptr, partials, (float)qnorm); }
         else
-            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, dim3(32, 8), 0, st>>>(work, pimg, g, s, distmap_out, partials, (float)qnorm); }
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, dim3(32, 8), 0, st>>>(ib, pimg, g, s, distmap_out, partials, (float)qnorm); }
     }
-    { ProfScope ps_("butter_finalize", st); butter_finalize_kernel<<<np, 256, 0, st>>>(partials, norms_out ? norms_out : norms, g, qnorm); }
+    { ProfScope ps_("butter_finalize", st); butter_finalize_kernel<<<np, 256, 0, st>>>(partials, norms_out, g, qnorm); }
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
 }

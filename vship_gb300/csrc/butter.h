@@ -33,6 +33,7 @@ public:
     float* distmap = nullptr;       // [pair][h][w] (paired form)
     double* norms = nullptr;        // [pair][3]
     int2* pimg_identity = nullptr;  // (2p, 2p + 1): the paired form's pair table
+    float** ibase = nullptr;        // device: base of image i = work + i * img_floats
 
     // Paired form: images 2p and 2p + 1 are pair p's reference and distorted frames.
     int init(int64_t width, int64_t height, int qnorm, float intensity, int max_pairs);
@@ -51,5 +52,17 @@ public:
     static size_t device_bytes(int64_t w, int64_t h, int pairs);
     static size_t image_bytes(int64_t w, int64_t h);
 };
+
+// Engine-free form (the serving runtime places images anywhere): upload this device's tables and
+// kernel attributes; floats of one image's workspace; norm partials per pair (x3 floats).
+int butter_prepare_device();
+size_t butter_image_floats(int64_t w, int64_t h);
+int butter_norm_tiles(int64_t w, int64_t h);
+// ib: device table of image workspaces; images [0, nstage) run their own stage (frames_dev[i]
+// is image i's frame), then every pair of pimg (indices into ib) runs the pair stage. partials:
+// npairs x 3 x norm_tiles floats; norms_out: npairs x 3 doubles; distmap_out: null or npairs maps.
+int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
+                   int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
+                   float* distmap_out, cudaStream_t st);
 
 }  // namespace vship
