@@ -167,13 +167,8 @@ def barrier(ws):
 
 
 def max_over_ranks(x: float, ws: int) -> float:
-    if ws == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from vship_gb300.dist import max_over_ranks as _m
+    return _m(x, ws)
 
 
 # ------------------------------------------------------------------------------------------

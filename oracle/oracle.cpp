@@ -723,13 +723,40 @@ void psycho_image(std::vector<T> src[3], int64_t w, int64_t h, float intensity, 
 }
 
 // butter/main.hpp:23-113 (getdiffmap) for one scale
+// half_bands models FP16 storage of the frequency bands that the pair stage reads: 1 = every
+// band of both images rounded to half; 2 = reference bands exact, distorted bands stored as
+// half(distorted - reference) and read back as reference + delta; 3 = as 2 but the LF bands
+// kept exact.
+template <typename T>
+void store_bands_half(Bands<T>& b1, Bands<T>& b2, int half_bands) {
+    auto each = [&](std::vector<T>& a, std::vector<T>& b) {
+        for (size_t i = 0; i < a.size(); i++) {
+            if (half_bands == 1) {
+                a[i] = round_half(a[i]);
+                b[i] = round_half(b[i]);
+            } else {
+                b[i] = a[i] + round_half(b[i] - a[i]);
+            }
+        }
+    };
+    for (int c = 0; c < 3; c++) {
+        if (half_bands != 3) each(b1.lf[c], b2.lf[c]);
+        each(b1.mf[c], b2.mf[c]);
+    }
+    for (int c = 0; c < 2; c++) {
+        each(b1.hf[c], b2.hf[c]);
+        each(b1.uhf[c], b2.uhf[c]);
+    }
+}
+
 template <typename T>
 std::vector<T> butter_diffmap(std::vector<T> src1[3], std::vector<T> src2[3], int64_t w, int64_t h, float intensity,
-                              const ButterKernels<T>& K, int nthreads) {
+                              const ButterKernels<T>& K, int nthreads, int half_bands = 0) {
     const int64_t n = w * h;
     Bands<T> b1, b2;
     psycho_image(src1, w, h, intensity, K, nthreads, b1);
     psycho_image(src2, w, h, intensity, K, nthreads, b2);
+    if (half_bands) store_bands_half(b1, b2, half_bands);
     std::vector<T> ac[3], dc[3];
     for (int c = 0; c < 3; c++) { ac[c].assign(n, (T)0); dc[c].assign(n, (T)0); }
     const T hf_asym = (T)0.8f;
@@ -785,7 +812,8 @@ std::vector<T> butter_diffmap(std::vector<T> src1[3], std::vector<T> src2[3], in
 // butter/main.hpp:116-195 (getmultiscalediffmap, butterprocess) and diffnorms.hpp:263-306
 template <typename T>
 void butteraugli(const uint8_t* const* src1, const uint8_t* const* src2, int64_t stride1, int64_t stride2, int64_t w,
-                 int64_t h, int intype, int qnorm, float intensity, int nthreads, double norms[3], float* distmap) {
+                 int64_t h, int intype, int qnorm, float intensity, int nthreads, double norms[3], float* distmap,
+                 int half_bands = 0) {
     ButterKernels<T> K;
     for (int i = 0; i < 5; i++) K.k[i] = butter_kernel<T>(i);
     const int64_t n = w * h, nw = half_dim(w), nh = half_dim(h);
@@ -801,8 +829,8 @@ void butteraugli(const uint8_t* const* src1, const uint8_t* const* src2, int64_t
             downsample(full[m][c].data(), half[m][c].data(), w, h);
         }
     }
-    std::vector<T> dm = butter_diffmap(full[0], full[1], w, h, intensity, K, nthreads);
-    std::vector<T> dms = butter_diffmap(half[0], half[1], nw, nh, intensity, K, nthreads);
+    std::vector<T> dm = butter_diffmap(full[0], full[1], w, h, intensity, K, nthreads, half_bands);
+    std::vector<T> dms = butter_diffmap(half[0], half[1], nw, nh, intensity, K, nthreads, half_bands);
     // butter/downupsample.hpp:287-301 (addsupersample2X, w = 0.5)
     const T wsup = (T)0.5f;
     for (int64_t y = 0; y < h; y++)
@@ -860,12 +888,14 @@ int oracle_butteraugli(const uint8_t* const* src1, const uint8_t* const* src2, i
                        int64_t width, int64_t height, int intype, int qnorm, float intensity, int precision,
                        int nthreads, double* norms3, float* distmap) {
     if (width <= 0 || height <= 0 || !norms3) return 1;
+    // precision 16: FP32 with every band stored as half; 17: FP32 with the distorted image's
+    // bands stored as half deltas against the reference's
     if (precision == 64)
         butteraugli<double>(src1, src2, stride1, stride2, width, height, intype, qnorm, intensity, nthreads, norms3,
                             distmap);
     else
         butteraugli<float>(src1, src2, stride1, stride2, width, height, intype, qnorm, intensity, nthreads, norms3,
-                           distmap);
+                           distmap, precision == 16 ? 1 : precision == 17 ? 2 : precision == 18 ? 3 : 0);
     return 0;
 }
 

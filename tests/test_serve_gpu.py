@@ -113,8 +113,9 @@ def test_serve_admission_and_eviction(vlib):
     reqs = _requests()
     mix, _ = _run(vlib, pool, reqs)
     w, h = RES[0]
-    # room for one 3-pair Butteraugli request at the larger size at a time; a cache of ~2 sources
-    tight, stats = _run(vlib, pool, reqs, admission_bytes=124 * w * h * 3, cache_bytes=2 * 4 * 16 * w * h * 5 // 4,
+    # room for one 3-pair Butteraugli request at the larger size at a time; a cache a little
+    # larger than one Butteraugli source at that size (2.9 MB), far below the stream's sources
+    tight, stats = _run(vlib, pool, reqs, admission_bytes=124 * w * h * 3, cache_bytes=3_500_000,
                         max_batch_pairs=4)
     assert tight == mix
     assert stats["admission_waits"] > 0 and stats["cache_evictions"] > 0
