@@ -1,17 +1,24 @@
 #!/usr/bin/env python3
-"""Benchmark: frame-pairs/s for SSIMULACRA2 at 1080p (headline) and Butteraugli at 4K.
+"""Benchmark: frame-pairs/s for SSIMULACRA2 at 1080p (headline) and Butteraugli at 4K, plus the
+batched multi-resolution form and the serving loop.
 
 Workloads (seeded synthetic frames, vship_gb300.synth; no dataset is available offline):
   * ssimu2_1080p : 240 pairs of 1920x1080 YUV420P10 (BT.709, limited range; 8x8 block-DCT
-                   distortion, step U[4, 32], chroma x2), converted to float32 R'G'B' planes.
+                   distortion, step U[4, 32], chroma x2).
   * butter_4k    : 60 pairs of 3840x2160 YUV420P10, Gaussian blur sigma U[0.5, 2] + noise sigma
-                   U[1, 6], float32 R'G'B' planes, intensity 203, Qnorm 2.
+                   U[1, 6], intensity 203, Qnorm 2.
+  Each is scored from three input forms: RGB48 (16-bit R'G'B' planes: what the reference's own
+  front-end converts every frame to before its Uint16 compute calls) -- the headline -- and,
+  beside it, float32 R'G'B' planes and the 10-bit 4:2:0 planes themselves (converted on the GPU).
+  * batched_multi: 64 sources at 360p/720p/1080p/2160p (26/19/13/6) x 8 block-DCT candidates,
+                   both metrics, one call per step (Vship_MultiComputeDeviceAsync).
+  * serving      : Poisson request arrivals at 50..2000 req/s against the serving runtime.
 
 A step scores every pair of the workload once.
   value : inputs resident in HBM, batched device entry points (Vship_*ComputeDeviceAsync), CUDA
-          events on the launching stream around the K timed steps. Inputs (12 GB per workload)
+          events on the launching stream around the K timed steps. Inputs (6-12 GB per workload)
           are far larger than L2, so no flush is needed between steps.
-  e2e   : the reference-facing C ABI (Vship_ComputeSSIMU2Float / Vship_ComputeButteraugliFloatv3)
+  e2e   : the reference-facing C ABI (Vship_ComputeSSIMU2Uint16 / Vship_ComputeButteraugliUint16v3)
           from pinned host buffers, one handler per host thread; every call copies its planes
           host->device and reads its score back.
 
@@ -203,7 +210,7 @@ def frames_table(v, ref, dst, start, count):
     frames = []
     for t in range(start, start + count):
         for x in (ref, dst):
-            frames.append(([x[t, c].data_ptr() for c in range(3)], x.stride(2) * 4))
+            frames.append(([x[t, c].data_ptr() for c in range(3)], x.stride(2) * x.element_size()))
     return v.device_frames_table(frames)
 
 
@@ -237,7 +244,7 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None):
         c = min(chunk, npairs - s)
         tables.append((s, c, frames_table(v, ref, dst, s, c) if yuv is None else yuv_table(v, yuv, s, c)))
     stream = torch.cuda.current_stream()
-    itype = v.IN_FLOAT if yuv is None else v.IN_YUV420P10
+    itype = v.IN_YUV420P10 if yuv is not None else (v.IN_UINT16 if ref.dtype == torch.int16 else v.IN_FLOAT)
 
     def step():
         for s, c, tb in tables:
@@ -298,7 +305,8 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
                 base = hy[t, m].data_ptr()
                 pp.append((ctypes.c_void_p * 3)(base, base + 2 * h * w, base + 2 * (h * w + ch * cw)))
             plane_ptrs.append(tuple(pp))
-    stride = w * 4
+    u16 = yuv is None and ref.dtype == torch.int16
+    stride = w * (2 if u16 else 4)
     handlers = []
     for _ in range(nthreads):
         hd = v.Handler()
@@ -326,10 +334,18 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
                 rc = L.Vship_ComputeButteraugliYuv420p10(hd, norms, None, 0, ctypes.cast(a, v._PP), ystr,
                                                          ctypes.cast(b, v._PP), ystr)
                 scores[i] = norms[0]
+            elif kind == "ssimu2" and u16:
+                rc = L.Vship_ComputeSSIMU2Uint16(hd, ctypes.byref(sc), ctypes.cast(a, v._PP), ctypes.cast(b, v._PP),
+                                                 stride)
+                scores[i] = sc.value
             elif kind == "ssimu2":
                 rc = L.Vship_ComputeSSIMU2Float(hd, ctypes.byref(sc), ctypes.cast(a, v._PP), ctypes.cast(b, v._PP),
                                                 stride)
                 scores[i] = sc.value
+            elif u16:
+                rc = L.Vship_ComputeButteraugliUint16v3(hd, norms, None, 0, ctypes.cast(a, v._PP),
+                                                        ctypes.cast(b, v._PP), stride, stride)
+                scores[i] = norms[0]
             else:
                 rc = L.Vship_ComputeButteraugliFloatv3(hd, norms, None, 0, ctypes.cast(a, v._PP),
                                                        ctypes.cast(b, v._PP), stride, stride)
@@ -357,7 +373,7 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
             L.Vship_ButteraugliFree(hd)
     if errors:
         raise v.VshipError(errors[0], "e2e compute")
-    h2d = npairs * 2 * 3 * w * h * 4 if yuv is None else npairs * 2 * 2 * (h * w + 2 * ((w + 1) // 2) * ((h + 1) // 2))
+    h2d = npairs * 2 * 3 * w * h * (2 if u16 else 4) if yuv is None else npairs * 2 * 2 * (h * w + 2 * ((w + 1) // 2) * ((h + 1) // 2))
     d2h = npairs * (8 if kind == "ssimu2" else 24)
     return sec, h2d, d2h, np.array(scores)
 
@@ -379,23 +395,48 @@ def cpu_baseline(kind, ref, dst, sample_pairs, nthreads):
     return sample_pairs / t_total, t_total
 
 
+def to_rgb48(x):
+    """float32 R'G'B' in [0, 1] -> 16-bit code values (uint16 bits held in int16), the RGB48
+    planes the reference's own front-end hands to its compute calls."""
+    import torch
+    return torch.round(x.clamp(0.0, 1.0) * 65535.0).to(torch.int32).to(torch.int16)
+
+
 def bench_workload(v, kind, args, ws, rank):
+    """The headline form is the reference front-end's own input: 16-bit R'G'B' planes (FFVship
+    converts every frame to RGB48 and calls the Uint16 entry points). Float32 R'G'B' and
+    10-bit 4:2:0 (converted on the GPU) are measured beside it."""
     import torch
     npairs = args.pairs if kind == "ssimu2" else args.butter_pairs
     chunk = args.chunk if kind == "ssimu2" else args.butter_chunk
     size = parse_size(args.ssimu2_size if kind == "ssimu2" else args.butter_size)
     ref, dst, yuv = make_inputs(kind, npairs, "cuda", size)
     torch.cuda.synchronize()
+    w, h = size
+    # float32 R'G'B' planes
+    fsec, _, _, _ = run_device(v, kind, ref, dst, args.steps, args.warmup, ws, chunk)
+    fsec = max_over_ranks(fsec, ws)
+    fe2e_sec, fh2d, d2h, _ = run_e2e(v, kind, ref, dst, args.e2e_steps, 1, args.e2e_threads)
+    fe2e_sec = max_over_ranks(fe2e_sec, ws)
+    cpu_res = None
+    if rank == 0 and args.cpu_sample > 0:
+        ns = args.cpu_sample if kind == "ssimu2" else max(1, args.cpu_sample // 4)
+        cv, csec = cpu_baseline(kind, ref, dst, ns, os.cpu_count() or 1)
+        cpu_res = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"{ns} pairs of the same workload ({csec:.1f} s)"}
+    # 16-bit R'G'B' (headline)
+    ref16, dst16 = to_rgb48(ref), to_rgb48(dst)
+    del ref, dst
+    torch.cuda.empty_cache()
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
-    sec, prof, launches, dev_scores = run_device(v, kind, ref, dst, args.steps, args.warmup, ws, chunk)
+    sec, prof, launches, dev_scores = run_device(v, kind, ref16, dst16, args.steps, args.warmup, ws, chunk)
     clocks = sampler.stop()
     sec = max_over_ranks(sec, ws)
     value = npairs * ws * args.steps / sec
-    e2e_sec, h2d, d2h, host_scores = run_e2e(v, kind, ref, dst, args.e2e_steps, 1, args.e2e_threads)
+    e2e_sec, h2d, d2h, host_scores = run_e2e(v, kind, ref16, dst16, args.e2e_steps, 1, args.e2e_threads)
     e2e_sec = max_over_ranks(e2e_sec, ws)
     e2e_value = npairs * ws * args.e2e_steps / e2e_sec
-    w, h = size
     kname = "ssimu2_stats" if kind == "ssimu2" else "butter_diff"
     per_pair = ssimu2_stats_bytes(w, h) if kind == "ssimu2" else butter_diff_bytes(w, h)
     peak, peak_kind = measured_peaks()
@@ -409,20 +450,26 @@ def bench_workload(v, kind, args, ws, rank):
     pairs_per_launch = npairs * args.steps / max(n_launch, 1)
     traffic = ncu_traffic(kname)
     total_kernel_ms = sum(t for _, t in prof.values())
-    # the same workload from 10-bit 4:2:0 input converted on the GPU (the configuration's native
-    # format: a quarter of the bytes of float RGB)
+    del ref16, dst16
+    torch.cuda.empty_cache()
+    # 10-bit 4:2:0 planes converted on the GPU (a quarter of the bytes of float RGB)
     ysec, _, _, _ = run_device(v, kind, None, None, args.steps, args.warmup, ws, chunk, yuv=(yuv, size))
     ysec = max_over_ranks(ysec, ws)
     ye2e_sec, yh2d, _, _ = run_e2e(v, kind, None, None, args.e2e_steps, 1, args.e2e_threads, yuv=(yuv, size))
     ye2e_sec = max_over_ranks(ye2e_sec, ws)
     res = {
         "value": value, "unit": "frame-pairs/s", "ms_per_step": sec / args.steps * 1e3,
+        "input": "RGB48 (16-bit R'G'B' planes)",
+        "float32_rgb": {"value": npairs * ws * args.steps / fsec,
+                        "e2e": {"value": npairs * ws * args.e2e_steps / fe2e_sec, "unit": "frame-pairs/s",
+                                "h2d_bytes_per_step": fh2d, "d2h_bytes_per_step": d2h}},
         "yuv420p10": {"value": npairs * ws * args.steps / ysec,
                       "e2e": {"value": npairs * ws * args.e2e_steps / ye2e_sec, "unit": "frame-pairs/s",
                               "h2d_bytes_per_step": yh2d, "d2h_bytes_per_step": d2h}},
         "pairs_per_step": npairs,
         "e2e": {"value": e2e_value, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "threads": args.e2e_threads, "steps": args.e2e_steps},
+                "threads": args.e2e_threads, "steps": args.e2e_steps,
+                "call": "Vship_ComputeSSIMU2Uint16" if kind == "ssimu2" else "Vship_ComputeButteraugliUint16v3"},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic * pairs_per_launch if traffic is not None else None,
@@ -435,13 +482,8 @@ def bench_workload(v, kind, args, ws, rank):
         "score_check": {"device_vs_e2e_max_abs": float(abs(
             (dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy()[0::3]) - host_scores).max())},
     }
-    if rank == 0 and args.cpu_sample > 0:
-        cv, csec = cpu_baseline(kind, ref, dst, args.cpu_sample if kind == "ssimu2" else max(1, args.cpu_sample // 4),
-                                os.cpu_count() or 1)
-        res["cpu_baseline"] = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
-                               "sample": f"{args.cpu_sample if kind == 'ssimu2' else max(1, args.cpu_sample // 4)} "
-                                         f"pairs of the same workload ({csec:.1f} s)"}
-    del ref, dst
+    if cpu_res:
+        res["cpu_baseline"] = cpu_res
     torch.cuda.empty_cache()
     return res
 
@@ -841,14 +883,15 @@ def main_ours(args):
     out = {
         "metric": "frame-pairs/s (1080p SSIMU2)", "value": s2["value"], "unit": "frame-pairs/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": s2["ms_per_step"], "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"ssimu2_1080p: {args.pairs} pairs 1920x1080 YUV420P10 -> float32 RGB planes, "
-                               "8x8 block-DCT distortion", "pairs_per_step": args.pairs,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gratings + noise, block-DCT distortion)",
+        "config": {"workload": f"ssimu2_1080p: {args.pairs} pairs 1920x1080 YUV420P10 -> RGB48 planes (the "
+                               "reference front-end's conversion), 8x8 block-DCT distortion",
+                   "pairs_per_step": args.pairs,
                    "parallelism": f"replicas x{ws}", "l2": "inputs 12 GB > L2, no flush",
                    "launch_chunk_pairs": args.chunk},
         "e2e": s2["e2e"], "roofline": s2["roofline"], "gpu_launches": s2["gpu_launches"], "clocks": s2["clocks"],
         "kernel_share": s2["kernel_share"], "pipeline_bytes_per_pair": s2["pipeline_bytes_per_pair"],
-        "yuv420p10": s2["yuv420p10"],
+        "yuv420p10": s2["yuv420p10"], "float32_rgb": s2["float32_rgb"], "input": s2["input"],
         "score_check": s2["score_check"],
     }
     if "cpu_baseline" in s2:
@@ -856,6 +899,7 @@ def main_ours(args):
     if not args.skip_butter:
         b = bench_workload(v, "butter", args, ws, rank)
         out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e", "yuv420p10",
+                                                   "float32_rgb", "input",
                                                    "roofline", "gpu_launches", "clocks", "kernel_share",
                                                    "pipeline_bytes_per_pair", "score_check")
                                  if k in b}
@@ -890,7 +934,9 @@ def main_reference(args):
     frames = []
     for t in range(args.warmup + args.steps):
         r, d = synth.yuv420p10_frames(H1080, W1080, t, seed=7, distortion="dct", device="cpu")
-        a, b = synth.yuv420p10_to_rgb(r).numpy(), synth.yuv420p10_to_rgb(d).numpy()
+        # RGB48 planes, the input form of the measured workload
+        a = to_rgb48(synth.yuv420p10_to_rgb(r)).numpy().view(np.uint16)
+        b = to_rgb48(synth.yuv420p10_to_rgb(d)).numpy().view(np.uint16)
         frames.append(([np.ascontiguousarray(a[c]) for c in range(3)], [np.ascontiguousarray(b[c]) for c in range(3)]))
     for t in range(args.warmup):
         oracle.ssimu2(*frames[t], precision=32, nthreads=nt)
@@ -902,9 +948,9 @@ def main_reference(args):
     out = {
         "impl": "reference", "metric": "frame-pairs/s (1080p SSIMU2)", "value": value, "unit": "frame-pairs/s",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec / args.steps * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded gratings + noise, block-DCT distortion)",
         "config": {"workload": "ssimu2_1080p: 1 pair per step of the 1920x1080 YUV420P10 block-DCT workload, "
-                               "float32 RGB planes", "pairs_per_step": 1},
+                               "RGB48 planes", "pairs_per_step": 1},
         "cpu_baseline": {"value": value, "unit": "frame-pairs/s", "cores": nt, "kind": "port",
                          "sample": f"{args.steps} pairs, 1 per step"},
         "e2e": {"value": value, "unit": "frame-pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
