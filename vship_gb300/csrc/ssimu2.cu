@@ -214,9 +214,9 @@ constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte 
 constexpr int ST_HP = 33;                // horizontal-pass output pitch
 constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
 constexpr int ST_HPLANE = ST_IH * ST_HP;
-// smem: 2 stages x 2 raw images, the horizontal pass as two float-pair planes {m1,m2} and
-// {s11,s22} plus one float plane s12, and the per-warp pools
-constexpr int kStatsSmem = (2 * 2 * ST_RAW + 5 * ST_HPLANE + 3 * 8 * 6) * 4;
+// smem: 2 stages x 2 raw images, the horizontal pass as two float-pair planes {m1, m2} and
+// {s11 + s22, s12}, and the per-warp pools
+constexpr int kStatsSmem = (2 * 2 * ST_RAW + 4 * ST_HPLANE + 3 * 8 * 6) * 4;
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
@@ -273,7 +273,7 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
     extern __shared__ __align__(16) float sm[];
     float* raw = sm;                   // [stage][image][64][52]
     float* hb = sm + 4 * ST_RAW;       // [5][64][33]
-    float* red = hb + 5 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
+    float* red = hb + 4 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
     const float* im2 = static_cast<const float*>(im2v);
     const __half* im2h = static_cast<const __half*>(im2v);
     const int tx0 = (lt % L.tiles_x) * ST_TW;
@@ -335,16 +335,15 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
         }
         {
             // Horizontal pass. Lane mapping: row hr = 8*warp + (lane & 7), outputs 8*hg..+7 with
-            // hg = lane >> 3. The reference / distorted moments travel as float pairs through the
-            // f32x2 FMA: {a, b} and {a^2, b^2} share every weight; a*b is scalar.
+            // hg = lane >> 3. The SSIM map needs the two variances only as their sum
+            // (score.hpp:147), so four moments are blurred: {a, b} and {a^2 + b^2, a*b}, each pair
+            // through the f32x2 FMA with a shared weight.
             f2_t h1[8], h2[8];
-            float h3[8];
             const f2_t z2 = f2_pack(0.f, 0.f);
 #pragma unroll
             for (int o = 0; o < 8; o++) {
                 h1[o] = z2;
                 h2[o] = z2;
-                h3[o] = 0.f;
             }
             const float* ra = r1 + hr * ST_RP + 8 * hg;
             const float* rb = r2 + hr * ST_RP + 8 * hg;
@@ -376,36 +375,31 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                     const float a = la[u] - shift;
                     const float b = DELTA ? a + dl[j] : lb[u] - shift;
                     const f2_t p1 = f2_pack(a, b);
-                    const f2_t p2 = f2_mul(p1, p1);
-                    const float ab = a * b;
+                    const f2_t p2 = f2_pack(fmaf(a, a, b * b), a * b);
 #pragma unroll
                     for (int o = 0; o < 8; o++) {
                         const int i = j - o;  // tap index
                         if (i >= 0 && i < 17) {
                             h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
                             h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
-                            h3[o] = fmaf(ab, c_s2_k[i], h3[o]);
                         }
                     }
                 }
             }
             f2_t* d1 = reinterpret_cast<f2_t*>(hb) + hr * ST_HP + 8 * hg;
             f2_t* d2 = reinterpret_cast<f2_t*>(hb + 2 * ST_HPLANE) + hr * ST_HP + 8 * hg;
-            float* d3 = hb + 4 * ST_HPLANE + hr * ST_HP + 8 * hg;
 #pragma unroll
             for (int o = 0; o < 8; o++) {
                 d1[o] = h1[o];
                 d2[o] = h2[o];
-                d3[o] = h3[o];
             }
         }
         __syncthreads();
         // vertical pass + maps (column vc, rows 6*vg .. 6*vg+5)
-        float m[5][6];
+        float m[4][6];  // mu1, mu2, E[a^2 + b^2], E[a b] (shifted)
         {
             const f2_t* c1 = reinterpret_cast<const f2_t*>(hb) + (6 * vg) * ST_HP + vc;
             const f2_t* c2 = reinterpret_cast<const f2_t*>(hb + 2 * ST_HPLANE) + (6 * vg) * ST_HP + vc;
-            const float* c3 = hb + 4 * ST_HPLANE + (6 * vg) * ST_HP + vc;
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const f2_t* col = q == 0 ? c1 : c2;
@@ -421,16 +415,6 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                     f2_unpack(a, m[2 * q][o], m[2 * q + 1][o]);
                 }
             }
-            float v[22];
-#pragma unroll
-            for (int j = 0; j < 22; j++) v[j] = c3[j * ST_HP];
-#pragma unroll
-            for (int o = 0; o < 6; o++) {
-                float a = 0.f;
-#pragma unroll
-                for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_s2_k[i], a);
-                m[4][o] = a * rxy[o];
-            }
         }
         float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -444,13 +428,15 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                                        : r2[so] - shift;
                 const float m1 = m[0][o], m2 = m[1][o];                 // shifted means
                 // SSIM map (score.hpp:141-148) as max((den - num) / den, 0), the same quantity
-                // as max(1 - num / den, 0) without the cancellation; explicit fma so identical
-                // frames give num == den bitwise whatever the compiler contracts
+                // as max(1 - num / den, 0) without the cancellation; sigma11 + sigma22 as
+                // (S/2 - m1^2) + (S/2 - m2^2) with S = E[a^2 + b^2]. Explicit fma: identical
+                // frames give S/2 == E[ab] exactly (a^2 + b^2 = 2ab), so num == den bitwise
                 const float md = m1 - m2;
                 const float num_m = fmaf(md, -md, 1.0f);
-                const float s12 = fmaf(-m1, m2, m[4][o]);
-                const float s11 = fmaf(-m1, m1, m[2][o]);
-                const float s22 = fmaf(-m2, m2, m[3][o]);
+                const float hs = 0.5f * m[2][o];
+                const float s12 = fmaf(-m1, m2, m[3][o]);
+                const float s11 = fmaf(-m1, m1, hs);
+                const float s22 = fmaf(-m2, m2, hs);
                 const float num_s = fmaf(s12, 2.0f, 0.0009f);
                 const float denom = (s11 + s22) + 0.0009f;
                 const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
