@@ -180,15 +180,17 @@ EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliUint16v3(Vship_Butterau
                                                                   int64_t stride, int64_t stride2);
 
 /* Sample formats of the device-resident entry points (0..3 numbered as the reference's
- * InputMemType, src/util/preprocessor.hpp:94). Vship_InYuv420p10 is 10-bit 4:2:0 Y'CbCr in
- * 16-bit little-endian containers, BT.709 limited range, converted on the GPU to full-range
- * R'G'B' (chroma upsampled bilinearly with MPEG-2 siting) -- the conversion the reference's
- * front-ends do on the CPU before calling the ABI, at a quarter of the bytes of float RGB. */
+ * InputMemType, src/util/preprocessor.hpp:94). Vship_InYuv is Y'CbCr converted on the GPU to
+ * full-range R'G'B' -- the conversion the reference's front-ends do on the CPU before calling
+ * the ABI -- in the handler's format (Vship_YuvFormat below), by default 10-bit 4:2:0 in 16-bit
+ * little-endian containers, BT.709 limited range, chroma upsampled bilinearly with MPEG-2 (left)
+ * siting (Vship_InYuv420p10, the same value): a quarter of the bytes of float RGB. */
 typedef enum {
     Vship_InUint8 = 0,
     Vship_InUint16 = 1,
     Vship_InHalf = 2,
     Vship_InFloat = 3,
+    Vship_InYuv = 4,
     Vship_InYuv420p10 = 4,
 } Vship_InputType;
 
@@ -210,6 +212,38 @@ EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliYuv420p10(Vship_Buttera
                                                                    const uint8_t* dstp, int64_t dststride,
                                                                    const uint8_t* srcp1[3], const int64_t stride1[3],
                                                                    const uint8_t* srcp2[3], const int64_t stride2[3]);
+
+/* Y'CbCr input of any common format, converted on the GPU the way the reference's front-ends
+ * convert it on the CPU (FFVship's zimg setup, ffmpegToZimgFormat.hpp): chroma upsampled
+ * bilinearly at its siting, the matrix and range applied, clamped full-range R'G'B' out.
+ * bits: 8 (samples in bytes) to 16 (little-endian 16-bit containers); subsampling_w/_h: log2
+ * chroma subsampling (0 or 1: 4:4:4, 4:2:2, 4:2:0); matrix: ITU-T H.273 matrix_coefficients 1
+ * (BT.709), 4 (FCC), 5 (BT.470BG), 6 (SMPTE 170M), 7 (SMPTE 240M), 9 (BT.2020 NCL), or 2
+ * (unspecified: BT.709 above 650 rows, BT.470BG below, as the reference guesses); range: 0
+ * limited, 1 full; chroma_location: 0 left, 1 center, 2 top-left, 3 top, 4 bottom-left,
+ * 5 bottom. Frames are in the BT.709 transfer and primaries (the reference's assumption). */
+typedef struct {
+    int bits;
+    int subsampling_w;
+    int subsampling_h;
+    int matrix;
+    int range;
+    int chroma_location;
+} Vship_YuvFormat;
+/* The format a handler uses for Vship_InYuv frames (device entry points) and for the
+ * Vship_Compute*Yuv calls; the default is 10-bit 4:2:0 BT.709 limited range, left siting. The
+ * Yuv420p10 calls always use that default. Vship_BadPointer: a format outside the list above. */
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2SetYuvFormat(Vship_SSIMU2Handler handler, const Vship_YuvFormat* format);
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliSetYuvFormat(Vship_ButteraugliHandler handler,
+                                                               const Vship_YuvFormat* format);
+/* Host-buffer scoring of Y'CbCr frames in the handler's format (planes Y, Cb, Cr, strides in bytes). */
+EXPORTPREPROCESS Vship_Exception Vship_ComputeSSIMU2Yuv(Vship_SSIMU2Handler handler, double* score,
+                                                        const uint8_t* srcp1[3], const int64_t stride1[3],
+                                                        const uint8_t* srcp2[3], const int64_t stride2[3]);
+EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliYuv(Vship_ButteraugliHandler handler, double norms[3],
+                                                             const uint8_t* dstp, int64_t dststride,
+                                                             const uint8_t* srcp1[3], const int64_t stride1[3],
+                                                             const uint8_t* srcp2[3], const int64_t stride2[3]);
 
 /* Batched, device-resident SSIMU2 for callers whose frames already live in GPU memory (decoders,
  * encoders' candidate buffers): one launch scores up to max_pairs pairs of one resolution.
@@ -300,6 +334,8 @@ EXPORTPREPROCESS Vship_Exception Vship_MultiComputeDeviceAsync(Vship_MultiHandle
                                                                const int* candidate_source,
                                                                Vship_InputType input_type, double* ssimu2_dev,
                                                                double* butter_norms_dev, void* stream);
+/* Format of Vship_InYuv frames (Vship_YuvFormat; matrix 2 resolves per resolution). */
+EXPORTPREPROCESS Vship_Exception Vship_MultiSetYuvFormat(Vship_MultiHandler handler, const Vship_YuvFormat* format);
 /* The launch knobs in use as JSON (same size/truncation contract as Vship_GetErrorMessage). */
 EXPORTPREPROCESS int Vship_MultiKnobs(Vship_MultiHandler handler, char* out_json, int len);
 EXPORTPREPROCESS uint64_t Vship_MultiDeviceBytes(int nres, const int* widths, const int* heights,
@@ -346,6 +382,9 @@ EXPORTPREPROCESS Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, 
                                                    uint64_t admission_bytes, uint64_t cache_bytes,
                                                    int max_batch_pairs, int flags, int Qnorm,
                                                    float intensity_multiplier);
+/* Format of Vship_InYuv frames (Vship_YuvFormat; matrix 2 resolves per resolution); set it
+ * before the first submit. */
+EXPORTPREPROCESS Vship_Exception Vship_ServeSetYuvFormat(Vship_ServeHandler handler, const Vship_YuvFormat* format);
 /* Vship_OutOfVRAM: the request's charge alone exceeds admission_bytes. */
 EXPORTPREPROCESS Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* request);
 /* Up to max completions, waiting up to timeout_seconds for the first; returns how many. */

@@ -26,7 +26,8 @@ EXCEPTION_NAMES = ["NoError", "OutOfVRAM", "OutOfRAM", "DifferingInputType", "No
                    "BadErrorType"]
 
 # Vship_InputType
-IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT, IN_YUV420P10 = 0, 1, 2, 3, 4
+IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT, IN_YUV = 0, 1, 2, 3, 4
+IN_YUV420P10 = IN_YUV  # the default Y'CbCr format (10-bit 4:2:0, BT.709, limited, left siting)
 
 
 class VshipError(RuntimeError):
@@ -64,6 +65,19 @@ _PP = ctypes.POINTER(ctypes.c_void_p)
 _H = Handler
 _E = ctypes.c_int
 _IP = ctypes.POINTER(ctypes.c_int)
+
+
+class YuvFormat(ctypes.Structure):
+    """Vship_YuvFormat: bits 8..16, log2 chroma subsampling, H.273 matrix (2 = by height), range
+    (0 limited, 1 full), chroma location (0 left, 1 center, 2 top-left, 3 top, 4 bottom-left,
+    5 bottom)."""
+    _fields_ = [("bits", ctypes.c_int), ("subsampling_w", ctypes.c_int), ("subsampling_h", ctypes.c_int),
+                ("matrix", ctypes.c_int), ("range", ctypes.c_int), ("chroma_location", ctypes.c_int)]
+
+
+def yuv_format(bits=10, subsampling=(1, 1), matrix=1, full_range=False, chroma_location=0) -> YuvFormat:
+    return YuvFormat(int(bits), int(subsampling[0]), int(subsampling[1]), int(matrix), 1 if full_range else 0,
+                     int(chroma_location))
 
 
 class ServeRequest(ctypes.Structure):
@@ -139,6 +153,14 @@ SIGNATURES = {
     "Vship_ServeDrain": (_E, [_H]),
     "Vship_ServeStats": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
     "Vship_ServeDestroy": (_E, [_H]),
+    "Vship_SSIMU2SetYuvFormat": (_E, [_H, ctypes.POINTER(YuvFormat)]),
+    "Vship_ButteraugliSetYuvFormat": (_E, [_H, ctypes.POINTER(YuvFormat)]),
+    "Vship_ComputeSSIMU2Yuv": (_E, [_H, ctypes.POINTER(ctypes.c_double), _PP, ctypes.POINTER(ctypes.c_int64), _PP,
+                                    ctypes.POINTER(ctypes.c_int64)]),
+    "Vship_ComputeButteraugliYuv": (_E, [_H, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int64, _PP,
+                                         ctypes.POINTER(ctypes.c_int64), _PP, ctypes.POINTER(ctypes.c_int64)]),
+    "Vship_MultiSetYuvFormat": (_E, [_H, ctypes.POINTER(YuvFormat)]),
+    "Vship_ServeSetYuvFormat": (_E, [_H, ctypes.POINTER(YuvFormat)]),
     "Vship_ProfileSetEnabled": (None, [ctypes.c_int]),
     "Vship_ProfileReport": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int]),
 }
@@ -237,14 +259,17 @@ def planes_of(frame):
     return arr, strides.pop(), w, h, dt, planes
 
 
-def _yuv_planes(frame, w, h):
-    """(Y, Cb, Cr) uint16 arrays of a w x h 4:2:0 frame -> (pointer array, stride array)."""
+def _yuv_planes(frame, w, h, fmt=None):
+    """(Y, Cb, Cr) arrays of a w x h frame in format fmt (default 10-bit 4:2:0) -> (pointer
+    array, stride array). Samples: uint8 for 8 bits, uint16 above."""
     planes = [np.asarray(p) for p in frame]
-    cw, ch = (w + 1) // 2, (h + 1) // 2
+    ssw, ssh, bits = (1, 1, 10) if fmt is None else (fmt.subsampling_w, fmt.subsampling_h, fmt.bits)
+    cw, ch = ((w + 1) // 2 if ssw else w), ((h + 1) // 2 if ssh else h)
     shapes = [(h, w), (ch, cw), (ch, cw)]
+    dt = np.uint8 if bits == 8 else np.uint16
     for p, shp in zip(planes, shapes):
-        if p.dtype != np.uint16 or p.shape != shp or p.strides[1] != 2:
-            raise VshipError(DifferingInputType, "4:2:0 planes must be uint16 (h, w), (ceil(h/2), ceil(w/2)) x2")
+        if p.dtype != dt or p.shape != shp or p.strides[1] != p.itemsize:
+            raise VshipError(DifferingInputType, f"Y'CbCr planes must be {np.dtype(dt).name} {shapes}")
     ptrs = (ctypes.c_void_p * 3)(*[p.ctypes.data for p in planes])
     strides = (ctypes.c_int64 * 3)(*[p.strides[0] for p in planes])
     return ptrs, strides
@@ -276,6 +301,20 @@ class SSIMU2Handler:
         out = ctypes.c_double()
         _check(lib().Vship_ComputeSSIMU2Yuv420p10(self._h, ctypes.byref(out), ctypes.cast(a1, _PP), s1,
                                                   ctypes.cast(a2, _PP), s2), "Vship_ComputeSSIMU2Yuv420p10")
+        return out.value
+
+    def set_yuv_format(self, fmt: YuvFormat) -> None:
+        _check(lib().Vship_SSIMU2SetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_SSIMU2SetYuvFormat")
+        self._fmt = fmt
+
+    def compute_yuv(self, reference, distorted) -> float:
+        """Score Y'CbCr frames in the format set by set_yuv_format (Vship_ComputeSSIMU2Yuv)."""
+        fmt = getattr(self, "_fmt", None)
+        a1, s1 = _yuv_planes(reference, self.width, self.height, fmt)
+        a2, s2 = _yuv_planes(distorted, self.width, self.height, fmt)
+        out = ctypes.c_double()
+        _check(lib().Vship_ComputeSSIMU2Yuv(self._h, ctypes.byref(out), ctypes.cast(a1, _PP), s1,
+                                            ctypes.cast(a2, _PP), s2), "Vship_ComputeSSIMU2Yuv")
         return out.value
 
     def free(self):
@@ -332,6 +371,23 @@ class ButteraugliHandler:
         res = (norms[0], norms[1], norms[2])
         return (res, dm) if distmap else res
 
+    def set_yuv_format(self, fmt: YuvFormat) -> None:
+        _check(lib().Vship_ButteraugliSetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_ButteraugliSetYuvFormat")
+        self._fmt = fmt
+
+    def compute_yuv(self, reference, distorted, distmap: bool = False):
+        """Butteraugli of Y'CbCr frames in the format set by set_yuv_format."""
+        fmt = getattr(self, "_fmt", None)
+        a1, s1 = _yuv_planes(reference, self.width, self.height, fmt)
+        a2, s2 = _yuv_planes(distorted, self.width, self.height, fmt)
+        norms = (ctypes.c_double * 3)()
+        dm = np.empty((self.height, self.width), np.float32) if distmap else None
+        _check(lib().Vship_ComputeButteraugliYuv(self._h, norms, dm.ctypes.data if dm is not None else None,
+                                                 self.width * 4, ctypes.cast(a1, _PP), s1,
+                                                 ctypes.cast(a2, _PP), s2), "Vship_ComputeButteraugliYuv")
+        res = (norms[0], norms[1], norms[2])
+        return (res, dm) if distmap else res
+
     def free(self):
         if self._h is not None:
             _check(lib().Vship_ButteraugliFree(self._h), "Vship_ButteraugliFree")
@@ -358,6 +414,9 @@ class SSIMU2Batch:
         self._h = Handler()
         _check(lib().Vship_SSIMU2BatchInit(ctypes.byref(self._h), self.width, self.height, self.max_pairs),
                "Vship_SSIMU2BatchInit")
+
+    def set_yuv_format(self, fmt: YuvFormat) -> None:
+        _check(lib().Vship_SSIMU2SetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_SSIMU2SetYuvFormat")
 
     def compute_async(self, frames_dev_ptr: int, npairs: int, input_type: int, scores_dev_ptr: int,
                       stream_ptr: int = 0) -> None:
@@ -386,6 +445,9 @@ class ButteraugliBatch:
         _check(lib().Vship_ButteraugliBatchInit(ctypes.byref(self._h), self.width, self.height, int(qnorm),
                                                 ctypes.c_float(intensity_multiplier), self.max_pairs),
                "Vship_ButteraugliBatchInit")
+
+    def set_yuv_format(self, fmt: YuvFormat) -> None:
+        _check(lib().Vship_ButteraugliSetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_ButteraugliSetYuvFormat")
 
     def compute_async(self, frames_dev_ptr: int, npairs: int, input_type: int, norms_dev_ptr: int,
                       distmaps_dev_ptr: int = 0, stream_ptr: int = 0) -> None:
@@ -457,6 +519,9 @@ class MultiScorer:
                                                    ctypes.c_void_p(butter_dev_ptr or None),
                                                    ctypes.c_void_p(stream_ptr)), "Vship_MultiComputeDeviceAsync")
 
+    def set_yuv_format(self, fmt: YuvFormat) -> None:
+        _check(lib().Vship_MultiSetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_MultiSetYuvFormat")
+
     def knobs(self) -> dict:
         import json
 
@@ -523,6 +588,9 @@ class Server:
             self._live.pop(rid, None)
             out.append((rid, int(buf[i].status), float(buf[i].latency_seconds)))
         return out
+
+    def set_yuv_format(self, fmt: YuvFormat) -> None:
+        _check(lib().Vship_ServeSetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_ServeSetYuvFormat")
 
     def drain(self):
         _check(lib().Vship_ServeDrain(self._h), "Vship_ServeDrain")

@@ -64,6 +64,10 @@ struct HandleTable {
     }
 };
 
+bool yuv_from_format(const Vship_YuvFormat& f, int64_t height, YuvParams* out) {
+    return make_yuv_params(f.bits, f.subsampling_w, f.subsampling_h, f.matrix, f.range, f.chroma_location, height, out);
+}
+
 Vship_Exception to_exc(int e) {
     return (e >= 0 && e <= E_BAD_ERROR_TYPE) ? (Vship_Exception)e : Vship_BadErrorType;
 }
@@ -111,7 +115,8 @@ struct HostPath {
     int device = 0;
     cudaStream_t stream = nullptr;
     uint8_t* staging = nullptr;      // 2 frames x 3 planes x h x (w*4) bytes
-    FrameDesc* frames_d = nullptr;   // [0..1]: 2-byte samples, [2..3]: 4-byte, [4..5]: YUV 4:2:0
+    FrameDesc* frames_d = nullptr;   // [0..1]: 2-byte samples, [2..3]: 4-byte, [4..5]: Y'CbCr
+    int64_t yuv_stride = 0, yuv_stride_c = 0;  // row pitches the Y'CbCr descriptors hold
     void* result_h = nullptr;        // pinned
     std::mutex mu;                   // one compute at a time per handler
 
@@ -129,11 +134,13 @@ struct HostPath {
                 fd[k * 2 + m].stride = w * bps;
                 fd[k * 2 + m].stride_c = w * bps;
             }
-        for (int m = 0; m < 2; m++) {  // YUV: planes at the float-plane slots of each frame
+        for (int m = 0; m < 2; m++) {  // Y'CbCr: planes at the float-plane slots of each frame
             for (int c = 0; c < 3; c++) fd[4 + m].plane[c] = staging + (size_t)(m * 3 + c) * plane4;
             fd[4 + m].stride = w * 2;
             fd[4 + m].stride_c = ((w + 1) / 2) * 2;
         }
+        yuv_stride = w * 2;
+        yuv_stride_c = ((w + 1) / 2) * 2;
         TRY_CUDA(cudaMemcpy(frames_d, fd, sizeof(fd), cudaMemcpyHostToDevice));
         if (cudaMallocHost(&result_h, result_bytes) != cudaSuccess) return E_OUT_OF_RAM;
         return E_OK;
@@ -163,18 +170,30 @@ struct HostPath {
         *fd_out = frames_d + (bps == 4 ? 2 : 0);
         return E_OK;
     }
-    // Uploads two 4:2:0 frames (Y, Cb, Cr with their own strides) into the YUV slots.
+    // Uploads two Y'CbCr frames (Y, Cb, Cr with their own strides) of format yp into the YUV
+    // slots (dense rows) and points their descriptors at them.
     int upload_yuv(const uint8_t* const* s1, const int64_t* st1, const uint8_t* const* s2, const int64_t* st2,
-                   int64_t w, int64_t h, const FrameDesc** fd_out) {
+                   int64_t w, int64_t h, const YuvParams& yp, const FrameDesc** fd_out) {
         if (!s1 || !s2 || !st1 || !st2) return E_BAD_POINTER;
-        const int64_t cw = (w + 1) / 2, ch = (h + 1) / 2;
+        const int64_t cw = yp.ssw ? (w + 1) / 2 : w, ch = yp.ssh ? (h + 1) / 2 : h;
         const size_t plane4 = (size_t)w * 4 * h;
+        if (yuv_stride != w * yp.bytes || yuv_stride_c != cw * yp.bytes) {
+            FrameDesc fd[2];
+            TRY_CUDA(cudaMemcpy(fd, frames_d + 4, sizeof(fd), cudaMemcpyDeviceToHost));
+            for (int m = 0; m < 2; m++) {
+                fd[m].stride = w * yp.bytes;
+                fd[m].stride_c = cw * yp.bytes;
+            }
+            TRY_CUDA(cudaMemcpy(frames_d + 4, fd, sizeof(fd), cudaMemcpyHostToDevice));
+            yuv_stride = w * yp.bytes;
+            yuv_stride_c = cw * yp.bytes;
+        }
         for (int m = 0; m < 2; m++) {
             const uint8_t* const* src = m == 0 ? s1 : s2;
             const int64_t* st = m == 0 ? st1 : st2;
             for (int c = 0; c < 3; c++) {
                 if (!src[c]) return E_BAD_POINTER;
-                const int64_t row = (c == 0 ? w : cw) * 2, rows = c == 0 ? h : ch;
+                const int64_t row = (c == 0 ? w : cw) * yp.bytes, rows = c == 0 ? h : ch;
                 if (st[c] < row) return E_BAD_POINTER;
                 uint8_t* dst = staging + (size_t)(m * 3 + c) * plane4;
                 if (st[c] == row)
@@ -192,6 +211,7 @@ struct Ssimu2Handle {
     Ssimu2Engine eng;
     HostPath io;
     bool host_io = true;
+    YuvParams yuv = yuv420p10_params();  // format of Vship_InYuv frames
     ~Ssimu2Handle() {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -206,6 +226,7 @@ struct ButterHandle {
     ButterEngine eng;
     HostPath io;
     bool host_io = true;
+    YuvParams yuv = yuv420p10_params();  // format of Vship_InYuv frames
     ~ButterHandle() {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -264,19 +285,22 @@ __global__ void probe_kernel(int* out) { *out = 4320984; }
 // ------------------------------------------------------------------------------------------
 // compute bodies
 
+// yuv_fixed: the Yuv420p10 entry points, whose format is fixed whatever the handler's setting
 int ssimu2_compute(int id, double* score, const uint8_t* s1[3], const uint8_t* s2[3], int64_t stride1,
-                   int64_t stride2, int intype, const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr) {
+                   int64_t stride2, int intype, const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr,
+                   bool yuv_fixed = false) {
     Ssimu2Handle* h = g_ssimu2.get(id);
     if (!h || !h->host_io) return E_BAD_HANDLER;
     if (!score) return E_BAD_POINTER;
     std::lock_guard<std::mutex> lk(h->io.mu);
     DeviceGuard dg(h->io.device);
     const int bps = intype == IN_FLOAT ? 4 : 2;
+    const YuvParams yp = yuv_fixed ? yuv420p10_params() : h->yuv;
     const FrameDesc* fd = nullptr;
-    int rc = intype == IN_YUV420P10 ? h->io.upload_yuv(s1, ystr1, s2, ystr2, h->eng.w, h->eng.h, &fd)
-                                    : h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
+    int rc = intype == IN_YUV ? h->io.upload_yuv(s1, ystr1, s2, ystr2, h->eng.w, h->eng.h, yp, &fd)
+                              : h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
     if (rc) return rc;
-    rc = h->eng.launch(fd, intype, 1, nullptr, h->io.stream);
+    rc = h->eng.launch(fd, intype, 1, nullptr, h->io.stream, &yp);
     if (rc) return rc;
     TRY_CUDA(cudaMemcpyAsync(h->io.result_h, h->eng.scores, sizeof(double), cudaMemcpyDeviceToHost, h->io.stream));
     TRY_CUDA(cudaStreamSynchronize(h->io.stream));
@@ -286,17 +310,18 @@ int ssimu2_compute(int id, double* score, const uint8_t* s1[3], const uint8_t* s
 
 int butter_compute(int id, double norms[3], const uint8_t* dstp, int64_t dststride, const uint8_t* s1[3],
                    const uint8_t* s2[3], int64_t stride1, int64_t stride2, int intype,
-                   const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr) {
+                   const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr, bool yuv_fixed = false) {
     ButterHandle* h = g_butter.get(id);
     if (!h || !h->host_io) return E_BAD_HANDLER;
     std::lock_guard<std::mutex> lk(h->io.mu);
     DeviceGuard dg(h->io.device);
     const int bps = intype == IN_FLOAT ? 4 : 2;
+    const YuvParams yp = yuv_fixed ? yuv420p10_params() : h->yuv;
     const FrameDesc* fd = nullptr;
-    int rc = intype == IN_YUV420P10 ? h->io.upload_yuv(s1, ystr1, s2, ystr2, h->eng.w, h->eng.h, &fd)
-                                    : h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
+    int rc = intype == IN_YUV ? h->io.upload_yuv(s1, ystr1, s2, ystr2, h->eng.w, h->eng.h, yp, &fd)
+                              : h->io.upload(s1, s2, stride1, stride2, h->eng.w, h->eng.h, bps, &fd);
     if (rc) return rc;
-    rc = h->eng.launch(fd, intype, 1, nullptr, h->io.stream);
+    rc = h->eng.launch(fd, intype, 1, nullptr, h->io.stream, &yp);
     if (rc) return rc;
     if (dstp) {
         const int64_t row = h->eng.w * 4;
@@ -490,7 +515,22 @@ Vship_Exception Vship_ComputeSSIMU2Uint16v2(Vship_SSIMU2Handler handler, double*
 Vship_Exception Vship_ComputeSSIMU2Yuv420p10(Vship_SSIMU2Handler handler, double* score, const uint8_t* srcp1[3],
                                              const int64_t stride1[3], const uint8_t* srcp2[3],
                                              const int64_t stride2[3]) {
-    return to_exc(ssimu2_compute(handler.id, score, srcp1, srcp2, 0, 0, IN_YUV420P10, stride1, stride2));
+    return to_exc(ssimu2_compute(handler.id, score, srcp1, srcp2, 0, 0, IN_YUV, stride1, stride2, true));
+}
+
+Vship_Exception Vship_ComputeSSIMU2Yuv(Vship_SSIMU2Handler handler, double* score, const uint8_t* srcp1[3],
+                                       const int64_t stride1[3], const uint8_t* srcp2[3], const int64_t stride2[3]) {
+    return to_exc(ssimu2_compute(handler.id, score, srcp1, srcp2, 0, 0, IN_YUV, stride1, stride2, false));
+}
+
+Vship_Exception Vship_SSIMU2SetYuvFormat(Vship_SSIMU2Handler handler, const Vship_YuvFormat* format) {
+    Ssimu2Handle* h = g_ssimu2.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    YuvParams p;
+    if (!format || !yuv_from_format(*format, h->eng.h, &p)) return Vship_BadPointer;
+    std::lock_guard<std::mutex> lk(h->io.mu);
+    h->yuv = p;
+    return Vship_NoError;
 }
 
 Vship_Exception Vship_SSIMU2ComputeDeviceAsync(Vship_SSIMU2Handler handler, const Vship_DeviceFrame* frames,
@@ -504,7 +544,7 @@ Vship_Exception Vship_SSIMU2ComputeDeviceAsync(Vship_SSIMU2Handler handler, cons
     static_assert(sizeof(Vship_DeviceFrame) == sizeof(FrameDesc), "frame descriptor layout");
     DeviceGuard dg(h->io.device);
     return to_exc(h->eng.launch(reinterpret_cast<const FrameDesc*>(frames), (int)input_type, npairs, scores_dev,
-                                (cudaStream_t)stream));
+                                (cudaStream_t)stream, &h->yuv));
 }
 
 uint64_t Vship_SSIMU2DeviceBytes(int width, int height, int max_pairs) {
@@ -550,7 +590,7 @@ Vship_Exception Vship_ButteraugliComputeDeviceAsync(Vship_ButteraugliHandler han
     if ((int)input_type < 0 || (int)input_type > 4) return Vship_BadPointer;
     DeviceGuard dg(h->io.device);
     cudaStream_t st = (cudaStream_t)stream;
-    int rc = h->eng.launch(reinterpret_cast<const FrameDesc*>(frames), (int)input_type, npairs, norms_dev, st);
+    int rc = h->eng.launch(reinterpret_cast<const FrameDesc*>(frames), (int)input_type, npairs, norms_dev, st, &h->yuv);
     if (rc) return to_exc(rc);
     if (distmaps_dev) {
         const size_t bytes = sizeof(float) * (size_t)h->eng.w * h->eng.h * npairs;
@@ -606,8 +646,26 @@ Vship_Exception Vship_ComputeButteraugliYuv420p10(Vship_ButteraugliHandler handl
                                                   const int64_t stride1[3], const uint8_t* srcp2[3],
                                                   const int64_t stride2[3]) {
     if (!norms) return Vship_BadPointer;
-    return to_exc(butter_compute(handler.id, norms, dstp, dststride, srcp1, srcp2, 0, 0, IN_YUV420P10, stride1,
-                                 stride2));
+    return to_exc(butter_compute(handler.id, norms, dstp, dststride, srcp1, srcp2, 0, 0, IN_YUV, stride1,
+                                 stride2, true));
+}
+
+Vship_Exception Vship_ComputeButteraugliYuv(Vship_ButteraugliHandler handler, double norms[3], const uint8_t* dstp,
+                                            int64_t dststride, const uint8_t* srcp1[3], const int64_t stride1[3],
+                                            const uint8_t* srcp2[3], const int64_t stride2[3]) {
+    if (!norms) return Vship_BadPointer;
+    return to_exc(butter_compute(handler.id, norms, dstp, dststride, srcp1, srcp2, 0, 0, IN_YUV, stride1,
+                                 stride2, false));
+}
+
+Vship_Exception Vship_ButteraugliSetYuvFormat(Vship_ButteraugliHandler handler, const Vship_YuvFormat* format) {
+    ButterHandle* h = g_butter.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    YuvParams p;
+    if (!format || !yuv_from_format(*format, h->eng.h, &p)) return Vship_BadPointer;
+    std::lock_guard<std::mutex> lk(h->io.mu);
+    h->yuv = p;
+    return Vship_NoError;
 }
 
 Vship_Exception Vship_ComputeButteraugliUint16v3(Vship_ButteraugliHandler handler, double norms[3],
@@ -652,6 +710,15 @@ Vship_Exception Vship_MultiComputeDeviceAsync(Vship_MultiHandler handler, int ns
                                  ssimu2_dev, butter_norms_dev, (cudaStream_t)stream));
 }
 
+Vship_Exception Vship_MultiSetYuvFormat(Vship_MultiHandler handler, const Vship_YuvFormat* f) {
+    MultiHandle* h = g_multi.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    if (!f) return Vship_BadPointer;
+    DeviceGuard dg(h->eng.device);
+    return to_exc(h->eng.set_yuv_format(f->bits, f->subsampling_w, f->subsampling_h, f->matrix, f->range,
+                                        f->chroma_location));
+}
+
 int Vship_MultiKnobs(Vship_MultiHandler handler, char* out_json, int len) {
     MultiHandle* h = g_multi.get(handler.id);
     const std::string s = h ? h->eng.knobs_json() : std::string("{}");
@@ -684,6 +751,14 @@ Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, int nres, const i
     if (rc) return to_exc(rc);
     handler->id = g_serve.put(std::move(h));
     return Vship_NoError;
+}
+
+Vship_Exception Vship_ServeSetYuvFormat(Vship_ServeHandler handler, const Vship_YuvFormat* f) {
+    ServeHandle* h = g_serve.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    if (!f) return Vship_BadPointer;
+    return to_exc(h->srv.set_yuv_format(f->bits, f->subsampling_w, f->subsampling_h, f->matrix, f->range,
+                                        f->chroma_location));
 }
 
 Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* q) {

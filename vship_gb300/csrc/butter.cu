@@ -112,7 +112,7 @@ __device__ __forceinline__ BScaleDev pick_scale(const BGeom& g, int s) { return 
 // grid (ceil(w/32), ceil(h/32), nimages), 256 threads; frames[image].
 template <int IT>
 __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __restrict__ frames,
-                                                            float* const* __restrict__ ib, BGeom g) {
+                                                            float* const* __restrict__ ib, BGeom g, YuvParams yp) {
     __shared__ float sm[3][32][33];
     const int img = blockIdx.z;
     const FrameDesc fd = frames[img];
@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
         const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ly;
         float v[3] = {0.f, 0.f, 0.f};
         if (gx < F.w && gy < F.h) {
-            load_rgb<IT>(fd, gx, gy, F.w, F.h, v[0], v[1], v[2]);
+            load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, v[0], v[1], v[2]);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 v[c] = to_linear_fast(v[c]);
@@ -1110,33 +1110,35 @@ size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs) {
            pairs;
 }
 
-int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st) {
+int ButterEngine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st,
+                         const YuvParams* yuv) {
     if (npairs <= 0 || npairs > max_pairs || !pimg_identity) return E_BAD_POINTER;
-    return launch_images(frames_dev, 2 * npairs, pimg_identity, npairs, intype, norms_out, distmap, st);
+    return launch_images(frames_dev, 2 * npairs, pimg_identity, npairs, intype, norms_out, distmap, st, yuv);
 }
 
 int ButterEngine::launch_images(const FrameDesc* frames_dev, int nimages, const int2* pimg, int npairs, int intype,
-                                double* norms_out, float* distmap_out, cudaStream_t st) {
+                                double* norms_out, float* distmap_out, cudaStream_t st, const YuvParams* yuv) {
     if (nimages <= 0 || nimages > max_images || npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
     return butter_enqueue(w, h, qnorm, intensity, ibase, frames_dev, nimages, pimg, npairs, intype, partials,
-                          norms_out ? norms_out : norms, distmap_out, st);
+                          norms_out ? norms_out : norms, distmap_out, st, yuv);
 }
 
 int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
                    int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
-                   float* distmap_out, cudaStream_t st) {
+                   float* distmap_out, cudaStream_t st, const YuvParams* yuv) {
     if (npairs <= 0 || nstage < 0) return E_BAD_POINTER;
+    const YuvParams yp = yuv ? *yuv : yuv420p10_params();
     const BGeom g = make_bgeom(w, h);
     const unsigned ni = (unsigned)nstage, np = (unsigned)npairs;
     if (ni) {
         dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), ni);
         ProfScope ps_("butter_decode", st);
         switch (intype) {
-            case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
-            case IN_UINT16: butter_decode_kernel<IN_UINT16><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
-            case IN_HALF: butter_decode_kernel<IN_HALF><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
-            case IN_YUV420P10: butter_decode_kernel<IN_YUV420P10><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
-            default: butter_decode_kernel<IN_FLOAT><<<gr, 256, 0, st>>>(frames_dev, ib, g); break;
+            case IN_UINT8: butter_decode_kernel<IN_UINT8><<<gr, 256, 0, st>>>(frames_dev, ib, g, yp); break;
+            case IN_UINT16: butter_decode_kernel<IN_UINT16><<<gr, 256, 0, st>>>(frames_dev, ib, g, yp); break;
+            case IN_HALF: butter_decode_kernel<IN_HALF><<<gr, 256, 0, st>>>(frames_dev, ib, g, yp); break;
+            case IN_YUV: butter_decode_kernel<IN_YUV><<<gr, 256, 0, st>>>(frames_dev, ib, g, yp); break;
+            default: butter_decode_kernel<IN_FLOAT><<<gr, 256, 0, st>>>(frames_dev, ib, g, yp); break;
         }
     }
     for (int s = 1; s >= 0; s--) {

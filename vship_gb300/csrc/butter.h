@@ -5,9 +5,9 @@
 #include <cstddef>
 #include <cstdint>
 
-namespace vship {
+#include "common.cuh"
 
-struct FrameDesc;
+namespace vship {
 
 // Per-scale plane set of the Butteraugli pipeline (all planes dense FP32, pitch == width).
 struct ButterScale {
@@ -44,11 +44,12 @@ public:
     // frames_dev: 2*npairs FrameDesc in device memory (pair-major: reference, distorted).
     // Writes the final distortion maps to this->distmap and {Qnorm, 3-norm, inf-norm} to
     // norms_out (device, 3 doubles per pair) or to this->norms when norms_out is null.
-    int launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st);
+    int launch(const FrameDesc* frames_dev, int intype, int npairs, double* norms_out, cudaStream_t st,
+               const YuvParams* yuv = nullptr);
     // frames_dev: nimages FrameDesc (device); pimg: npairs (reference, distorted) image indices
     // (device); distmap_out: null or npairs maps.
     int launch_images(const FrameDesc* frames_dev, int nimages, const int2* pimg, int npairs, int intype,
-                      double* norms_out, float* distmap_out, cudaStream_t st);
+                      double* norms_out, float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr);
     static size_t device_bytes(int64_t w, int64_t h, int pairs);
     static size_t image_bytes(int64_t w, int64_t h);
 };
@@ -60,9 +61,10 @@ size_t butter_image_floats(int64_t w, int64_t h);
 int butter_norm_tiles(int64_t w, int64_t h);
 // ib: device table of image workspaces; images [0, nstage) run their own stage (frames_dev[i]
 // is image i's frame), then every pair of pimg (indices into ib) runs the pair stage. partials:
-// npairs x 3 x norm_tiles floats; norms_out: npairs x 3 doubles; distmap_out: null or npairs maps.
+// npairs x 3 x norm_tiles floats; norms_out: npairs x 3 doubles; distmap_out: null or npairs maps;
+// yuv: format of IN_YUV frames (null: 10-bit 4:2:0 BT.709 limited, left siting).
 int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
                    int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
-                   float* distmap_out, cudaStream_t st);
+                   float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr);
 
 }  // namespace vship

@@ -91,6 +91,7 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
         pair_cap += max_pairs[r];
     }
     if (src_cap <= 0 || pair_cap <= 0) return E_BAD_POINTER;
+    for (int r = 0; r < nres; r++) yuv_r[r] = yuv420p10_params();
     if (tune_cache_path && *tune_cache_path)
         tune_path = tune_cache_path;
     else if (const char* e = getenv("VSHIP_TUNE_CACHE"))
@@ -331,6 +332,7 @@ void MultiEngine::fill_images(int nsrc, const FrameDesc* src, int npairs, const 
             Ssimu2MultiImage& I = s_imgs_h[i];
             I.geom = r;
             I.fd = src[i];
+            I.yp = yuv_r[r];
             I.f32 = s_src[r] + src_slot[i] * plane3;
             I.d16 = nullptr;
             I.ref = nullptr;
@@ -341,6 +343,7 @@ void MultiEngine::fill_images(int nsrc, const FrameDesc* src, int npairs, const 
             Ssimu2MultiImage& I = s_imgs_h[nsrc + j];
             I.geom = r;
             I.fd = cand[j];
+            I.yp = yuv_r[r];
             if (fp16) {
                 I.f32 = nullptr;
                 I.d16 = static_cast<__half*>(s_cand[r]) + cand_slot[j] * plane3;
@@ -376,7 +379,7 @@ int MultiEngine::enqueue(int npairs, cudaStream_t st) {
     if (flags & MULTI_BUTTERAUGLI) {
         for (const BChunk& c : b_chunks) {
             rc = b_eng[c.res].launch_images(b_frames_d + c.img_off, c.nimg, b_pimg_d + c.pair_off, c.npairs,
-                                            plan_intype, b_norms_d + 3 * c.pair_off, nullptr, st);
+                                            plan_intype, b_norms_d + 3 * c.pair_off, nullptr, st, &yuv_r[c.res]);
             if (rc) return rc;
         }
         multi_scatter_norms_kernel<<<(unsigned)ceil_div(3 * npairs, 256), 256, 0, st>>>(
@@ -495,6 +498,18 @@ int MultiEngine::autotune(int npairs, cudaStream_t st) {
     return upload_items(st);
 }
 
+int MultiEngine::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc) {
+    YuvParams p[kMaxRes];
+    for (int r = 0; r < nres; r++)
+        if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r])) return E_BAD_POINTER;
+    for (int r = 0; r < nres; r++) yuv_r[r] = p[r];
+    if (gexec) {  // the Butteraugli launches carry the format as a kernel argument
+        cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+    }
+    return E_OK;
+}
+
 std::string MultiEngine::knobs_json() const {
     char buf[160];
     snprintf(buf, sizeof(buf), "{\"grid_per_sm\": %d, \"order\": %d, \"source\": \"%s\"}", knobs.grid_per_sm,
@@ -508,7 +523,7 @@ int MultiEngine::compute(int nsrc, const FrameDesc* src, const int* src_res, int
                          const int* cand_src, int intype, double* ssimu2_dev, double* butter_dev, cudaStream_t st) {
     if (nsrc <= 0 || npairs <= 0 || !src || !src_res || !cand || !cand_src) return E_BAD_POINTER;
     if (nsrc > src_cap || npairs > pair_cap) return E_BAD_POINTER;
-    if (intype < 0 || intype > IN_YUV420P10) return E_BAD_POINTER;
+    if (intype < 0 || intype > IN_YUV) return E_BAD_POINTER;
     if ((flags & MULTI_SSIMU2) && !ssimu2_dev) return E_BAD_POINTER;
     if ((flags & MULTI_BUTTERAUGLI) && !butter_dev) return E_BAD_POINTER;
 

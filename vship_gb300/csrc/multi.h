@@ -62,6 +62,8 @@ public:
     // src/cand: HOST arrays of frame descriptors pointing at device planes.
     int compute(int nsrc, const FrameDesc* src, const int* src_res, int npairs, const FrameDesc* cand,
                 const int* cand_src, int intype, double* ssimu2_dev, double* butter_dev, cudaStream_t st);
+    // Format of IN_YUV frames for every resolution (make_yuv_params; matrix 2 resolves per height).
+    int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc);
     // The knobs in use as JSON ({"grid_per_sm": g, "order": o, "source": "default|cache|tuned"}).
     std::string knobs_json() const;
     static size_t device_bytes(int nres, const int* widths, const int* heights, const int* max_sources,
@@ -96,6 +98,8 @@ private:
     int2* b_pimg_d = nullptr;         // per grouped pair: (source, candidate) image inside its chunk
     double* b_norms_d = nullptr;      // grouped norms, then the caller-ordered copy
     int* b_perm_d = nullptr;          // grouped pair -> caller's pair index
+
+    YuvParams yuv_r[kMaxRes];
 
     // current layout
     bool plan_valid = false;

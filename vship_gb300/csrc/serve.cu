@@ -25,7 +25,7 @@ static size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 int Server::create(int nres_, const int* widths, const int* heights, int intype_, uint64_t admission_bytes,
                    uint64_t cache_bytes, int max_batch_pairs_, int flags_, int qnorm_, float intensity_) {
     if (nres_ <= 0 || nres_ > kMaxRes || !widths || !heights) return E_BAD_POINTER;
-    if (intype_ < 0 || intype_ > IN_YUV420P10 || max_batch_pairs_ <= 0 || admission_bytes == 0) return E_BAD_POINTER;
+    if (intype_ < 0 || intype_ > IN_YUV || max_batch_pairs_ <= 0 || admission_bytes == 0) return E_BAD_POINTER;
     nres = nres_;
     intype = intype_;
     flags = flags_;
@@ -41,6 +41,7 @@ int Server::create(int nres_, const int* widths, const int* heights, int intype_
         sgeom[r] = make_ssimu2_geom(rw[r], rh[r]);
         bimg_floats[r] = butter_image_floats(rw[r], rh[r]);
         bnorm_tiles[r] = butter_norm_tiles(rw[r], rh[r]);
+        yuv_r[r] = yuv420p10_params();
     }
     VSHIP_CUDA_TRY(cudaGetDevice(&device));
     cudaDeviceProp prop;
@@ -99,6 +100,15 @@ int Server::submit(ServeReq* r) {
         n_submitted++;
     }
     cv.notify_all();
+    return E_OK;
+}
+
+int Server::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc) {
+    YuvParams p[kMaxRes];
+    for (int r = 0; r < nres; r++)
+        if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r])) return E_BAD_POINTER;
+    std::lock_guard<std::mutex> g(mu);
+    for (int r = 0; r < nres; r++) yuv_r[r] = p[r];
     return E_OK;
 }
 
@@ -221,9 +231,11 @@ int Server::launch(Batch* b) {
     std::vector<char> stage(nreq, 0);
     std::vector<void*> temp, evicted;
     std::vector<SourceKey> inserted;
+    YuvParams yuv[kMaxRes];
     int rc = E_OK;
     {
         std::lock_guard<std::mutex> g(mu);
+        for (int r = 0; r < nres; r++) yuv[r] = yuv_r[r];
         for (int i = 0; i < nreq && !rc; i++) {
             ServeReq* r = b->reqs[i];
             const size_t bytes = r->metric == SERVE_SSIMU2 ? sizeof(float) * 3 * (size_t)sgeom[r->res].plane_elems
@@ -375,7 +387,7 @@ int Server::launch(Batch* b) {
         for (int i = 0; i < nreq; i++) {  // sources whose pyramid this batch builds
             ServeReq* r = b->reqs[i];
             if (r->metric != SERVE_SSIMU2 || !stage[i]) continue;
-            imgs[ni] = Ssimu2MultiImage{r->res, r->src, src[i], nullptr, nullptr};
+            imgs[ni] = Ssimu2MultiImage{r->res, r->src, yuv[r->res], src[i], nullptr, nullptr};
             add_tiles(ni, r->res, ps);
             ni++;
         }
@@ -388,8 +400,9 @@ int Server::launch(Batch* b) {
             for (size_t c = 0; c < r->cands.size(); c++) {
                 uint8_t* cp = block + cand_off[i] + c * plane3 * celem;
                 float* part = reinterpret_cast<float*>(block + part_off[i]) + c * 18 * (size_t)G.tiles_total;
-                imgs[ni] = fp16 ? Ssimu2MultiImage{r->res, r->cands[c], nullptr, cp, src[i]}
-                                : Ssimu2MultiImage{r->res, r->cands[c], reinterpret_cast<float*>(cp), nullptr, nullptr};
+                imgs[ni] = fp16 ? Ssimu2MultiImage{r->res, r->cands[c], yuv[r->res], nullptr, cp, src[i]}
+                                : Ssimu2MultiImage{r->res, r->cands[c], yuv[r->res], reinterpret_cast<float*>(cp),
+                                                   nullptr, nullptr};
                 add_tiles(ni, r->res, pc);
                 ni++;
                 pairs[npair] = Ssimu2MultiPair{r->res, src[i], cp, part, dres + ro};
@@ -455,7 +468,8 @@ int Server::launch(Batch* b) {
         rc = butter_enqueue(rw[G.res], rh[G.res], qnorm, intensity, reinterpret_cast<float* const*>(dtab + G.t_ib),
                             reinterpret_cast<const FrameDesc*>(dtab + G.t_fr), G.nstage,
                             reinterpret_cast<const int2*>(dtab + G.t_pi), G.npairs, intype,
-                            reinterpret_cast<float*>(block + G.part), dres + b->out_off[G.reqs[0]], nullptr, st);
+                            reinterpret_cast<float*>(block + G.part), dres + b->out_off[G.reqs[0]], nullptr, st,
+                            &yuv[G.res]);
     }
     if (!rc && cudaMemcpyAsync(h + b->res_off, dres, res_doubles * sizeof(double), cudaMemcpyDeviceToHost, st) !=
                    cudaSuccess)

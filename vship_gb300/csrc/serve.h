@@ -56,6 +56,8 @@ public:
                uint64_t cache_bytes, int max_batch_pairs, int flags, int qnorm, float intensity);
     int submit(ServeReq* r);  // takes ownership (deleted after completion)
     int poll(ServeDone* out, int max, double timeout_s);
+    // Format of IN_YUV frames for every resolution (make_yuv_params; matrix 2 resolves per height).
+    int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc);
     int drain();
     std::string stats_json();
     void destroy();
@@ -72,12 +74,13 @@ private:
         int status = E_OK;
     };
 
-    int nres = 0, intype = IN_YUV420P10, flags = 0, qnorm = 2, max_batch_pairs = 256, sms = 0, stats_grid = 0;
+    int nres = 0, intype = IN_YUV, flags = 0, qnorm = 2, max_batch_pairs = 256, sms = 0, stats_grid = 0;
     float intensity = 203.f;
     int64_t rw[kMaxRes]{}, rh[kMaxRes]{};
     Ssimu2Geom sgeom[kMaxRes]{};
     Ssimu2Geom* sgeom_d = nullptr;
     size_t bimg_floats[kMaxRes]{};
+    YuvParams yuv_r[kMaxRes];
     int bnorm_tiles[kMaxRes]{};
 
     cudaStream_t st = nullptr;

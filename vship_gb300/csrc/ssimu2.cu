@@ -118,8 +118,8 @@ __device__ __forceinline__ void pyr_store(const PyrOut& out, int64_t pe, int64_t
 }
 
 template <int IT, bool DELTA>
-__device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const PyrOut& out, const Ssimu2Geom& g, int bx,
-                                             int by) {
+__device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParams& yp, const PyrOut& out,
+                                             const Ssimu2Geom& g, int bx, int by) {
     __shared__ float smA[3 * 32 * 33];
     __shared__ float smB[3 * 16 * 17];
     const int64_t pe = g.plane_elems;
@@ -132,7 +132,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const PyrOut& 
             const int gx = bx * 32 + tx, gy = by * 32 + ly;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f;
             if (gx < L.w && gy < L.h) {
-                load_rgb<IT>(fd, gx, gy, L.w, L.h, v0, v1, v2);
+                load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, v0, v1, v2);
                 v0 = to_linear_fast(v0);
                 v1 = to_linear_fast(v1);
                 v2 = to_linear_fast(v2);
@@ -189,11 +189,11 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const PyrOut& 
 // grid (tiles_x0, tiles_y0, 2*npairs)
 template <int IT>
 __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
-                                                             float* __restrict__ pyr, Ssimu2Geom g) {
+                                                             float* __restrict__ pyr, Ssimu2Geom g, YuvParams yp) {
     const int img = blockIdx.z;  // pair*2 + image
     const FrameDesc fd = frames[img];
     PyrOut out{pyr + (int64_t)img * 3 * g.plane_elems, nullptr, nullptr};
-    pyramid_tile<IT, false>(fd, out, g, blockIdx.x, blockIdx.y);
+    pyramid_tile<IT, false>(fd, yp, out, g, blockIdx.x, blockIdx.y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -544,7 +544,7 @@ __global__ void __launch_bounds__(256) ssimu2_multi_pyramid_kernel(const Ssimu2M
     const int4 it = items[blockIdx.x];
     const Ssimu2MultiImage im = imgs[it.x];
     const PyrOut out{im.f32, static_cast<__half*>(im.d16), im.ref};
-    pyramid_tile<IT, DELTA>(im.fd, out, geoms[im.geom], it.y, it.z);
+    pyramid_tile<IT, DELTA>(im.fd, im.yp, out, geoms[im.geom], it.y, it.z);
 }
 
 // persistent: CTA b takes items b, b + gridDim.x, ...; items {pair, tile}
@@ -631,17 +631,19 @@ size_t Ssimu2Engine::device_bytes(int64_t w, int64_t h, int pairs) {
            sizeof(double) * pairs;
 }
 
-int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st) {
+int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st,
+                         const YuvParams* yuv) {
     if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
+    const YuvParams yp = yuv ? *yuv : yuv420p10_params();
     dim3 g1((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), (unsigned)(2 * npairs));
     {
     ProfScope ps("ssimu2_pyramid", st);
     switch (intype) {
-        case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
-        case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
-        case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
-        case IN_YUV420P10: ssimu2_pyramid_kernel<IN_YUV420P10><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
-        default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_dev, pyr, geom); break;
+        case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_dev, pyr, geom, yp); break;
+        case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_dev, pyr, geom, yp); break;
+        case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_dev, pyr, geom, yp); break;
+        case IN_YUV: ssimu2_pyramid_kernel<IN_YUV><<<g1, 256, 0, st>>>(frames_dev, pyr, geom, yp); break;
+        default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_dev, pyr, geom, yp); break;
     }
     }
     dim3 g2((unsigned)geom.tiles_total, (unsigned)npairs);
@@ -678,16 +680,17 @@ __global__ void ssimu2_store_frames_kernel(FrameDesc a, FrameDesc b, FrameDesc* 
 
 int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intype, const Ssimu2Geom& geom,
                           FrameDesc* frames_scratch, float* scratch, double* out_score, cudaStream_t st) {
+    const YuvParams yp = yuv420p10_params();
     float* pyr = scratch;
     float* partials = scratch + (size_t)geom.plane_elems * 6;
     ssimu2_store_frames_kernel<<<1, 1, 0, st>>>(ref, dist, frames_scratch);
     dim3 g1((unsigned)ceil_div(geom.lv[0].w, 32), (unsigned)ceil_div(geom.lv[0].h, 32), 2u);
     switch (intype) {
-        case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
-        case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
-        case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
-        case IN_YUV420P10: ssimu2_pyramid_kernel<IN_YUV420P10><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
-        default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom); break;
+        case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
+        case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
+        case IN_HALF: ssimu2_pyramid_kernel<IN_HALF><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
+        case IN_YUV: ssimu2_pyramid_kernel<IN_YUV><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
+        default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
     }
     ssimu2_stats_kernel<<<dim3((unsigned)geom.tiles_total, 1u), 256, kStatsSmem, st>>>(pyr, partials, geom);
     ssimu2_finalize_kernel<<<1, 256, 0, st>>>(partials, out_score, geom);
@@ -722,8 +725,8 @@ static void launch_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items
         case IN_UINT8: ssimu2_multi_pyramid_kernel<IN_UINT8, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
         case IN_UINT16: ssimu2_multi_pyramid_kernel<IN_UINT16, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
         case IN_HALF: ssimu2_multi_pyramid_kernel<IN_HALF, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
-        case IN_YUV420P10:
-            ssimu2_multi_pyramid_kernel<IN_YUV420P10, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms);
+        case IN_YUV:
+            ssimu2_multi_pyramid_kernel<IN_YUV, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms);
             break;
         default: ssimu2_multi_pyramid_kernel<IN_FLOAT, DELTA><<<n, 256, 0, st>>>(imgs, items, geoms); break;
     }

@@ -41,7 +41,9 @@ public:
     void destroy();
     // frames_dev: 2*npairs FrameDesc in device memory (pair-major: reference, distorted).
     // Scores land in out_scores (device) or in this->scores when out_scores is null.
-    int launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st);
+    // yuv: the Y'CbCr format of IN_YUV frames (null: 10-bit 4:2:0 BT.709 limited, left siting).
+    int launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st,
+               const YuvParams* yuv = nullptr);
     static size_t device_bytes(int64_t w, int64_t h, int pairs);
 };
 
@@ -60,6 +62,7 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
 struct Ssimu2MultiImage {
     int geom;
     FrameDesc fd;
+    YuvParams yp;  // IN_YUV frames
     float* f32;
     void* d16;
     const float* ref;

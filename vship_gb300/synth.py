@@ -178,6 +178,98 @@ def yuv420p10_to_rgb(yuv, dtype=torch.float32) -> torch.Tensor:
     return rgb.to(dtype)
 
 
+# ------------------------------------------------------------------------------------------
+# Y'CbCr of any depth / subsampling / matrix / range / chroma siting
+
+_MATRICES = {1: (0.2126, 0.0722), 4: (0.30, 0.11), 5: (0.299, 0.114), 6: (0.299, 0.114), 7: (0.212, 0.087),
+             9: (0.2627, 0.0593)}
+
+
+def _range(bits: int, full: bool):
+    sc = float(1 << (bits - 8))
+    if full:
+        mx = float((1 << bits) - 1)
+        return 0.0, mx, float(1 << (bits - 1)), mx
+    return 16.0 * sc, 219.0 * sc, 128.0 * sc, 224.0 * sc
+
+
+def _siting(loc: int):
+    """(horizontal, vertical) chroma siting in luma half-samples: 0 even positions, 1 halfway,
+    2 odd positions (left, center, top-left, top, bottom-left, bottom)."""
+    sx = 1 if loc in (1, 3, 5) else 0
+    sy = 1 if loc <= 1 else (0 if loc <= 3 else 2)
+    return sx, sy
+
+
+def _upsample_axis(c: torch.Tensor, n: int, ss: int, s: int, axis: int) -> torch.Tensor:
+    if not ss:
+        return c
+    m = c.shape[axis]
+    p = torch.arange(n, dtype=torch.float64, device=c.device)
+    pos = (2 * p - s) / 4.0  # chroma sample k sits at luma position 2k + s/2
+    k0f = torch.floor(pos)
+    f = pos - k0f
+    k0 = torch.clamp(k0f, 0, m - 1).long()
+    k1 = torch.clamp(k0f + 1, 0, m - 1).long()
+    a, b = c.index_select(axis, k0), c.index_select(axis, k1)
+    shape = [1, 1]
+    shape[axis] = n
+    f = f.view(shape)
+    return a * (1 - f) + b * f
+
+
+def yuv_to_rgb(yuv, bits=10, ssw=1, ssh=1, matrix=1, full=False, loc=0, dtype=torch.float32) -> torch.Tensor:
+    """Y'CbCr planes of the given format -> full-range R'G'B' (3, h, w) in [0, 1], in FP64: chroma
+    upsampled bilinearly at its siting (edge samples clamped), the matrix (H.273 id; 2 = BT.709
+    above 650 rows, BT.470BG below) and range applied, clamped."""
+    Y, U, V = [p.to(torch.float64) for p in yuv]
+    h, w = Y.shape
+    if matrix == 2:
+        matrix = 1 if h > 650 else 5
+    kr, kb = _MATRICES[matrix]
+    kg = 1.0 - kr - kb
+    yo, yd, co, cd = _range(bits, full)
+    sx, sy = _siting(loc)
+    ups = lambda c: _upsample_axis(_upsample_axis(c, w, ssw, sx, 1), h, ssh, sy, 0)
+    y = (Y - yo) / yd
+    cb = (ups(U) - co) / cd
+    cr = (ups(V) - co) / cd
+    r = y + 2.0 * (1.0 - kr) * cr
+    b = y + 2.0 * (1.0 - kb) * cb
+    g = y - (2.0 * (1.0 - kb) * kb / kg) * cb - (2.0 * (1.0 - kr) * kr / kg) * cr
+    return torch.stack([r, g, b]).clamp_(0.0, 1.0).to(dtype)
+
+
+def yuv_frames(h: int, w: int, t: int, bits=10, ssw=1, ssh=1, full=False, seed: int = 7, distortion="dct",
+               device="cpu"):
+    """(reference, distorted) Y'CbCr frames (int32 planes) of the given depth, subsampling and
+    range: the grating model of yuv420p10_source at that depth, distorted by 8x8 block-DCT
+    quantisation or by blur + noise, clipped to the range's codes."""
+    rs = np.random.default_rng([seed, bits, ssw, ssh, int(full)])
+    gen = torch.Generator(device=device).manual_seed(seed * 7919 + t)
+    sc = float(1 << (bits - 8))
+    top = (1 << bits) - 1
+    ylo, yhi = (0, top) if full else (int(16 * sc), int(235 * sc))
+    clo, chi = (0, top) if full else (int(16 * sc), int(240 * sc))
+    ch, cw = ((h + 1) // 2 if ssh else h), ((w + 1) // 2 if ssw else w)
+    yv = _gratings(h, w, rs, 8, 0.6 * sc, 0.05 * t, device) + 125.0 * sc
+    yv += torch.rand((h, w), generator=gen, device=device, dtype=torch.float64) * 16 * sc - 8 * sc
+    planes = [torch.clamp(torch.round(yv), ylo, yhi).to(torch.int32)]
+    for _ in range(2):
+        c = _gratings(ch, cw, rs, 8, 0.5 * sc, 0.05 * t, device) + 128.0 * sc
+        c += torch.rand((ch, cw), generator=gen, device=device, dtype=torch.float64) * 8 * sc - 4 * sc
+        planes.append(torch.clamp(torch.round(c), clo, chi).to(torch.int32))
+    if distortion == "dct":
+        step = rs.uniform(4.0, 32.0) * sc
+        dist = [block_dct_quantise(planes[0], step, ylo, yhi)] + \
+               [block_dct_quantise(p, 2 * step, clo, chi) for p in planes[1:]]
+    else:
+        sigma, ns = rs.uniform(0.5, 2.0), rs.uniform(1.0, 6.0) * sc
+        dist = [gaussian_blur_noise(planes[0], sigma, ns, ylo, yhi, gen)] + \
+               [gaussian_blur_noise(p, sigma, ns, clo, chi, gen) for p in planes[1:]]
+    return tuple(planes), tuple(dist)
+
+
 def rgb_float_pair(h: int, w: int, t: int, seed: int = 7, distortion: str = "dct", device="cpu"):
     """Float32 (3, h, w) R'G'B' reference/distorted planes for pair t of a YUV sequence."""
     ref, dist = yuv420p10_frames(h, w, t, seed, distortion, device)
