@@ -1,6 +1,7 @@
 """The FFVship-compatible command-line tool (vship_gb300/ffvship): argument handling, YUV4MPEG2
-input, frame selection, JSON output (doc/FFVship.md format) and agreement with the library's
-4:2:0 entry points."""
+input (4:2:0 / 4:2:2 / 4:4:4, 8-16 bit, sitings), frame selection, JSON output (doc/FFVship.md
+format) and agreement with the library's Y'CbCr entry points in the file's format (matrix by
+height, as the reference guesses for files without one)."""
 import json
 import os
 import subprocess
@@ -40,11 +41,20 @@ def test_missing_files_fail(cli):
     assert r.returncode == 1 and "cannot open" in r.stderr
 
 
-def test_rejects_non_420(cli, tmp_path):
+def test_rejects_unsupported_colorspace(cli, tmp_path):
     p = tmp_path / "a.y4m"
-    p.write_bytes(b"YUV4MPEG2 W8 H8 F24:1 C444\nFRAME\n" + bytes(8 * 8 * 3))
+    p.write_bytes(b"YUV4MPEG2 W8 H8 F24:1 Cmono\nFRAME\n" + bytes(8 * 8))
     r = run("-s", p, "-e", p)
-    assert r.returncode == 1 and "4:2:0" in r.stderr
+    assert r.returncode == 1 and "unsupported" in r.stderr
+
+
+def test_rejects_differing_formats(cli, tmp_path):
+    a, b = tmp_path / "a.y4m", tmp_path / "b.y4m"
+    synth.write_y4m(str(a), [synth.yuv420p10_source(8, 8, 0, 1)], 8, 8)
+    f = synth.yuv_frames(8, 8, 0, 10, 0, 0)[0]
+    synth.write_y4m(str(b), [f], 8, 8, 10, chroma="444")
+    r = run("-s", a, "-e", b)
+    assert r.returncode == 1 and "differ" in r.stderr
 
 
 def test_unknown_metric(cli, tmp_path):
@@ -54,33 +64,40 @@ def test_unknown_metric(cli, tmp_path):
     assert r.returncode == 1 and "Unknown metric" in r.stderr
 
 
-def _clip(tmp_path, h, w, n, bits=10):
+def _clip(tmp_path, h, w, n, bits=10, chroma="420", siting=""):
+    """n frame pairs written as .y4m, and the same planes as arrays of the file's sample type."""
+    ssw, ssh = {"420": (1, 1), "422": (1, 0), "444": (0, 0)}[chroma]
     src, enc = [], []
     for t in range(n):
-        r, d = synth.yuv420p10_frames(h, w, t, seed=13, distortion="dct")
-        if bits == 8:  # 8-bit limited-range codes: 10-bit value / 4
-            r = tuple(np.asarray(p) // 4 for p in r)
-            d = tuple(np.asarray(p) // 4 for p in d)
+        r, d = synth.yuv_frames(h, w, t, bits, ssw, ssh, False, seed=13, distortion="dct")
         src.append(r)
         enc.append(d)
-    ps, pe = tmp_path / f"src{bits}.y4m", tmp_path / f"enc{bits}.y4m"
-    synth.write_y4m(str(ps), src, w, h, bits)
-    synth.write_y4m(str(pe), enc, w, h, bits)
-    up = lambda f: [np.ascontiguousarray(np.asarray(p).astype(np.uint16) * (4 if bits == 8 else 1)) for p in f]
-    return ps, pe, [up(f) for f in src], [up(f) for f in enc]
+    ps, pe = tmp_path / f"src{bits}{chroma}.y4m", tmp_path / f"enc{bits}{chroma}.y4m"
+    synth.write_y4m(str(ps), src, w, h, bits, chroma=chroma, siting=siting)
+    synth.write_y4m(str(pe), enc, w, h, bits, chroma=chroma, siting=siting)
+    dt = np.uint8 if bits == 8 else np.uint16
+    arr = lambda f: [np.ascontiguousarray(np.asarray(p).astype(dt)) for p in f]
+    return ps, pe, [arr(f) for f in src], [arr(f) for f in enc]
+
+
+def _fmt(vlib, bits, chroma="420", loc=0):
+    ss = {"420": (1, 1), "422": (1, 0), "444": (0, 0)}[chroma]
+    return vlib.yuv_format(bits, ss, 2, False, loc)
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bits", [10, 8])
-def test_ssimu2_json_matches_library(cli, vlib, tmp_path, bits):
+@pytest.mark.parametrize("bits,chroma,siting,loc", [(10, "420", "", 0), (8, "420", "", 1), (8, "420", "mpeg2", 0),
+                                                    (12, "422", "", 0), (16, "444", "", 0), (8, "420", "paldv", 2)])
+def test_ssimu2_json_matches_library(cli, vlib, tmp_path, bits, chroma, siting, loc):
     h, w, n = 72, 96, 5
-    ps, pe, src, enc = _clip(tmp_path, h, w, n, bits)
+    ps, pe, src, enc = _clip(tmp_path, h, w, n, bits, chroma, siting)
     out = tmp_path / "s.json"
     r = run("-s", ps, "-e", pe, "-m", "SSIMULACRA2", "--json", out, "-g", 2, "-t", 2)
     assert r.returncode == 0, r.stderr
     got = json.loads(out.read_text())
     with vlib.SSIMU2Handler(w, h) as hd:
-        want = [hd.compute_yuv420p10(a, b) for a, b in zip(src, enc)]
+        hd.set_yuv_format(_fmt(vlib, bits, chroma, loc))
+        want = [hd.compute_yuv(a, b) for a, b in zip(src, enc)]
     assert [len(x) for x in got] == [1] * n
     assert np.allclose([x[0] for x in got], want, atol=1e-5)
     assert "SSIMULACRA2" in r.stdout and "Average" in r.stdout
@@ -96,7 +113,8 @@ def test_butteraugli_selection_and_offset(cli, vlib, tmp_path):
     assert r.returncode == 0, r.stderr
     got = json.loads(out.read_text())
     with vlib.ButteraugliHandler(w, h, 3, 120.0) as hd:
-        want = [hd.compute_yuv420p10(src[s], enc[s - 1]) for s in (1, 3, 5)]
+        hd.set_yuv_format(_fmt(vlib, 10))
+        want = [hd.compute_yuv(src[s], enc[s - 1]) for s in (1, 3, 5)]
     assert len(got) == 3
     for g, wv in zip(got, want):
         assert np.allclose(g, wv, rtol=1e-5)
@@ -116,5 +134,6 @@ def test_crop_and_live_output(cli, vlib, tmp_path):
     crop = lambda f: [np.ascontiguousarray(f[0][8:, 4:]), np.ascontiguousarray(f[1][4:, 2:]),
                       np.ascontiguousarray(f[2][4:, 2:])]
     with vlib.SSIMU2Handler(w - 4, h - 8) as hd:
+        hd.set_yuv_format(_fmt(vlib, 10))
         for i in range(n):
-            assert abs(got[i] - hd.compute_yuv420p10(crop(src[i]), crop(enc[i]))) < 1e-5
+            assert abs(got[i] - hd.compute_yuv(crop(src[i]), crop(enc[i]))) < 1e-5

@@ -96,7 +96,7 @@ struct BScaleDev {
 struct BGeom {
     BScaleDev s[2];  // 0 = full, 1 = half
     int64_t img_floats;
-    int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x8) at full scale
+    int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x32) at full scale
 };
 
 // ib[img] = that image's workspace (both scales); the launch's image list indexes it
@@ -655,7 +655,7 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 constexpr int DF_RAW = DF_IH * DF_IW;
 constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW) * 4;
 
-__global__ void __launch_bounds__(256, 2) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
+__global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
                                                              BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* Dt = sm + 4 * DF_RAW;
@@ -815,6 +815,13 @@ __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* const* 
     }
 }
 
+// One reciprocal and a residual correction (Markstein): num / den to within rounding.
+__device__ __forceinline__ float div_fast(float num, float den) {
+    const float r = __frcp_rn(den);
+    const float q = num * r;
+    return fmaf(fmaf(-q, den, num), r, q);
+}
+
 // combineMasks.hpp:3-19
 __device__ __forceinline__ float mask_common(float c) {
     constexpr DConst kK = dconst(1.0 / (double)(0.79079917404f * 17.83f));
@@ -828,10 +835,10 @@ __device__ __forceinline__ float mask_common(float c) {
     return r * r;
 }
 __device__ __forceinline__ float mask_y(float delta) {
-    return mask_common(2.5485944793f / ((0.451936922203f * delta) + 0.829591754942f));
+    return mask_common(div_fast(2.5485944793f, (0.451936922203f * delta) + 0.829591754942f));
 }
 __device__ __forceinline__ float mask_dc_y(float delta) {
-    return mask_common(0.505054525019f / ((3.87449418804f * delta) + 0.20025578522f));
+    return mask_common(div_fast(0.505054525019f, (3.87449418804f * delta) + 0.20025578522f));
 }
 // maskPsycho.hpp:42-55
 __device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float& m2) {
@@ -850,54 +857,77 @@ __device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float&
 }
 
 // Fuzzy erosion + diffmap; FINAL also folds in the half-scale map, stores the distortion map
-// (when distmap is not null) and emits norm partials. grid (ceil(w/32), ceil(h/8), npairs),
-// block (32, 8).
+// (when distmap is not null) and emits norm partials. grid (ceil(w/32), ceil(h/32), npairs),
+// 256 threads: thread (tx, ty) = (tid % 32, tid / 32) makes column x0 + tx, rows y0 + ty + 8k
+// (k < 4). The blurred mask
+// tile and its 3-px halo are staged in shared memory; neighbours outside the image are +inf,
+// which store_min3 ignores, as the reference skips them (maskPsycho.hpp:57-110).
+constexpr int DM_TW = 32, DM_TH = 32, DM_HX = 4, DM_HY = 3;
+constexpr int DM_IW = DM_TW + 2 * DM_HX, DM_IH = DM_TH + 2 * DM_HY;  // 40 x 38
+
 template <bool FINAL>
 __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
                                                              BGeom g, int s, float* __restrict__ distmap,
                                                              float* __restrict__ partials, float qnorm) {
+    __shared__ __align__(16) float bt[DM_IH * DM_IW];
     const int pair = blockIdx.z;
     const int i1 = pimg[pair].y;
     const BScaleDev S = pick_scale(g, s);
-    const int x = blockIdx.x * 32 + threadIdx.x, y = blockIdx.y * 8 + threadIdx.y;
+    const int x0 = blockIdx.x * DM_TW, y0 = blockIdx.y * DM_TH;
+    // 1-D block of 256 (stage_rows distributes chunks over threadIdx.x)
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const float* b0 = iplane(ib, g, S, i1, Q_B0);
+    stage_rows<256>(bt, DM_IW, b0, S.p, S.w, S.h, x0 - DM_HX, y0 - DM_HY, DM_IH, DM_IW / 4);
+    cp_async_commit();
+    cp_async_wait<0>();
+    __syncthreads();
+    if (x0 < DM_HX || y0 < DM_HY || x0 + DM_TW + DM_HX > S.w || y0 + DM_TH + DM_HY > S.h) {
+        for (int e = tid; e < DM_IH * DM_IW; e += 256) {
+            const int r = e / DM_IW, c = e - r * DM_IW;
+            const int gx = x0 - DM_HX + c, gy = y0 - DM_HY + r;
+            if (gx < 0 || gx >= S.w || gy < 0 || gy >= S.h) bt[e] = __int_as_float(0x7f800000);
+        }
+        __syncthreads();
+    }
+    const float* sac = iplane(ib, g, S, i1, Q_SAC);
+    const float* sdc = iplane(ib, g, S, i1, Q_SDC);
     float sq = 0.f, s3 = 0.f, mx = 0.f;
-    if (x < S.w && y < S.h) {
-        const float* b0 = iplane(ib, g, S, i1, Q_B0);
-        const int k = 3;
-        const int W = S.w, H = S.h, p = S.p;
-        float m0 = b0[(int64_t)y * p + x], m1 = 2.0f * m0, m2 = m1;
-        if (x >= k) {
-            store_min3(b0[(int64_t)y * p + x - k], m0, m1, m2);
-            if (y >= k) store_min3(b0[(int64_t)(y - k) * p + x - k], m0, m1, m2);
-            if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x - k], m0, m1, m2);
-        }
-        if (x < W - k) {
-            store_min3(b0[(int64_t)y * p + x + k], m0, m1, m2);
-            if (y >= k) store_min3(b0[(int64_t)(y - k) * p + x + k], m0, m1, m2);
-            if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x + k], m0, m1, m2);
-        }
-        if (y >= k) store_min3(b0[(int64_t)(y - k) * p + x], m0, m1, m2);
-        if (y < H - k) store_min3(b0[(int64_t)(y + k) * p + x], m0, m1, m2);
-        const float mask = 0.45f * m0 + 0.3f * m1 + 0.25f * m2;
-        const int64_t i = (int64_t)y * p + x;
-        float d = sqrtf(mask_y(mask) * iplane(ib, g, S, i1, Q_SAC)[i] +
-                        mask_dc_y(mask) * iplane(ib, g, S, i1, Q_SDC)[i]);
-        if (!FINAL) {
-            iplane(ib, g, S, i1, Q_DIFF)[i] = d;
-        } else {
-            constexpr DConst k085 = dconst(1.0 - 0.3 * (double)0.5f);
-            const BScaleDev Hs = g.s[1];
-            const float small = iplane(ib, g, Hs, i1, Q_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
-            d = fmaf(0.5f, small, mul_dc(d, k085));
-            if (distmap) distmap[(int64_t)pair * W * H + (int64_t)y * W + x] = d;
-            sq = powf(d, qnorm);
-            s3 = fabsf(d) * d * d;
-            mx = fabsf(d);
+    const int x = x0 + tx;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int ly = ty + 8 * k, y = y0 + ly;
+        if (x < S.w && y < S.h) {
+            const float* c = bt + (ly + DM_HY) * DM_IW + tx + DM_HX;
+            constexpr int K = 3, R = 3 * DM_IW;
+            float m0 = c[0], m1 = 2.0f * m0, m2 = m1;
+            store_min3(c[-K], m0, m1, m2);
+            store_min3(c[-K - R], m0, m1, m2);
+            store_min3(c[-K + R], m0, m1, m2);
+            store_min3(c[K], m0, m1, m2);
+            store_min3(c[K - R], m0, m1, m2);
+            store_min3(c[K + R], m0, m1, m2);
+            store_min3(c[-R], m0, m1, m2);
+            store_min3(c[R], m0, m1, m2);
+            const float mask = 0.45f * m0 + 0.3f * m1 + 0.25f * m2;
+            const int64_t i = (int64_t)y * S.p + x;
+            float d = sqrtf(mask_y(mask) * __ldg(sac + i) + mask_dc_y(mask) * __ldg(sdc + i));
+            if (!FINAL) {
+                iplane(ib, g, S, i1, Q_DIFF)[i] = d;
+            } else {
+                constexpr DConst k085 = dconst(1.0 - 0.3 * (double)0.5f);
+                const BScaleDev Hs = g.s[1];
+                const float small = iplane(ib, g, Hs, i1, Q_DIFF)[(int64_t)(y / 2) * Hs.p + x / 2];
+                d = fmaf(0.5f, small, mul_dc(d, k085));
+                if (distmap) distmap[(int64_t)pair * S.w * S.h + (int64_t)y * S.w + x] = d;
+                sq += qnorm == 2.0f ? d * d : powf(d, qnorm);  // diffnorms.hpp:63
+                s3 += fabsf(d) * d * d;
+                mx = fmaxf(mx, fabsf(d));
+            }
         }
     }
     if (FINAL) {
         __shared__ float red[3][8];
-        const int lane = threadIdx.x, warp = threadIdx.y;
+        const int lane = tx, warp = ty;
         sq = warp_sum(sq);
         s3 = warp_sum(s3);
         mx = warp_max(mx);
@@ -981,8 +1011,8 @@ static BGeom make_bgeom(int64_t w, int64_t h) {
         ch = half_dim(ch);
     }
     g.img_floats = off;
-    g.norm_tiles_x = (int)ceil_div(w, 32);
-    g.norm_tiles = g.norm_tiles_x * (int)ceil_div(h, 8);
+    g.norm_tiles_x = (int)ceil_div(w, DM_TW);
+    g.norm_tiles = g.norm_tiles_x * (int)ceil_div(h, DM_TH);
     return g;
 }
 
@@ -1158,11 +1188,11 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
         { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s); }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
         { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(ib, pimg, g, s); }
-        const dim3 gf((unsigned)ceil_div(sw, 32), (unsigned)ceil_div(sh, 8), np);
+        const dim3 gf((unsigned)ceil_div(sw, DM_TW), (unsigned)ceil_div(sh, DM_TH), np);
         if (s == 1)
-            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, dim3(32, 8), 0, st>>>(ib, pimg, g, s, nullptr, partials, (float)qnorm); }
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, 256, 0, st>>>(ib, pimg, g, s, nullptr, partials, (float)qnorm); }
         else
-            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, dim3(32, 8), 0, st>>>(ib, pimg, g, s, distmap_out, partials, (float)qnorm); }
+            { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<true><<<gf, 256, 0, st>>>(ib, pimg, g, s, distmap_out, partials, (float)qnorm); }
     }
     { ProfScope ps_("butter_finalize", st); butter_finalize_kernel<<<np, 256, 0, st>>>(partials, norms_out, g, qnorm); }
     VSHIP_CUDA_TRY(cudaGetLastError());

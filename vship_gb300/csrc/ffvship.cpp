@@ -3,9 +3,9 @@
 //
 // Same flags, per-frame JSON format and statistics block as the reference. Decoding: the
 // reference decodes any container with ffms2 and converts colour with zimg on the CPU; neither
-// library is available here, so this tool reads YUV4MPEG2 (.y4m) 4:2:0 files, 8- or 10-bit, and
-// hands the planes to the GPU front-end (Vship_ComputeSSIMU2Yuv420p10 /
-// Vship_ComputeButteraugliYuv420p10), which does the BT.709 conversion on the device.
+// library is available here, so this tool reads YUV4MPEG2 (.y4m) files (4:2:0 / 4:2:2 / 4:4:4,
+// 8-16 bit) and hands the planes to the GPU front-end (Vship_SSIMU2SetYuvFormat +
+// Vship_ComputeSSIMU2Yuv, and the Butteraugli pair), which converts colour on the device.
 //
 // Pipeline (as the reference's): reader threads fill a bounded frame-pair queue, GPU worker
 // threads (one handler each) score pairs, the main thread aggregates results in frame order.
@@ -34,12 +34,18 @@ namespace {
 const char* kVersion = "vship_gb300 ffvship 3.1.0";
 
 // ------------------------------------------------------------------------------------------
-// YUV4MPEG2 reader (4:2:0, 8 or 10 bit)
+// YUV4MPEG2 reader: C420jpeg / C420 (center siting), C420mpeg2 (left), C420paldv (top-left),
+// C420pN / C422[pN] / C444[pN] (N = 9..16; chroma siting unspecified, read as left, the
+// reference's default, ffmpegToZimgFormat.hpp:224-227), optional XCOLORRANGE=FULL. Y4M carries no
+// matrix, so the reference's guess by height applies (matrix 2).
 struct Y4M {
     std::string path;
-    int w = 0, h = 0, bits = 8;
+    int w = 0, h = 0, bits = 8, ssw = 1, ssh = 1, loc = 0, full = 0;
     int64_t header_len = 0, frame_bytes = 0, nframes = 0;
     int64_t frame_stride = 0;  // "FRAME\n" + payload
+
+    int64_t cw() const { return ssw ? (w + 1) / 2 : w; }
+    int64_t ch() const { return ssh ? (h + 1) / 2 : h; }
 
     bool open(const std::string& p, std::string& err) {
         path = p;
@@ -64,27 +70,43 @@ struct Y4M {
             if (tok[0] == 'W') w = std::atoi(tok.c_str() + 1);
             else if (tok[0] == 'H') h = std::atoi(tok.c_str() + 1);
             else if (tok[0] == 'C') cs = tok.substr(1);
+            else if (tok == "XCOLORRANGE=FULL") full = 1;
         }
-        if (cs.rfind("420", 0) != 0) {
+        const std::string sub = cs.substr(0, 3);
+        if (sub == "420") {
+            ssw = ssh = 1;
+        } else if (sub == "422") {
+            ssw = 1;
+            ssh = 0;
+        } else if (sub == "444") {
+            ssw = ssh = 0;
+        } else {
             std::fclose(f);
-            err = p + ": only 4:2:0 YUV4MPEG2 input is supported (got C" + cs + ")";
+            err = p + ": unsupported YUV4MPEG2 colorspace C" + cs;
             return false;
         }
+        const std::string rest = cs.substr(3);
         bits = 8;
-        if (cs.find("p10") != std::string::npos) bits = 10;
-        else if (cs.find("p12") != std::string::npos || cs.find("p16") != std::string::npos || cs.find("p9") != std::string::npos) {
+        loc = 0;
+        if (rest.empty() || rest == "jpeg") {
+            loc = ssw ? 1 : 0;  // 4:2:0 JPEG / MPEG-1 siting: center
+        } else if (rest == "mpeg2") {
+            loc = 0;
+        } else if (rest == "paldv") {
+            loc = 2;
+        } else if (rest[0] == 'p') {
+            bits = std::atoi(rest.c_str() + 1);
+        } else {
             std::fclose(f);
-            err = p + ": only 8-bit and 10-bit 4:2:0 are supported (got C" + cs + ")";
+            err = p + ": unsupported YUV4MPEG2 colorspace C" + cs;
             return false;
         }
-        if (w <= 0 || h <= 0) {
+        if (bits < 8 || bits > 16 || w <= 0 || h <= 0) {
             std::fclose(f);
-            err = p + ": missing W/H";
+            err = p + ": bad bit depth or missing W/H";
             return false;
         }
-        const int64_t cw = (w + 1) / 2, ch = (h + 1) / 2;
-        const int bps = bits > 8 ? 2 : 1;
-        frame_bytes = ((int64_t)w * h + 2 * cw * ch) * bps;
+        frame_bytes = ((int64_t)w * h + 2 * cw() * ch()) * (bits > 8 ? 2 : 1);
         // frame header: "FRAME" plus optional parameters up to '\n'
         std::fseek(f, header_len, SEEK_SET);
         std::string fh;
@@ -102,9 +124,10 @@ struct Y4M {
         return true;
     }
 
-    // Reads frame k as 10-bit samples (8-bit input is scaled by 4: limited-range 8-bit codes map
-    // exactly onto the 10-bit ones).
-    bool read(int64_t k, std::vector<uint16_t>& out, std::string& err) const {
+    // Reads frame k. Samples stay as stored (bytes for 8 bits, 16-bit containers above), except
+    // that `to_bits` > bits widens limited-range samples to that depth by a shift, which keeps
+    // every decoded value exactly (both map code 16 << (d - 8) to 0 and 235 << (d - 8) to 1).
+    bool read(int64_t k, std::vector<uint8_t>& out, int to_bits, std::string& err) const {
         FILE* f = std::fopen(path.c_str(), "rb");
         if (!f) {
             err = "cannot open " + path;
@@ -113,14 +136,20 @@ struct Y4M {
         const int64_t off = header_len + k * frame_stride + (frame_stride - frame_bytes);
         std::fseek(f, off, SEEK_SET);
         const int64_t n = frame_bytes / (bits > 8 ? 2 : 1);
-        out.resize(n);
         bool ok;
-        if (bits > 8) {
-            ok = std::fread(out.data(), 2, n, f) == (size_t)n;
+        if (to_bits == bits) {
+            out.resize(frame_bytes);
+            ok = std::fread(out.data(), 1, frame_bytes, f) == (size_t)frame_bytes;
         } else {
-            std::vector<uint8_t> tmp(n);
-            ok = std::fread(tmp.data(), 1, n, f) == (size_t)n;
-            for (int64_t i = 0; i < n; i++) out[i] = (uint16_t)(tmp[i] << 2);
+            std::vector<uint8_t> raw(frame_bytes);
+            ok = std::fread(raw.data(), 1, frame_bytes, f) == (size_t)frame_bytes;
+            out.resize(n * 2);
+            uint16_t* o16 = reinterpret_cast<uint16_t*>(out.data());
+            const int sh = to_bits - bits;
+            for (int64_t i = 0; i < n; i++) {
+                const unsigned v = bits > 8 ? (unsigned)raw[2 * i] | ((unsigned)raw[2 * i + 1] << 8) : raw[i];
+                o16[i] = (uint16_t)(v << sh);
+            }
         }
         std::fclose(f);
         if (!ok) err = path + ": short read at frame " + std::to_string(k);
@@ -132,22 +161,23 @@ struct Crop {
     int top = 0, bottom = 0, left = 0, right = 0;
 };
 
-// planes of a (cropped) frame inside a 10-bit buffer
+// planes of a (cropped) frame inside a read buffer of `bytes` per sample
 struct PlaneView {
     const uint8_t* p[3];
     int64_t stride[3];
 };
-PlaneView view(const std::vector<uint16_t>& buf, int w, int h, const Crop& c) {
-    const int cw = (w + 1) / 2, ch = (h + 1) / 2;
-    const uint16_t* Y = buf.data();
-    const uint16_t* U = Y + (size_t)w * h;
-    const uint16_t* V = U + (size_t)cw * ch;
+PlaneView view(const std::vector<uint8_t>& buf, const Y4M& y, int bytes, const Crop& c) {
+    const int64_t w = y.w, h = y.h, cw = y.cw(), ch = y.ch();
+    const uint8_t* Y = buf.data();
+    const uint8_t* U = Y + (size_t)w * h * bytes;
+    const uint8_t* V = U + (size_t)cw * ch * bytes;
+    const int cl = y.ssw ? c.left / 2 : c.left, ct = y.ssh ? c.top / 2 : c.top;
     PlaneView v;
-    v.p[0] = reinterpret_cast<const uint8_t*>(Y + (size_t)c.top * w + c.left);
-    v.p[1] = reinterpret_cast<const uint8_t*>(U + (size_t)(c.top / 2) * cw + c.left / 2);
-    v.p[2] = reinterpret_cast<const uint8_t*>(V + (size_t)(c.top / 2) * cw + c.left / 2);
-    v.stride[0] = (int64_t)w * 2;
-    v.stride[1] = v.stride[2] = (int64_t)cw * 2;
+    v.p[0] = Y + ((size_t)c.top * w + c.left) * bytes;
+    v.p[1] = U + ((size_t)ct * cw + cl) * bytes;
+    v.p[2] = V + ((size_t)ct * cw + cl) * bytes;
+    v.stride[0] = w * bytes;
+    v.stride[1] = v.stride[2] = cw * bytes;
     return v;
 }
 
@@ -323,7 +353,7 @@ public:
 
 struct Loaded {
     int idx;
-    std::vector<uint16_t> src, enc;
+    std::vector<uint8_t> src, enc;
 };
 
 std::string err_text(Vship_Exception e) {
@@ -370,10 +400,20 @@ int main(int argc, char** argv) {
     const Crop& cs = o.crop_src;
     const Crop& ce = o.crop_enc;
     for (const Crop* c : {&cs, &ce})
-        if ((c->top | c->bottom | c->left | c->right) & 1) {
-            std::cerr << "crops must be even for 4:2:0 input\n";
+        if ((((c->top | c->bottom) & 1) && src.ssh) || (((c->left | c->right) & 1) && src.ssw)) {
+            std::cerr << "crops must be even along subsampled chroma directions\n";
             return 1;
         }
+    // one Y'CbCr format for both files: equal formats, or limited-range ones that differ only in
+    // depth (the shallower one is widened, exactly)
+    if (src.ssw != enc.ssw || src.ssh != enc.ssh || src.loc != enc.loc || src.full != enc.full ||
+        (src.bits != enc.bits && src.full)) {
+        std::cerr << "DifferingInputType: source and encoded Y'CbCr formats differ\n";
+        return 1;
+    }
+    const int bits = std::max(src.bits, enc.bits);
+    const int bytes = bits > 8 ? 2 : 1;
+    Vship_YuvFormat yfmt{bits, src.ssw, src.ssh, 2, src.full, src.loc};
     const int w = src.w - cs.left - cs.right, h = src.h - cs.top - cs.bottom;
     if (w != enc.w - ce.left - ce.right || h != enc.h - ce.top - ce.bottom || w <= 0 || h <= 0) {
         std::cerr << "DifferingInputType: source and encoded differ in size after cropping\n";
@@ -423,7 +463,7 @@ int main(int argc, char** argv) {
                 Loaded l;
                 l.idx = k;
                 std::string e;
-                if (!src.read(jobs[k].src_frame, l.src, e) || !enc.read(jobs[k].enc_frame, l.enc, e)) {
+                if (!src.read(jobs[k].src_frame, l.src, bits, e) || !enc.read(jobs[k].enc_frame, l.enc, bits, e)) {
                     std::cerr << e << "\n";
                     failed = 1;
                     continue;
@@ -442,6 +482,9 @@ int main(int argc, char** argv) {
             Vship_ButteraugliHandler hb{};
             Vship_Exception e = o.metric == Metric::SSIMU2 ? Vship_SSIMU2Init(&hs, w, h)
                                                            : Vship_ButteraugliInitv2(&hb, w, h, o.qnorm, o.intensity);
+            if (e == Vship_NoError)
+                e = o.metric == Metric::SSIMU2 ? Vship_SSIMU2SetYuvFormat(hs, &yfmt)
+                                               : Vship_ButteraugliSetYuvFormat(hb, &yfmt);
             if (e != Vship_NoError) {
                 std::cerr << err_text(e) << "\n";
                 failed = 1;
@@ -449,15 +492,15 @@ int main(int argc, char** argv) {
             Loaded l;
             while (frames.pop(l)) {
                 if (e != Vship_NoError) continue;
-                PlaneView a = view(l.src, src.w, src.h, cs), b = view(l.enc, enc.w, enc.h, ce);
+                PlaneView a = view(l.src, src, bytes, cs), b = view(l.enc, enc, bytes, ce);
                 Vship_Exception rc;
                 if (o.metric == Metric::SSIMU2) {
                     double s = 0;
-                    rc = Vship_ComputeSSIMU2Yuv420p10(hs, &s, a.p, a.stride, b.p, b.stride);
+                    rc = Vship_ComputeSSIMU2Yuv(hs, &s, a.p, a.stride, b.p, b.stride);
                     scores[l.idx] = (float)s;
                 } else {
                     double n[3] = {0, 0, 0};
-                    rc = Vship_ComputeButteraugliYuv420p10(hb, n, nullptr, 0, a.p, a.stride, b.p, b.stride);
+                    rc = Vship_ComputeButteraugliYuv(hb, n, nullptr, 0, a.p, a.stride, b.p, b.stride);
                     for (int i = 0; i < 3; i++) scores[3 * l.idx + i] = (float)n[i];
                 }
                 if (rc != Vship_NoError) {

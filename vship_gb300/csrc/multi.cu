@@ -66,7 +66,7 @@ size_t MultiEngine::device_bytes(int nres, const int* widths, const int* heights
             int ci = 0, cp = 0;
             butter_caps(widths[r], heights[r], max_sources[r], max_pairs[r], &ci, &cp);
             total += ButterEngine::image_bytes(widths[r], heights[r]) * ci +
-                     (size_t)cp * (3 * 4 * (size_t)ceil_div(widths[r], 32) * (size_t)ceil_div(heights[r], 8) + 24);
+                     (size_t)cp * (3 * 4 * (size_t)butter_norm_tiles(widths[r], heights[r]) + 24);
         }
     }
     return total;

@@ -276,12 +276,17 @@ def rgb_float_pair(h: int, w: int, t: int, seed: int = 7, distortion: str = "dct
     return yuv420p10_to_rgb(ref), yuv420p10_to_rgb(dist)
 
 
-def write_y4m(path: str, frames, w: int, h: int, bits: int = 10, fps: str = "24:1") -> None:
-    """Write 4:2:0 frames [(Y, Cb, Cr) integer arrays] as YUV4MPEG2 (8-bit C420 or 10-bit
-    C420p10, little-endian 16-bit containers)."""
+def write_y4m(path: str, frames, w: int, h: int, bits: int = 10, fps: str = "24:1", chroma: str = "420",
+              siting: str = "") -> None:
+    """Write frames [(Y, Cb, Cr) integer arrays] as YUV4MPEG2: chroma "420", "422" or "444";
+    8-bit samples in bytes, deeper ones in little-endian 16-bit containers. The colorspace tag is
+    C<chroma><siting> for 8 bits (siting "jpeg", "mpeg2", "paldv" or "" for 4:2:0) and
+    C<chroma>p<bits> above."""
     import numpy as np
 
-    tag = "C420p10 XYSCSS=420P10" if bits == 10 else "C420jpeg"
+    tag = f"C{chroma}{siting}" if bits == 8 else f"C{chroma}p{bits}"
+    if chroma == "420" and bits == 8 and not siting:
+        tag = "C420jpeg"
     with open(path, "wb") as f:
         f.write(f"YUV4MPEG2 W{w} H{h} F{fps} Ip A1:1 {tag}\n".encode())
         for fr in frames:
