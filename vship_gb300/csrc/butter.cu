@@ -64,6 +64,19 @@ __device__ __forceinline__ float b_inv_mass(int pos, int extent) {
     const int end = min(extent, pos + R + 1) - (pos - R);
     return 1.0f / (c_bI[KI][end] - c_bI[KI][beg]);
 }
+// The same for n consecutive positions p0 .. p0+n-1: positions whose whole window lies inside
+// the extent share the interior value (beg = 0, end = 2R + 1), computed once.
+template <int KI, int R, int N>
+__device__ __forceinline__ void b_inv_mass_run(int p0, int extent, float out[N]) {
+    if (p0 >= R && p0 + N - 1 + R < extent) {
+        const float v = 1.0f / (c_bI[KI][2 * R + 1] - c_bI[KI][0]);
+#pragma unroll
+        for (int o = 0; o < N; o++) out[o] = v;
+    } else {
+#pragma unroll
+        for (int o = 0; o < N; o++) out[o] = b_inv_mass<KI, R>(p0 + o, extent);
+    }
+}
 
 // ------------------------------------------------------------------------------------------
 // Workspace layout. Every image (a reference / source or a distorted / candidate frame) owns, per
@@ -215,8 +228,10 @@ template <int KI>
 __device__ __forceinline__ void tile_masses_r8(int x0, int y0, int w, int h, float rxy[6]) {
     const int tid = threadIdx.x;
     const float rx = b_inv_mass<KI, 8>(x0 + (tid & 31), w);
+    float ry[6];
+    b_inv_mass_run<KI, 8, 6>(y0 + 6 * (tid >> 5), h, ry);
 #pragma unroll
-    for (int o = 0; o < 6; o++) rxy[o] = rx * b_inv_mass<KI, 8>(y0 + 6 * (tid >> 5) + o, h);
+    for (int o = 0; o < 6; o++) rxy[o] = rx * ry[o];
 }
 
 // ------------------------------------------------------------------------------------------
@@ -343,13 +358,14 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* const* __restr
         v[4 * j4 + 2] = q.z;
         v[4 * j4 + 3] = q.w;
     }
-    float out[8];
+    float out[8], rx[8];
+    b_inv_mass_run<KI, R, 8>(x0 + col0, S.w, rx);
 #pragma unroll
     for (int o = 0; o < 8; o++) {
         float a = 0.f;
 #pragma unroll
         for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[OFF + o + i], c_bk[KI][i], a);
-        out[o] = a * b_inv_mass<KI, R>(x0 + col0 + o, S.w);
+        out[o] = a * rx[o];
     }
     float* d = dst + (int64_t)gy * S.p + x0 + col0;
     if (x0 + col0 + 8 <= S.p) {  // rows are padded to a multiple of 8 floats
@@ -382,8 +398,7 @@ __device__ __forceinline__ void vblur3(float* in, float* ctr, float* const* __re
     __syncthreads();
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float ry[8];
-#pragma unroll
-    for (int o = 0; o < 8; o++) ry[o] = b_inv_mass<KI, R>(y0 + 8 * vg + o, S.h);
+    b_inv_mass_run<KI, R, 8>(y0 + 8 * vg, S.h, ry);
 #pragma unroll
     for (int c = 0; c < 3; c++) {
         const float* col = in + c * IH * VB_TW + (8 * vg) * VB_TW + vc;
