@@ -58,8 +58,8 @@ size_t MultiEngine::device_bytes(int nres, const int* widths, const int* heights
             total += (size_t)max_sources[r] * 3 * pe * 4;
             total += (size_t)max_pairs[r] * 3 * pe * ((flags & MULTI_FP16) ? 2 : 4);
             total += (size_t)max_pairs[r] * 18 * g.tiles_total * 4;
-            total += ((size_t)max_sources[r] + max_pairs[r]) * (size_t)ceil_div(widths[r], 32) *
-                     (size_t)ceil_div(heights[r], 32) * sizeof(int4);
+            total += ((size_t)max_sources[r] + max_pairs[r]) * (size_t)ceil_div(widths[r], kPyrTile) *
+                     (size_t)ceil_div(heights[r], kPyrTile) * sizeof(int4);
             total += (size_t)max_pairs[r] * g.tiles_total * sizeof(int2);
         }
         if ((flags & MULTI_BUTTERAUGLI) && max_pairs[r] > 0) {
@@ -120,7 +120,7 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
                 VSHIP_CUDA_TRY(cudaMalloc(&s_cand[r], (size_t)max_pairs[r] * 3 * pe * cand_elem));
                 VSHIP_CUDA_TRY(cudaMalloc(&s_part[r], (size_t)max_pairs[r] * 18 * geoms_h[r].tiles_total * 4));
             }
-            cap_pitems += ((size_t)max_src[r] + max_pairs[r]) * (size_t)ceil_div(rw[r], 32) * (size_t)ceil_div(rh[r], 32);
+            cap_pitems += ((size_t)max_src[r] + max_pairs[r]) * (size_t)ceil_div(rw[r], kPyrTile) * (size_t)ceil_div(rh[r], kPyrTile);
             cap_sitems += (size_t)max_pairs[r] * geoms_h[r].tiles_total;
         }
         VSHIP_CUDA_TRY(cudaMalloc(&geoms_d, sizeof(Ssimu2Geom) * nres));
@@ -237,14 +237,14 @@ int MultiEngine::build_plan(int nsrc, const int* src_res, int npairs, const int*
         std::vector<int4> pit;
         for (int i = 0; i < nsrc; i++) {
             const int r = src_res[i];
-            const int tx = (int)ceil_div(rw[r], 32), ty = (int)ceil_div(rh[r], 32);
+            const int tx = (int)ceil_div(rw[r], kPyrTile), ty = (int)ceil_div(rh[r], kPyrTile);
             for (int y = 0; y < ty; y++)
                 for (int x = 0; x < tx; x++) pit.push_back(make_int4(i, x, y, 0));
         }
         n_pitems_src = (int)pit.size();
         for (int j = 0; j < npairs; j++) {
             const int r = src_res[cand_src[j]];
-            const int tx = (int)ceil_div(rw[r], 32), ty = (int)ceil_div(rh[r], 32);
+            const int tx = (int)ceil_div(rw[r], kPyrTile), ty = (int)ceil_div(rh[r], kPyrTile);
             for (int y = 0; y < ty; y++)
                 for (int x = 0; x < tx; x++) pit.push_back(make_int4(nsrc + j, x, y, 0));
         }

@@ -290,7 +290,7 @@ int Server::launch(Batch* b) {
     for (int i = 0; i < nreq; i++) {
         ServeReq* r = b->reqs[i];
         if (r->metric != SERVE_SSIMU2) continue;
-        const size_t t0 = (size_t)ceil_div(rw[r->res], 32) * (size_t)ceil_div(rh[r->res], 32);
+        const size_t t0 = (size_t)ceil_div(rw[r->res], kPyrTile) * (size_t)ceil_div(rh[r->res], kPyrTile);
         if (stage[i]) n_pitems_src += t0;
         n_pitems_cand += t0 * r->cands.size();
         n_sitems += (size_t)sgeom[r->res].tiles_total * r->cands.size();
@@ -380,7 +380,7 @@ int Server::launch(Batch* b) {
         int ni = 0, npair = 0;
         size_t ps = 0, pc = n_pitems_src, si = 0, ro = 0;
         auto add_tiles = [&](int img, int res, size_t& cursor) {
-            const int tx = (int)ceil_div(rw[res], 32), ty = (int)ceil_div(rh[res], 32);
+            const int tx = (int)ceil_div(rw[res], kPyrTile), ty = (int)ceil_div(rh[res], kPyrTile);
             for (int y = 0; y < ty; y++)
                 for (int x = 0; x < tx; x++) pit[cursor++] = make_int4(img, x, y, 0);
         };

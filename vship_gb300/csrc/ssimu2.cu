@@ -117,41 +117,69 @@ __device__ __forceinline__ void pyr_store(const PyrOut& out, int64_t pe, int64_t
     }
 }
 
+// One kPyrTile x kPyrTile (64 x 64) level-0 tile per CTA. Level 0 and level 1 are fused: each
+// thread takes 2x2 quads of level-0 pixels, stores their XYB and sums their linear RGB into the
+// level-1 sample (at odd image edges the quad's second column / row is the clamped last one,
+// as the reference's downsample reads it), so level 0 never goes through shared memory.
+// Levels 2..5 (sides 16, 8, 4, 2) are built from shared memory with shifts.
 template <int IT, bool DELTA>
 __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParams& yp, const PyrOut& out,
                                              const Ssimu2Geom& g, int bx, int by) {
     __shared__ float smA[3 * 32 * 33];
     __shared__ float smB[3 * 16 * 17];
     const int64_t pe = g.plane_elems;
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     {
-        const Ssimu2Level L = g.lv[0];
+        const Ssimu2Level L0 = g.lv[0], L1 = g.lv[1];
+#pragma unroll 1
+        for (int q = threadIdx.x; q < 32 * 32; q += 256) {
+            const int qx = q & 31, qy = q >> 5;  // level-1 position inside the tile
+            const int gx1 = bx * 32 + qx, gy1 = by * 32 + qy;
+            float v[3] = {0.f, 0.f, 0.f};
+            if (gx1 < L1.w && gy1 < L1.h) {
+                const int xa = 2 * gx1, ya = 2 * gy1;
+                const int xb = min(xa + 1, L0.w - 1), yb = min(ya + 1, L0.h - 1);
+                float lin[4][3];
+                // summation order of the downsample: (xa, ya), (xa, yb), (xb, ya), (xb, yb)
+                const int px[4] = {xa, xa, xb, xb}, py[4] = {ya, yb, ya, yb};
 #pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int ly = ty + 8 * r;
-            const int gx = bx * 32 + tx, gy = by * 32 + ly;
-            float v0 = 0.f, v1 = 0.f, v2 = 0.f;
-            if (gx < L.w && gy < L.h) {
-                load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, v0, v1, v2);
-                v0 = to_linear_fast(v0);
-                v1 = to_linear_fast(v1);
-                v2 = to_linear_fast(v2);
-                float X = v0, Y = v1, B = v2;
+                for (int k = 0; k < 4; k++) {
+                    float r, gg, b;
+                    load_rgb<IT>(fd, yp, px[k], py[k], L0.w, L0.h, r, gg, b);
+                    lin[k][0] = to_linear_fast(r);
+                    lin[k][1] = to_linear_fast(gg);
+                    lin[k][2] = to_linear_fast(b);
+                    // each level-0 pixel is stored once: by the quad sample that is not a clamp copy
+                    const bool own = (k == 0) || (k == 1 && yb != ya) || (k == 2 && xb != xa) ||
+                                     (k == 3 && xb != xa && yb != ya);
+                    if (own) {
+                        float X = lin[k][0], Y = lin[k][1], B = lin[k][2];
+                        positive_xyb(X, Y, B);
+                        pyr_store<DELTA>(out, pe, L0.off + (int64_t)py[k] * L0.pitch + px[k], X, Y, B);
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    float s = lin[0][c];
+                    s += lin[1][c];
+                    s += lin[2][c];
+                    s += lin[3][c];
+                    v[c] = s * 0.25f;
+                }
+                float X = v[0], Y = v[1], B = v[2];
                 positive_xyb(X, Y, B);
-                pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);
+                pyr_store<DELTA>(out, pe, L1.off + (int64_t)gy1 * L1.pitch + gx1, X, Y, B);
             }
-            smA[(0 * 32 + ly) * 33 + tx] = v0;
-            smA[(1 * 32 + ly) * 33 + tx] = v1;
-            smA[(2 * 32 + ly) * 33 + tx] = v2;
+#pragma unroll
+            for (int c = 0; c < 3; c++) smA[(c * 32 + qy) * 33 + qx] = v[c];
         }
     }
     __syncthreads();
     float* cur = smA;
     float* nxt = smB;
-    // levels 1..5: the tile side halves each level (16, 8, 4, 2, 1), so indices are shifts
+    // levels 2..5: the tile side halves each level (16, 8, 4, 2), so indices are shifts
 #pragma unroll
-    for (int k = 1; k < 6; k++) {
-        const int cside = 32 >> (k - 1), nside = 32 >> k, lg = 5 - k;
+    for (int k = 2; k < 6; k++) {
+        const int cside = 64 >> (k - 1), nside = 64 >> k, lg = 6 - k;
         const Ssimu2Level L = g.lv[k], P = g.lv[k - 1];
         const int ox = bx * nside, oy = by * nside;
         const int pox = bx * cside, poy = by * cside;
@@ -197,12 +225,12 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
 }
 
 // ------------------------------------------------------------------------------------------
-// Kernel 2: fused 5-moment blur + SSIM/edge maps + per-CTA pooling, all scales in one launch.
-// grid (tiles_total, npairs), 256 threads, dynamic smem kStatsSmem.
+// Kernel 2: fused moment blur + SSIM/edge maps + per-CTA pooling, all scales in one launch.
+// grid (tiles_total, npairs), 256 threads, dynamic smem kStatsSmem, three CTAs per SM.
 //
 // Per CTA: one 32x48 output tile of one scale. For each channel the raw I1 and I2 tiles with an
 // 8-px halo (64 rows x 48 columns) are staged with cp.async (bytes outside the image are
-// zero-filled), double-buffered so channel c+1 streams in while channel c computes. The
+// zero-filled); one CTA's loads overlap the arithmetic of the other CTAs on its SM. The
 // horizontal pass reads the raw rows as float4 (row pitch 52 floats: the 8 lanes of each
 // quarter-warp phase hit distinct bank quads), forms the shifted samples and their products in
 // registers and scatters them into 8 outputs x 5 moments; the vertical pass gathers 22 rows per
@@ -214,9 +242,9 @@ constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte 
 constexpr int ST_HP = 33;                // horizontal-pass output pitch
 constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
 constexpr int ST_HPLANE = ST_IH * ST_HP;
-// smem: 2 stages x 2 raw images, the horizontal pass as two float-pair planes {m1, m2} and
-// {s11 + s22, s12}, and the per-warp pools
-constexpr int kStatsSmem = (2 * 2 * ST_RAW + 4 * ST_HPLANE + 3 * 8 * 6) * 4;
+// smem: the 2 raw images, the horizontal pass as two float-pair planes {m1, m2} and
+// {s11 + s22, s12}, and the per-warp pools: 61 KB, so that three CTAs share an SM
+constexpr int kStatsSmem = (2 * ST_RAW + 4 * ST_HPLANE + 3 * 8 * 6) * 4;
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
@@ -271,8 +299,8 @@ template <bool DELTA>
 __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const void* __restrict__ im2v, int64_t pe,
                                            const Ssimu2Level& L, int lt, float* __restrict__ out, int stride) {
     extern __shared__ __align__(16) float sm[];
-    float* raw = sm;                   // [stage][image][64][52]
-    float* hb = sm + 4 * ST_RAW;       // [5][64][33]
+    float* raw = sm;                   // [image][64][52]
+    float* hb = sm + 2 * ST_RAW;       // [4][64][33]
     float* red = hb + 4 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
     const float* im2 = static_cast<const float*>(im2v);
     const __half* im2h = static_cast<const __half*>(im2v);
@@ -293,28 +321,19 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
 #pragma unroll
     for (int o = 0; o < 6; o++) rxy[o] = rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
 
-    stage_tile(raw, im1, L.pitch, L.w, L.h, tx0, ty0);
-    if (DELTA) stage_tile_h(reinterpret_cast<__half*>(raw + ST_RAW), im2h, L.pitch, L.w, L.h, tx0, ty0);
-    else stage_tile(raw + ST_RAW, im2, L.pitch, L.w, L.h, tx0, ty0);
-    cp_async_commit();
-
 #pragma unroll 1
     for (int c = 0; c < 3; c++) {
-        float* r1 = raw + (c & 1) * 2 * ST_RAW;
-        float* r2 = r1 + ST_RAW;
-        if (c < 2) {
-            float* n1 = raw + ((c + 1) & 1) * 2 * ST_RAW;
-            stage_tile(n1, im1 + (int64_t)(c + 1) * pe, L.pitch, L.w, L.h, tx0, ty0);
-            if (DELTA)
-                stage_tile_h(reinterpret_cast<__half*>(n1 + ST_RAW), im2h + (int64_t)(c + 1) * pe, L.pitch, L.w, L.h,
-                             tx0, ty0);
-            else
-                stage_tile(n1 + ST_RAW, im2 + (int64_t)(c + 1) * pe, L.pitch, L.w, L.h, tx0, ty0);
-            cp_async_commit();
-            cp_async_wait<1>();
-        } else {
-            cp_async_wait<0>();
-        }
+        // one stage: the channel's two raw tiles; the loads of one CTA overlap the arithmetic of
+        // the SM's other two
+        float* r1 = raw;
+        float* r2 = raw + ST_RAW;
+        stage_tile(r1, im1 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+        if (DELTA)
+            stage_tile_h(reinterpret_cast<__half*>(r2), im2h + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+        else
+            stage_tile(r2, im2 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+        cp_async_commit();
+        cp_async_wait<0>();
         __syncthreads();
         // Moments are formed on values shifted by one per-tile constant (the reference image's
         // value at the tile origin). The blur is normalised, so sigma = E[(x-s)^2] - (E[x]-s)^2
@@ -472,7 +491,7 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
 }
 
 // grid (tiles_total, npairs), dynamic smem kStatsSmem
-__global__ void __launch_bounds__(256, 2) ssimu2_stats_kernel(const float* __restrict__ pyr,
+__global__ void __launch_bounds__(256, 3) ssimu2_stats_kernel(const float* __restrict__ pyr,
                                                               float* __restrict__ partials, Ssimu2Geom g) {
     const int pair = blockIdx.y;
     const int t = blockIdx.x;
@@ -549,7 +568,7 @@ __global__ void __launch_bounds__(256) ssimu2_multi_pyramid_kernel(const Ssimu2M
 
 // persistent: CTA b takes items b, b + gridDim.x, ...; items {pair, tile}
 template <bool DELTA>
-__global__ void __launch_bounds__(256, 2) ssimu2_multi_stats_kernel(const Ssimu2MultiPair* __restrict__ pairs,
+__global__ void __launch_bounds__(256, 3) ssimu2_multi_stats_kernel(const Ssimu2MultiPair* __restrict__ pairs,
                                                                     const int2* __restrict__ items, int nitems,
                                                                     const Ssimu2Geom* __restrict__ geoms) {
     for (int i = blockIdx.x; i < nitems; i += gridDim.x) {
@@ -635,7 +654,7 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
                          const YuvParams* yuv) {
     if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
     const YuvParams yp = yuv ? *yuv : yuv420p10_params();
-    dim3 g1((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), (unsigned)(2 * npairs));
+    dim3 g1((unsigned)ceil_div(w, kPyrTile), (unsigned)ceil_div(h, kPyrTile), (unsigned)(2 * npairs));
     {
     ProfScope ps("ssimu2_pyramid", st);
     switch (intype) {
@@ -684,7 +703,7 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
     float* pyr = scratch;
     float* partials = scratch + (size_t)geom.plane_elems * 6;
     ssimu2_store_frames_kernel<<<1, 1, 0, st>>>(ref, dist, frames_scratch);
-    dim3 g1((unsigned)ceil_div(geom.lv[0].w, 32), (unsigned)ceil_div(geom.lv[0].h, 32), 2u);
+    dim3 g1((unsigned)ceil_div(geom.lv[0].w, kPyrTile), (unsigned)ceil_div(geom.lv[0].h, kPyrTile), 2u);
     switch (intype) {
         case IN_UINT8: ssimu2_pyramid_kernel<IN_UINT8><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
         case IN_UINT16: ssimu2_pyramid_kernel<IN_UINT16><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;

@@ -9,6 +9,9 @@
 
 namespace vship {
 
+// Side of the level-0 tile one pyramid CTA builds (all six levels of it).
+constexpr int kPyrTile = 64;
+
 // One pyramid level in device memory: planar FP32, rows padded to `pitch` floats.
 struct Ssimu2Level {
     int w, h, pitch;
@@ -79,7 +82,7 @@ struct Ssimu2MultiPair {
 
 int ssimu2_multi_prepare();
 int ssimu2_multi_stats_blocks_per_sm(bool delta, int* blocks);
-// items: {image, level-0 tile x, tile y, 0}, one CTA each. delta selects the FP16-delta store.
+// items: {image, level-0 tile x, tile y, 0} in kPyrTile tiles, one CTA each. delta selects the FP16-delta store.
 int ssimu2_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items, int nitems, const Ssimu2Geom* geoms,
                          int intype, bool delta, cudaStream_t st);
 // Persistent: `grid` CTAs walk items {pair, tile} with stride grid.
