@@ -580,14 +580,11 @@ __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) 
     const float scaler2 = m.n2lt * inv;
     const float fabs0 = fabsf(a);
     const float too_small = 0.55f * fabs0, too_big = 1.05f * fabs0;
-    float impact = 0.0f;
-    if (a < 0.0f) {
-        if (b > -too_small) impact = b + too_small;
-        else if (b < -too_big) impact = -b - too_big;
-    } else {
-        if (b < too_small) impact = -b + too_small;
-        else if (b > too_big) impact = b - too_big;
-    }
+    // maltaDiff.hpp's two sign branches as one, on b mirrored to a's side: for a < 0 the
+    // reference's b + too_small and -b - too_big are too_small - (-b) and (-b) - too_big, the same
+    // IEEE operations, so the value is bitwise the same without divergent branches
+    const float bm = a < 0.0f ? -b : b;
+    float impact = bm < too_small ? too_small - bm : (bm > too_big ? bm - too_big : 0.0f);
     impact *= scaler2;
     return diff < 0.0f ? v - impact : v + impact;
 }

@@ -117,69 +117,42 @@ __device__ __forceinline__ void pyr_store(const PyrOut& out, int64_t pe, int64_t
     }
 }
 
-// One kPyrTile x kPyrTile (64 x 64) level-0 tile per CTA. Level 0 and level 1 are fused: each
-// thread takes 2x2 quads of level-0 pixels, stores their XYB and sums their linear RGB into the
-// level-1 sample (at odd image edges the quad's second column / row is the clamped last one,
-// as the reference's downsample reads it), so level 0 never goes through shared memory.
-// Levels 2..5 (sides 16, 8, 4, 2) are built from shared memory with shifts.
+// One kPyrTile x kPyrTile (32 x 32) level-0 tile per CTA, levels 1..5 from shared memory.
 template <int IT, bool DELTA>
 __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParams& yp, const PyrOut& out,
                                              const Ssimu2Geom& g, int bx, int by) {
     __shared__ float smA[3 * 32 * 33];
     __shared__ float smB[3 * 16 * 17];
     const int64_t pe = g.plane_elems;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     {
-        const Ssimu2Level L0 = g.lv[0], L1 = g.lv[1];
-#pragma unroll 1
-        for (int q = threadIdx.x; q < 32 * 32; q += 256) {
-            const int qx = q & 31, qy = q >> 5;  // level-1 position inside the tile
-            const int gx1 = bx * 32 + qx, gy1 = by * 32 + qy;
-            float v[3] = {0.f, 0.f, 0.f};
-            if (gx1 < L1.w && gy1 < L1.h) {
-                const int xa = 2 * gx1, ya = 2 * gy1;
-                const int xb = min(xa + 1, L0.w - 1), yb = min(ya + 1, L0.h - 1);
-                float lin[4][3];
-                // summation order of the downsample: (xa, ya), (xa, yb), (xb, ya), (xb, yb)
-                const int px[4] = {xa, xa, xb, xb}, py[4] = {ya, yb, ya, yb};
+        const Ssimu2Level L = g.lv[0];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    float r, gg, b;
-                    load_rgb<IT>(fd, yp, px[k], py[k], L0.w, L0.h, r, gg, b);
-                    lin[k][0] = to_linear_fast(r);
-                    lin[k][1] = to_linear_fast(gg);
-                    lin[k][2] = to_linear_fast(b);
-                    // each level-0 pixel is stored once: by the quad sample that is not a clamp copy
-                    const bool own = (k == 0) || (k == 1 && yb != ya) || (k == 2 && xb != xa) ||
-                                     (k == 3 && xb != xa && yb != ya);
-                    if (own) {
-                        float X = lin[k][0], Y = lin[k][1], B = lin[k][2];
-                        positive_xyb(X, Y, B);
-                        pyr_store<DELTA>(out, pe, L0.off + (int64_t)py[k] * L0.pitch + px[k], X, Y, B);
-                    }
-                }
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    float s = lin[0][c];
-                    s += lin[1][c];
-                    s += lin[2][c];
-                    s += lin[3][c];
-                    v[c] = s * 0.25f;
-                }
-                float X = v[0], Y = v[1], B = v[2];
+        for (int r = 0; r < 4; r++) {
+            const int ly = ty + 8 * r;
+            const int gx = bx * 32 + tx, gy = by * 32 + ly;
+            float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+            if (gx < L.w && gy < L.h) {
+                load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, v0, v1, v2);
+                v0 = to_linear_fast(v0);
+                v1 = to_linear_fast(v1);
+                v2 = to_linear_fast(v2);
+                float X = v0, Y = v1, B = v2;
                 positive_xyb(X, Y, B);
-                pyr_store<DELTA>(out, pe, L1.off + (int64_t)gy1 * L1.pitch + gx1, X, Y, B);
+                pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);
             }
-#pragma unroll
-            for (int c = 0; c < 3; c++) smA[(c * 32 + qy) * 33 + qx] = v[c];
+            smA[(0 * 32 + ly) * 33 + tx] = v0;
+            smA[(1 * 32 + ly) * 33 + tx] = v1;
+            smA[(2 * 32 + ly) * 33 + tx] = v2;
         }
     }
     __syncthreads();
     float* cur = smA;
     float* nxt = smB;
-    // levels 2..5: the tile side halves each level (16, 8, 4, 2), so indices are shifts
+    // levels 1..5: the tile side halves each level (16, 8, 4, 2, 1), so indices are shifts
 #pragma unroll
-    for (int k = 2; k < 6; k++) {
-        const int cside = 64 >> (k - 1), nside = 64 >> k, lg = 6 - k;
+    for (int k = 1; k < 6; k++) {
+        const int cside = 32 >> (k - 1), nside = 32 >> k, lg = 5 - k;
         const Ssimu2Level L = g.lv[k], P = g.lv[k - 1];
         const int ox = bx * nside, oy = by * nside;
         const int pox = bx * cside, poy = by * cside;

@@ -10,7 +10,7 @@
 namespace vship {
 
 // Side of the level-0 tile one pyramid CTA builds (all six levels of it).
-constexpr int kPyrTile = 64;
+constexpr int kPyrTile = 32;
 
 // One pyramid level in device memory: planar FP32, rows padded to `pitch` floats.
 struct Ssimu2Level {
