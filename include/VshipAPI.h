@@ -221,7 +221,10 @@ EXPORTPREPROCESS Vship_Exception Vship_ComputeButteraugliYuv420p10(Vship_Buttera
  * (BT.709), 4 (FCC), 5 (BT.470BG), 6 (SMPTE 170M), 7 (SMPTE 240M), 9 (BT.2020 NCL), or 2
  * (unspecified: BT.709 above 650 rows, BT.470BG below, as the reference guesses); range: 0
  * limited, 1 full; chroma_location: 0 left, 1 center, 2 top-left, 3 top, 4 bottom-left,
- * 5 bottom. Frames are in the BT.709 transfer and primaries (the reference's assumption). */
+ * 5 bottom; transfer (H.273 transfer_characteristics): 1 / 6 / 14 / 15 (the BT.709 family,
+ * which the reference's metrics linearise as a 2.4 power law) or 2 (unspecified), 13 (sRGB),
+ * 4 (gamma 2.2), 5 (gamma 2.8), 8 (linear); primaries (H.273 colour_primaries): 1 (BT.709) or
+ * 2 (unspecified), 9 (BT.2020, converted to BT.709 in linear light). */
 typedef struct {
     int bits;
     int subsampling_w;
@@ -229,6 +232,8 @@ typedef struct {
     int matrix;
     int range;
     int chroma_location;
+    int transfer;
+    int primaries;
 } Vship_YuvFormat;
 /* The format a handler uses for Vship_InYuv frames (device entry points) and for the
  * Vship_Compute*Yuv calls; the default is 10-bit 4:2:0 BT.709 limited range, left siting. The

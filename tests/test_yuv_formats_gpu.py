@@ -60,6 +60,39 @@ def test_butteraugli_yuv_formats(vlib, fmt):
         assert abs(a - b) <= 1e-5 * abs(b), (n_yuv, n_rgb)
 
 
+# (bits, ssw, ssh, matrix, full, loc, h, w, transfer, primaries)
+CONVERSIONS = [
+    (10, 1, 1, 9, False, 2, 270, 480, 14, 9),  # BT.2020 SDR: BT.2020 matrix and primaries
+    (8, 0, 0, 1, True, 0, 256, 320, 13, 1),    # sRGB transfer, full-range 4:4:4
+    (12, 1, 0, 6, False, 0, 256, 256, 4, 9),   # gamma 2.2 with BT.2020 primaries
+    (10, 1, 1, 1, False, 0, 144, 256, 8, 1),   # linear-light samples
+]
+
+
+@pytest.mark.parametrize("fmt", CONVERSIONS, ids=lambda f: f"trc{f[8]}-pri{f[9]}")
+def test_transfer_and_primaries(vlib, fmt):
+    """Frames in another transfer / primaries: the GPU takes them to linear BT.709 light and the
+    metric skips its own linearisation; the reference path gets R'G'B' planes that linearise to
+    the same light (2.4 power law of the FP64 conversion)."""
+    bits, ssw, ssh, matrix, full, loc, h, w, trc, pri = fmt
+    ref, dist = synth.yuv_frames(h, w, 2, bits, ssw, ssh, full, seed=4, distortion="dct")
+    dt = np.uint8 if bits == 8 else np.uint16
+    host = lambda f: [np.ascontiguousarray(p.numpy().astype(dt)) for p in f]
+    rgb = lambda f: float_planes(synth.yuv_to_rgb(f, bits, ssw, ssh, matrix, full, loc, transfer=trc, primaries=pri))
+    fm = vlib.yuv_format(bits, (ssw, ssh), matrix, full, loc, trc, pri)
+    with vlib.SSIMU2Handler(w, h) as hd:
+        hd.set_yuv_format(fm)
+        s_yuv = hd.compute_yuv(host(ref), host(dist))
+        s_rgb = hd.compute(rgb(ref), rgb(dist))
+    assert abs(s_yuv - s_rgb) < 2e-4, (s_yuv, s_rgb)
+    with vlib.ButteraugliHandler(w, h) as hd:
+        hd.set_yuv_format(fm)
+        n_yuv = hd.compute_yuv(host(ref), host(dist))
+        n_rgb = hd.compute(rgb(ref), rgb(dist))
+    for a, b in zip(n_yuv, n_rgb):
+        assert abs(a - b) <= 2e-5 * abs(b), (n_yuv, n_rgb)
+
+
 def test_default_format_unchanged(vlib):
     """A handler whose format was changed still scores the Yuv420p10 calls in 10-bit 4:2:0."""
     ref, dist = synth.yuv420p10_frames(96, 130, 1, seed=5)
@@ -76,7 +109,8 @@ def test_default_format_unchanged(vlib):
 def test_bad_formats_rejected(vlib):
     with vlib.SSIMU2Handler(64, 64) as hd:
         for f in [vlib.yuv_format(7), vlib.yuv_format(17), vlib.yuv_format(10, (2, 1)), vlib.yuv_format(10, matrix=3),
-                  vlib.yuv_format(10, chroma_location=6)]:
+                  vlib.yuv_format(10, chroma_location=6), vlib.yuv_format(10, transfer=16),
+                  vlib.yuv_format(10, primaries=12)]:
             with pytest.raises(vlib.VshipError):
                 hd.set_yuv_format(f)
 

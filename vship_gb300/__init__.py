@@ -70,14 +70,18 @@ _IP = ctypes.POINTER(ctypes.c_int)
 class YuvFormat(ctypes.Structure):
     """Vship_YuvFormat: bits 8..16, log2 chroma subsampling, H.273 matrix (2 = by height), range
     (0 limited, 1 full), chroma location (0 left, 1 center, 2 top-left, 3 top, 4 bottom-left,
-    5 bottom)."""
+    5 bottom), transfer and primaries (H.273 ids)."""
     _fields_ = [("bits", ctypes.c_int), ("subsampling_w", ctypes.c_int), ("subsampling_h", ctypes.c_int),
-                ("matrix", ctypes.c_int), ("range", ctypes.c_int), ("chroma_location", ctypes.c_int)]
+                ("matrix", ctypes.c_int), ("range", ctypes.c_int), ("chroma_location", ctypes.c_int),
+                ("transfer", ctypes.c_int), ("primaries", ctypes.c_int)]
 
 
-def yuv_format(bits=10, subsampling=(1, 1), matrix=1, full_range=False, chroma_location=0) -> YuvFormat:
+def yuv_format(bits=10, subsampling=(1, 1), matrix=1, full_range=False, chroma_location=0, transfer=1,
+               primaries=1) -> YuvFormat:
+    """H.273 ids: transfer 1/6/14/15/2 (BT.709 family), 13 sRGB, 4 gamma 2.2, 5 gamma 2.8, 8 linear;
+    primaries 1/2 BT.709, 9 BT.2020."""
     return YuvFormat(int(bits), int(subsampling[0]), int(subsampling[1]), int(matrix), 1 if full_range else 0,
-                     int(chroma_location))
+                     int(chroma_location), int(transfer), int(primaries))
 
 
 class ServeRequest(ctypes.Structure):

@@ -65,7 +65,8 @@ struct HandleTable {
 };
 
 bool yuv_from_format(const Vship_YuvFormat& f, int64_t height, YuvParams* out) {
-    return make_yuv_params(f.bits, f.subsampling_w, f.subsampling_h, f.matrix, f.range, f.chroma_location, height, out);
+    return make_yuv_params(f.bits, f.subsampling_w, f.subsampling_h, f.matrix, f.range, f.chroma_location, height, out,
+                           f.transfer, f.primaries);
 }
 
 Vship_Exception to_exc(int e) {
@@ -716,7 +717,7 @@ Vship_Exception Vship_MultiSetYuvFormat(Vship_MultiHandler handler, const Vship_
     if (!f) return Vship_BadPointer;
     DeviceGuard dg(h->eng.device);
     return to_exc(h->eng.set_yuv_format(f->bits, f->subsampling_w, f->subsampling_h, f->matrix, f->range,
-                                        f->chroma_location));
+                                        f->chroma_location, f->transfer, f->primaries));
 }
 
 int Vship_MultiKnobs(Vship_MultiHandler handler, char* out_json, int len) {
@@ -758,7 +759,7 @@ Vship_Exception Vship_ServeSetYuvFormat(Vship_ServeHandler handler, const Vship_
     if (!h) return Vship_BadHandler;
     if (!f) return Vship_BadPointer;
     return to_exc(h->srv.set_yuv_format(f->bits, f->subsampling_w, f->subsampling_h, f->matrix, f->range,
-                                        f->chroma_location));
+                                        f->chroma_location, f->transfer, f->primaries));
 }
 
 Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* q) {

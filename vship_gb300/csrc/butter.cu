@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
             load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, v[0], v[1], v[2]);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                v[c] = to_linear_fast(v[c]);
+                if (!(IT == IN_YUV && yp.linear_out)) v[c] = to_linear_fast(v[c]);
                 iplane(ib, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
             }
         }

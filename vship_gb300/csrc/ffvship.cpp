@@ -413,7 +413,7 @@ int main(int argc, char** argv) {
     }
     const int bits = std::max(src.bits, enc.bits);
     const int bytes = bits > 8 ? 2 : 1;
-    Vship_YuvFormat yfmt{bits, src.ssw, src.ssh, 2, src.full, src.loc};
+    Vship_YuvFormat yfmt{bits, src.ssw, src.ssh, 2, src.full, src.loc, 2, 2};
     const int w = src.w - cs.left - cs.right, h = src.h - cs.top - cs.bottom;
     if (w != enc.w - ce.left - ce.right || h != enc.h - ce.top - ce.bottom || w <= 0 || h <= 0) {
         std::cerr << "DifferingInputType: source and encoded differ in size after cropping\n";

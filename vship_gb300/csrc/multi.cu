@@ -498,10 +498,11 @@ int MultiEngine::autotune(int npairs, cudaStream_t st) {
     return upload_items(st);
 }
 
-int MultiEngine::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc) {
+int MultiEngine::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc, int transfer, int primaries) {
     YuvParams p[kMaxRes];
     for (int r = 0; r < nres; r++)
-        if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r])) return E_BAD_POINTER;
+        if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r], transfer, primaries))
+            return E_BAD_POINTER;
     for (int r = 0; r < nres; r++) yuv_r[r] = p[r];
     if (gexec) {  // the Butteraugli launches carry the format as a kernel argument
         cudaGraphExecDestroy(gexec);

@@ -63,7 +63,8 @@ public:
     int compute(int nsrc, const FrameDesc* src, const int* src_res, int npairs, const FrameDesc* cand,
                 const int* cand_src, int intype, double* ssimu2_dev, double* butter_dev, cudaStream_t st);
     // Format of IN_YUV frames for every resolution (make_yuv_params; matrix 2 resolves per height).
-    int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc);
+    int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc, int transfer = 1,
+                       int primaries = 1);
     // The knobs in use as JSON ({"grid_per_sm": g, "order": o, "source": "default|cache|tuned"}).
     std::string knobs_json() const;
     static size_t device_bytes(int nres, const int* widths, const int* heights, const int* max_sources,

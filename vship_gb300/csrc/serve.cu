@@ -103,10 +103,11 @@ int Server::submit(ServeReq* r) {
     return E_OK;
 }
 
-int Server::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc) {
+int Server::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc, int transfer, int primaries) {
     YuvParams p[kMaxRes];
     for (int r = 0; r < nres; r++)
-        if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r])) return E_BAD_POINTER;
+        if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r], transfer, primaries))
+            return E_BAD_POINTER;
     std::lock_guard<std::mutex> g(mu);
     for (int r = 0; r < nres; r++) yuv_r[r] = p[r];
     return E_OK;

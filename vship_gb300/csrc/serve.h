@@ -57,7 +57,8 @@ public:
     int submit(ServeReq* r);  // takes ownership (deleted after completion)
     int poll(ServeDone* out, int max, double timeout_s);
     // Format of IN_YUV frames for every resolution (make_yuv_params; matrix 2 resolves per height).
-    int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc);
+    int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc, int transfer = 1,
+                       int primaries = 1);
     int drain();
     std::string stats_json();
     void destroy();

@@ -134,9 +134,11 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
             float v0 = 0.f, v1 = 0.f, v2 = 0.f;
             if (gx < L.w && gy < L.h) {
                 load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, v0, v1, v2);
-                v0 = to_linear_fast(v0);
-                v1 = to_linear_fast(v1);
-                v2 = to_linear_fast(v2);
+                if (!(IT == IN_YUV && yp.linear_out)) {  // frames converted to linear light skip x^2.4
+                    v0 = to_linear_fast(v0);
+                    v1 = to_linear_fast(v1);
+                    v2 = to_linear_fast(v2);
+                }
                 float X = v0, Y = v1, B = v2;
                 positive_xyb(X, Y, B);
                 pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);

@@ -218,10 +218,39 @@ def _upsample_axis(c: torch.Tensor, n: int, ss: int, s: int, axis: int) -> torch
     return a * (1 - f) + b * f
 
 
-def yuv_to_rgb(yuv, bits=10, ssw=1, ssh=1, matrix=1, full=False, loc=0, dtype=torch.float32) -> torch.Tensor:
+def _bt2020_to_bt709() -> np.ndarray:
+    def npm(xy):
+        P = np.array([[x / y for x, y in xy[:3]], [1.0, 1.0, 1.0], [(1 - x - y) / y for x, y in xy[:3]]])
+        wx, wy = xy[3]
+        W = np.array([wx / wy, 1.0, (1 - wx - wy) / wy])
+        return P * np.linalg.solve(P, W)[None, :]
+    d65 = (0.3127, 0.3290)
+    a = npm([(0.640, 0.330), (0.300, 0.600), (0.150, 0.060), d65])
+    b = npm([(0.708, 0.292), (0.170, 0.797), (0.131, 0.046), d65])
+    return np.linalg.solve(a, b)
+
+
+def _eotf(v: torch.Tensor, transfer: int) -> torch.Tensor:
+    a = v.abs()
+    if transfer == 13:
+        l = torch.where(a <= 0.04045, a / 12.92, ((a + 0.055) / 1.055) ** 2.4)
+    elif transfer in (4, 5):
+        l = a ** (2.2 if transfer == 4 else 2.8)
+    elif transfer == 8:
+        l = a
+    else:
+        l = a ** 2.4
+    return torch.sign(v) * l
+
+
+def yuv_to_rgb(yuv, bits=10, ssw=1, ssh=1, matrix=1, full=False, loc=0, dtype=torch.float32, transfer=1,
+               primaries=1) -> torch.Tensor:
     """Y'CbCr planes of the given format -> full-range R'G'B' (3, h, w) in [0, 1], in FP64: chroma
     upsampled bilinearly at its siting (edge samples clamped), the matrix (H.273 id; 2 = BT.709
-    above 650 rows, BT.470BG below) and range applied, clamped."""
+    above 650 rows, BT.470BG below) and range applied, clamped. A transfer outside the BT.709
+    family (H.273 13 sRGB, 4 / 5 gamma 2.2 / 2.8, 8 linear) or BT.2020 primaries (9): the samples
+    go to linear light, to BT.709 primaries, are clamped there, and come back as the 2.4 power law
+    the metrics linearise with."""
     Y, U, V = [p.to(torch.float64) for p in yuv]
     h, w = Y.shape
     if matrix == 2:
@@ -237,7 +266,14 @@ def yuv_to_rgb(yuv, bits=10, ssw=1, ssh=1, matrix=1, full=False, loc=0, dtype=to
     r = y + 2.0 * (1.0 - kr) * cr
     b = y + 2.0 * (1.0 - kb) * cb
     g = y - (2.0 * (1.0 - kb) * kb / kg) * cb - (2.0 * (1.0 - kr) * kr / kg) * cr
-    return torch.stack([r, g, b]).clamp_(0.0, 1.0).to(dtype)
+    rgb = torch.stack([r, g, b])
+    if transfer in (1, 2, 6, 14, 15) and primaries in (1, 2):
+        return rgb.clamp_(0.0, 1.0).to(dtype)
+    lin = _eotf(rgb, transfer)
+    if primaries == 9:
+        m = torch.from_numpy(_bt2020_to_bt709()).to(lin)
+        lin = torch.einsum("ij,jhw->ihw", m, lin)
+    return lin.clamp_(0.0, 1.0).pow_(1.0 / 2.4).to(dtype)
 
 
 def yuv_frames(h: int, w: int, t: int, bits=10, ssw=1, ssh=1, full=False, seed: int = 7, distortion="dct",
