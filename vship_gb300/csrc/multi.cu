@@ -103,6 +103,11 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
     device_name = prop.name;
     VSHIP_CUDA_TRY(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
     VSHIP_CUDA_TRY(cudaEventCreateWithFlags(&staging_free, cudaEventDisableTiming));
+    VSHIP_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    for (int i = 0; i <= kMaxRes; i++) {
+        VSHIP_CUDA_TRY(cudaStreamCreateWithFlags(&side[i], cudaStreamNonBlocking));
+        VSHIP_CUDA_TRY(cudaEventCreateWithFlags(&ev_join[i], cudaEventDisableTiming));
+    }
 
     if (flags & MULTI_SSIMU2) {
         int rc = ssimu2_multi_prepare();
@@ -187,6 +192,17 @@ void MultiEngine::destroy() {
     b_perm_d = nullptr;
     if (staging_free) cudaEventDestroy(staging_free);
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    ev_fork = nullptr;
+    for (int i = 0; i <= kMaxRes; i++) {
+        if (side[i]) {
+            cudaStreamSynchronize(side[i]);
+            cudaStreamDestroy(side[i]);
+        }
+        if (ev_join[i]) cudaEventDestroy(ev_join[i]);
+        side[i] = nullptr;
+        ev_join[i] = nullptr;
+    }
     staging_free = nullptr;
     cap_stream = nullptr;
 }
@@ -365,27 +381,51 @@ void MultiEngine::fill_images(int nsrc, const FrameDesc* src, int npairs, const 
 
 // The whole launch sequence of one batch (captured into the graph, or run directly).
 int MultiEngine::enqueue(int npairs, cudaStream_t st) {
+    // Fork: SSIMULACRA2 on one side stream, the Butteraugli chunks of each resolution on that
+    // resolution's side stream (chunks of one resolution share its workspace, so they stay in
+    // order), joined back into st. Kernels with different limits (the FMA-bound stats and diff
+    // kernels, the memory-heavy vertical blurs) then fill each other's gaps.
+    VSHIP_CUDA_TRY(cudaEventRecord(ev_fork, st));
     int rc = E_OK;
+    int joins = 0;
     if (flags & MULTI_SSIMU2) {
+        cudaStream_t s2 = side[kMaxRes];
+        VSHIP_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
         const bool fp16 = (flags & MULTI_FP16) != 0;
-        rc = ssimu2_multi_pyramid(s_imgs_d, s_pitems_d, n_pitems_src, geoms_d, plan_intype, false, st);
+        rc = ssimu2_multi_pyramid(s_imgs_d, s_pitems_d, n_pitems_src, geoms_d, plan_intype, false, s2);
         if (!rc) rc = ssimu2_multi_pyramid(s_imgs_d, s_pitems_d + n_pitems_src, n_pitems_cand, geoms_d, plan_intype,
-                                           fp16, st);
+                                           fp16, s2);
         const int grid = knobs.grid_per_sm > 0 ? knobs.grid_per_sm * sms : n_sitems;
-        if (!rc) rc = ssimu2_multi_stats(s_pairs_d, s_sitems_d, n_sitems, geoms_d, fp16, grid, st);
-        if (!rc) rc = ssimu2_multi_finalize(s_pairs_d, npairs, geoms_d, st);
+        if (!rc) rc = ssimu2_multi_stats(s_pairs_d, s_sitems_d, n_sitems, geoms_d, fp16, grid, s2);
+        if (!rc) rc = ssimu2_multi_finalize(s_pairs_d, npairs, geoms_d, s2);
+        VSHIP_CUDA_TRY(cudaEventRecord(ev_join[kMaxRes], s2));
+        VSHIP_CUDA_TRY(cudaStreamWaitEvent(st, ev_join[kMaxRes], 0));
+        joins++;
         if (rc) return rc;
     }
     if (flags & MULTI_BUTTERAUGLI) {
+        bool used[kMaxRes] = {};
         for (const BChunk& c : b_chunks) {
+            cudaStream_t sr = side[c.res];
+            if (!used[c.res]) {
+                VSHIP_CUDA_TRY(cudaStreamWaitEvent(sr, ev_fork, 0));
+                used[c.res] = true;
+            }
             rc = b_eng[c.res].launch_images(b_frames_d + c.img_off, c.nimg, b_pimg_d + c.pair_off, c.npairs,
-                                            plan_intype, b_norms_d + 3 * c.pair_off, nullptr, st, &yuv_r[c.res]);
+                                            plan_intype, b_norms_d + 3 * c.pair_off, nullptr, sr, &yuv_r[c.res]);
             if (rc) return rc;
         }
+        for (int r = 0; r < nres; r++)
+            if (used[r]) {
+                VSHIP_CUDA_TRY(cudaEventRecord(ev_join[r], side[r]));
+                VSHIP_CUDA_TRY(cudaStreamWaitEvent(st, ev_join[r], 0));
+                joins++;
+            }
         multi_scatter_norms_kernel<<<(unsigned)ceil_div(3 * npairs, 256), 256, 0, st>>>(
             b_norms_d, b_perm_d, b_norms_d + 3 * pair_cap, npairs);
         VSHIP_CUDA_TRY(cudaGetLastError());
     }
+    (void)joins;
     return E_OK;
 }
 

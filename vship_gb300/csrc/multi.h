@@ -111,6 +111,8 @@ private:
     const char* knobs_source = "default";
 
     cudaStream_t cap_stream = nullptr;
+    cudaStream_t side[kMaxRes + 1]{};  // per-resolution Butteraugli streams, then SSIMULACRA2's
+    cudaEvent_t ev_fork = nullptr, ev_join[kMaxRes + 1]{};
     cudaGraphExec_t gexec = nullptr;
     cudaEvent_t staging_free = nullptr;
 
