@@ -64,6 +64,20 @@ def ssimu2_stats_bytes(w, h):
     return 2 * 3 * 4 * total_scale_pixels(w, h)
 
 
+def ssimu2_stats_flops(w, h):
+    """Algorithmic FP32 work of the stats kernel per pair: per channel and pyramid pixel, the
+    17-tap horizontal and vertical passes over four moments (136 FMA = 272 FLOP); the maps and
+    pooling (a few tens of FLOP) and the vertical halo of the horizontal pass are not counted."""
+    return 272 * 3 * total_scale_pixels(w, h)
+
+
+def fp32_peak_tflops(clock_mhz):
+    """Dense FP32 FMA peak at the sampled SM clock: 128 FMA lanes per SM per cycle, 2 FLOP each."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    return sms * 128 * 2 * clock_mhz * 1e6 / 1e12
+
+
 def butter_diff_bytes(w, h):
     n = w * h
     nh = ((w - 1) // 2 + 1) * ((h - 1) // 2 + 1)
@@ -450,6 +464,15 @@ def bench_workload(v, kind, args, ws, rank):
     pairs_per_launch = npairs * args.steps / max(n_launch, 1)
     traffic = ncu_traffic(kname)
     total_kernel_ms = sum(t for _, t in prof.values())
+    fp32_roof = None
+    if kind == "ssimu2" and tot_ms > 0:
+        # the stats kernel is bound by the FP32 pipe, not by HBM: its arithmetic against the FP32 peak
+        mhz = clocks.get("sm_mhz") or 2070.0
+        tf = ssimu2_stats_flops(w, h) * npairs * args.steps / (tot_ms / 1e3) / 1e12
+        pk = fp32_peak_tflops(mhz)
+        fp32_roof = {"kernel": kname, "achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
+                     "flops_per_pair": ssimu2_stats_flops(w, h),
+                     "peak_source": f"128 FP32 FMA lanes x SMs x {mhz:.0f} MHz (sampled clock)"}
     del ref16, dst16
     torch.cuda.empty_cache()
     # 10-bit 4:2:0 planes converted on the GPU (a quarter of the bytes of float RGB)
@@ -470,6 +493,7 @@ def bench_workload(v, kind, args, ws, rank):
         "e2e": {"value": e2e_value, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "threads": args.e2e_threads, "steps": args.e2e_steps,
                 "call": "Vship_ComputeSSIMU2Uint16" if kind == "ssimu2" else "Vship_ComputeButteraugliUint16v3"},
+        "fp32_roofline": fp32_roof,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic * pairs_per_launch if traffic is not None else None,
@@ -887,7 +911,8 @@ def main_ours(args):
                    "pairs_per_step": args.pairs,
                    "parallelism": f"replicas x{ws}", "l2": "inputs 12 GB > L2, no flush",
                    "launch_chunk_pairs": args.chunk},
-        "e2e": s2["e2e"], "roofline": s2["roofline"], "gpu_launches": s2["gpu_launches"], "clocks": s2["clocks"],
+        "e2e": s2["e2e"], "roofline": s2["roofline"], "fp32_roofline": s2["fp32_roofline"],
+        "gpu_launches": s2["gpu_launches"], "clocks": s2["clocks"],
         "kernel_share": s2["kernel_share"], "pipeline_bytes_per_pair": s2["pipeline_bytes_per_pair"],
         "yuv420p10": s2["yuv420p10"], "float32_rgb": s2["float32_rgb"], "input": s2["input"],
         "score_check": s2["score_check"],

@@ -97,3 +97,39 @@ def test_4k_pair(vlib, orc):
         got = hd.compute(a, b)
     want = orc.butteraugli(a, b, precision=64)
     assert close_norms(got, want), (got, want)
+
+
+def test_threads_on_own_and_shared_handlers(vlib):
+    """test/apibenchmark.cpp:132-157 drives Butteraugli from 3 threads that share one handler
+    (which the reference's API does not allow); here threads on their own handlers and threads
+    sharing one (calls on one handler are serialised) give the single-thread results."""
+    import threading
+    pairs = [grating_float_pair(96, 128, t=t, distortion="blur_noise") for t in range(6)]
+    with vlib.ButteraugliHandler(128, 96, 2, 80.0) as hd:
+        want = [hd.compute(a, b) for a, b in pairs]
+    for shared in (False, True):
+        got = [None] * len(pairs)
+        common = vlib.ButteraugliHandler(128, 96, 2, 80.0) if shared else None
+
+        def worker(k):
+            h = common or vlib.ButteraugliHandler(128, 96, 2, 80.0)
+            for i in range(k, len(pairs), 3):
+                got[i] = h.compute(*pairs[i])
+            if not shared:
+                h.free()
+
+        th = [threading.Thread(target=worker, args=(k,)) for k in range(3)]
+        [t.start() for t in th]
+        [t.join() for t in th]
+        if common:
+            common.free()
+        assert got == want, shared
+
+
+def test_init_rejects_bad_sizes(vlib):
+    L = vlib.lib()
+    import ctypes
+    h = vlib.Handler()
+    for w, hh in [(0, 10), (10, 0), (-4, 8)]:
+        assert L.Vship_ButteraugliInitv2(ctypes.byref(h), w, hh, 2, ctypes.c_float(203.0)) == vlib.BadPointer
+        assert L.Vship_SSIMU2Init(ctypes.byref(h), w, hh) == vlib.BadPointer
