@@ -379,7 +379,7 @@ typedef struct {
 } Vship_ServeRequest;
 typedef struct {
     uint64_t request_id;
-    int status; /* Vship_Exception */
+    int status; /* Vship_Exception, or Vship_ServeCancelled */
     double latency_seconds;
 } Vship_ServeCompletion;
 EXPORTPREPROCESS Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, int nres, const int* widths,
@@ -392,6 +392,11 @@ EXPORTPREPROCESS Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, 
 EXPORTPREPROCESS Vship_Exception Vship_ServeSetYuvFormat(Vship_ServeHandler handler, const Vship_YuvFormat* format);
 /* Vship_OutOfVRAM: the request's charge alone exceeds admission_bytes. */
 EXPORTPREPROCESS Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* request);
+/* Withdraws a request still waiting in the queue: it is reported at once with status
+ * Vship_ServeCancelled. Vship_BadPointer when no queued request has this id (it is already on
+ * the GPU, done, or unknown). */
+#define Vship_ServeCancelled (-1)
+EXPORTPREPROCESS Vship_Exception Vship_ServeCancel(Vship_ServeHandler handler, uint64_t request_id);
 /* Up to max completions, waiting up to timeout_seconds for the first; returns how many. */
 EXPORTPREPROCESS int Vship_ServePoll(Vship_ServeHandler handler, Vship_ServeCompletion* out, int max,
                                      double timeout_seconds);

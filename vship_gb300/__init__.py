@@ -155,6 +155,7 @@ SIGNATURES = {
     "Vship_ServeSubmit": (_E, [_H, ctypes.POINTER(ServeRequest)]),
     "Vship_ServePoll": (ctypes.c_int, [_H, ctypes.POINTER(ServeCompletion), ctypes.c_int, ctypes.c_double]),
     "Vship_ServeDrain": (_E, [_H]),
+    "Vship_ServeCancel": (_E, [_H, ctypes.c_uint64]),
     "Vship_ServeStats": (ctypes.c_int, [_H, ctypes.c_char_p, ctypes.c_int]),
     "Vship_ServeDestroy": (_E, [_H]),
     "Vship_SSIMU2SetYuvFormat": (_E, [_H, ctypes.POINTER(YuvFormat)]),
@@ -284,8 +285,9 @@ class SSIMU2Handler:
 
     def __init__(self, width: int, height: int):
         self.width, self.height = int(width), int(height)
-        self._h = Handler()
-        _check(lib().Vship_SSIMU2Init(ctypes.byref(self._h), self.width, self.height), "Vship_SSIMU2Init")
+        h = Handler()
+        _check(lib().Vship_SSIMU2Init(ctypes.byref(h), self.width, self.height), "Vship_SSIMU2Init")
+        self._h = h  # only a created handler is ever freed
 
     def compute(self, reference, distorted) -> float:
         a1, s1, w, h, dt, k1 = planes_of(reference)
@@ -345,9 +347,10 @@ class ButteraugliHandler:
     def __init__(self, width: int, height: int, qnorm: int = 2, intensity_multiplier: float = 203.0):
         self.width, self.height = int(width), int(height)
         self.qnorm, self.intensity = int(qnorm), float(intensity_multiplier)
-        self._h = Handler()
-        _check(lib().Vship_ButteraugliInitv2(ctypes.byref(self._h), self.width, self.height, self.qnorm,
+        h = Handler()
+        _check(lib().Vship_ButteraugliInitv2(ctypes.byref(h), self.width, self.height, self.qnorm,
                                              ctypes.c_float(self.intensity)), "Vship_ButteraugliInitv2")
+        self._h = h  # only a created handler is ever freed
 
     def compute(self, reference, distorted, distmap: bool = False):
         """Returns (norm_q, norm_3, norm_inf) and, with distmap=True, the float32 (H, W) map."""
@@ -415,9 +418,10 @@ class SSIMU2Batch:
 
     def __init__(self, width: int, height: int, max_pairs: int):
         self.width, self.height, self.max_pairs = int(width), int(height), int(max_pairs)
-        self._h = Handler()
-        _check(lib().Vship_SSIMU2BatchInit(ctypes.byref(self._h), self.width, self.height, self.max_pairs),
+        h = Handler()
+        _check(lib().Vship_SSIMU2BatchInit(ctypes.byref(h), self.width, self.height, self.max_pairs),
                "Vship_SSIMU2BatchInit")
+        self._h = h  # only a created handler is ever freed
 
     def set_yuv_format(self, fmt: YuvFormat) -> None:
         _check(lib().Vship_SSIMU2SetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_SSIMU2SetYuvFormat")
@@ -445,10 +449,11 @@ class ButteraugliBatch:
 
     def __init__(self, width: int, height: int, max_pairs: int, qnorm: int = 2, intensity_multiplier: float = 203.0):
         self.width, self.height, self.max_pairs = int(width), int(height), int(max_pairs)
-        self._h = Handler()
-        _check(lib().Vship_ButteraugliBatchInit(ctypes.byref(self._h), self.width, self.height, int(qnorm),
+        h = Handler()
+        _check(lib().Vship_ButteraugliBatchInit(ctypes.byref(h), self.width, self.height, int(qnorm),
                                                 ctypes.c_float(intensity_multiplier), self.max_pairs),
                "Vship_ButteraugliBatchInit")
+        self._h = h  # only a created handler is ever freed
 
     def set_yuv_format(self, fmt: YuvFormat) -> None:
         _check(lib().Vship_ButteraugliSetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_ButteraugliSetYuvFormat")
@@ -501,11 +506,12 @@ class MultiScorer:
         self.resolutions = [(int(w), int(h)) for w, h in resolutions]
         self.flags = int(flags)
         n = len(self.resolutions)
-        self._h = Handler()
-        _check(lib().Vship_MultiInit(ctypes.byref(self._h), n, _ints([w for w, _ in self.resolutions]),
+        h = Handler()
+        _check(lib().Vship_MultiInit(ctypes.byref(h), n, _ints([w for w, _ in self.resolutions]),
                                      _ints([h for _, h in self.resolutions]), _ints(max_sources), _ints(max_pairs),
                                      self.flags, int(qnorm), ctypes.c_float(intensity_multiplier),
                                      tune_cache.encode() if tune_cache else None), "Vship_MultiInit")
+        self._h = h  # only a created handler is ever freed
 
     @staticmethod
     def device_bytes(resolutions, max_sources, max_pairs, flags=MULTI_SSIMU2) -> int:
@@ -547,6 +553,7 @@ class MultiScorer:
 
 
 SERVE_SSIMU2, SERVE_BUTTERAUGLI = 0, 1
+SERVE_CANCELLED = -1
 SERVE_FP32_CANDIDATES = 1
 
 
@@ -558,13 +565,14 @@ class Server:
     def __init__(self, resolutions, input_type=4, admission_bytes=64 << 30, cache_bytes=16 << 30,
                  max_batch_pairs=256, flags=0, qnorm=2, intensity_multiplier=203.0):
         self.resolutions = [(int(w), int(h)) for w, h in resolutions]
-        self._h = Handler()
+        h = Handler()
         self._live = {}
-        _check(lib().Vship_ServeCreate(ctypes.byref(self._h), len(self.resolutions),
+        _check(lib().Vship_ServeCreate(ctypes.byref(h), len(self.resolutions),
                                        _ints([w for w, _ in self.resolutions]), _ints([h for _, h in self.resolutions]),
                                        int(input_type), int(admission_bytes), int(cache_bytes), int(max_batch_pairs),
                                        int(flags), int(qnorm), ctypes.c_float(intensity_multiplier)),
                "Vship_ServeCreate")
+        self._h = h  # only a created handler is ever freed
 
     def submit(self, request_id, metric, resolution, source_key, source, candidates, out):
         """source / candidates: (planes, stride_bytes[, chroma_stride_bytes]) of device pointers;
@@ -595,6 +603,11 @@ class Server:
 
     def set_yuv_format(self, fmt: YuvFormat) -> None:
         _check(lib().Vship_ServeSetYuvFormat(self._h, ctypes.byref(fmt)), "Vship_ServeSetYuvFormat")
+
+    def cancel(self, request_id) -> bool:
+        """True when the request was still queued and is withdrawn (reported with status
+        SERVE_CANCELLED)."""
+        return lib().Vship_ServeCancel(self._h, int(request_id)) == 0
 
     def drain(self):
         _check(lib().Vship_ServeDrain(self._h), "Vship_ServeDrain")

@@ -84,7 +84,7 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None) -> str:
             jobs.append("vs_plugin")
         objs.append(obj)
     if jobs or not os.path.exists(LIB):
-        run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
+        run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-ldl"])
     cli_src = os.path.join(CSRC, "ffvship.cpp")
     if _needs_rebuild(CLI, [cli_src, LIB, os.path.join(ROOT, "include", "VshipAPI.h")]):
         # the FFVship-compatible command-line tool, linked against the library next to it

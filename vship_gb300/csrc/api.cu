@@ -125,8 +125,8 @@ struct HostPath {
         TRY_CUDA(cudaGetDevice(&device));
         TRY_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
         const size_t plane4 = (size_t)w * 4 * h;
-        TRY_CUDA(cudaMalloc(&staging, plane4 * 6));
-        TRY_CUDA(cudaMalloc(&frames_d, sizeof(FrameDesc) * 6));
+        TRY_CUDA(vship_malloc((void**)&staging, plane4 * 6));
+        TRY_CUDA(vship_malloc((void**)&frames_d, sizeof(FrameDesc) * 6));
         FrameDesc fd[6];
         for (int bps = 2, k = 0; bps <= 4; bps += 2, k++)
             for (int m = 0; m < 2; m++) {
@@ -143,7 +143,7 @@ struct HostPath {
         yuv_stride = w * 2;
         yuv_stride_c = ((w + 1) / 2) * 2;
         TRY_CUDA(cudaMemcpy(frames_d, fd, sizeof(fd), cudaMemcpyHostToDevice));
-        if (cudaMallocHost(&result_h, result_bytes) != cudaSuccess) return E_OUT_OF_RAM;
+        if (vship_malloc_host((void**)&result_h, result_bytes) != cudaSuccess) return E_OUT_OF_RAM;
         return E_OK;
     }
     void destroy() {
@@ -433,7 +433,7 @@ Vship_Exception Vship_GPUFullCheck(int gpu_id) {
     if (cudaSetDevice(gpu_id) != cudaSuccess) return Vship_BadDeviceCode;
     int* d = nullptr;
     int v = 0;
-    if (cudaMalloc(&d, sizeof(int)) != cudaSuccess) return Vship_BadDeviceCode;
+    if (vship_malloc((void**)&d, sizeof(int)) != cudaSuccess) return Vship_BadDeviceCode;
     cudaMemset(d, 0, sizeof(int));
     probe_kernel<<<1, 1>>>(d);
     cudaError_t e = cudaMemcpy(&v, d, sizeof(int), cudaMemcpyDeviceToHost);
@@ -454,7 +454,7 @@ int Vship_GetErrorMessage(Vship_Exception exception, char* out_message, int len)
 
 Vship_Exception Vship_PinnedMalloc(void** ptr, uint64_t size) {
     if (!ptr) return Vship_BadPointer;
-    if (cudaMallocHost(ptr, size) != cudaSuccess) return Vship_OutOfRAM;
+    if (vship_malloc_host(ptr, size) != cudaSuccess) return Vship_OutOfRAM;
     return Vship_NoError;
 }
 
@@ -776,6 +776,12 @@ Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeR
     std::memcpy(r->cands.data(), q->candidates, sizeof(FrameDesc) * q->npairs);
     r->out = q->results;
     return to_exc(h->srv.submit(r));
+}
+
+Vship_Exception Vship_ServeCancel(Vship_ServeHandler handler, uint64_t request_id) {
+    ServeHandle* h = g_serve.get(handler.id);
+    if (!h) return Vship_BadHandler;
+    return to_exc(h->srv.cancel(request_id));
 }
 
 int Vship_ServePoll(Vship_ServeHandler handler, Vship_ServeCompletion* out, int max, double timeout_seconds) {

@@ -1100,7 +1100,7 @@ int butter_norm_tiles(int64_t w, int64_t h) { return make_bgeom(w, h).norm_tiles
 int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensity_, int max_pairs_) {
     int rc = init_images(width, height, qnorm_, intensity_, 2 * max_pairs_, max_pairs_, true);
     if (rc) return rc;
-    VSHIP_CUDA_TRY(cudaMalloc(&pimg_identity, sizeof(int2) * max_pairs));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&pimg_identity, sizeof(int2) * max_pairs));
     butter_identity_pairs_kernel<<<(unsigned)ceil_div(max_pairs, 256), 256>>>(pimg_identity, max_pairs);
     VSHIP_CUDA_TRY(cudaGetLastError());
     VSHIP_CUDA_TRY(cudaDeviceSynchronize());
@@ -1126,13 +1126,13 @@ int ButterEngine::init_images(int64_t width, int64_t height, int qnorm_, float i
     norm_blocks = g.norm_tiles;
     int rc = butter_prepare_device();
     if (rc) return rc;
-    VSHIP_CUDA_TRY(cudaMalloc(&work, sizeof(float) * img_floats * max_images));
-    VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
-    if (keep_distmap) VSHIP_CUDA_TRY(cudaMalloc(&distmap, sizeof(float) * (size_t)w * h * max_pairs));
-    VSHIP_CUDA_TRY(cudaMalloc(&norms, sizeof(double) * 3 * max_pairs));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&work, sizeof(float) * img_floats * max_images));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&partials, sizeof(float) * 3 * (size_t)norm_blocks * max_pairs));
+    if (keep_distmap) VSHIP_CUDA_TRY(vship_malloc((void**)&distmap, sizeof(float) * (size_t)w * h * max_pairs));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&norms, sizeof(double) * 3 * max_pairs));
     std::vector<float*> bases(max_images);
     for (int i = 0; i < max_images; i++) bases[i] = work + (size_t)i * img_floats;
-    VSHIP_CUDA_TRY(cudaMalloc(&ibase, sizeof(float*) * max_images));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&ibase, sizeof(float*) * max_images));
     VSHIP_CUDA_TRY(cudaMemcpy(ibase, bases.data(), sizeof(float*) * max_images, cudaMemcpyHostToDevice));
     return E_OK;
 }

@@ -120,22 +120,23 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
         for (int r = 0; r < nres; r++) {
             geoms_h[r] = make_ssimu2_geom(rw[r], rh[r]);
             const size_t pe = (size_t)geoms_h[r].plane_elems;
-            if (max_src[r]) VSHIP_CUDA_TRY(cudaMalloc(&s_src[r], (size_t)max_src[r] * 3 * pe * 4));
+            if (max_src[r]) VSHIP_CUDA_TRY(vship_malloc((void**)&s_src[r], (size_t)max_src[r] * 3 * pe * 4));
             if (max_pairs[r]) {
-                VSHIP_CUDA_TRY(cudaMalloc(&s_cand[r], (size_t)max_pairs[r] * 3 * pe * cand_elem));
-                VSHIP_CUDA_TRY(cudaMalloc(&s_part[r], (size_t)max_pairs[r] * 18 * geoms_h[r].tiles_total * 4));
+                VSHIP_CUDA_TRY(vship_malloc((void**)&s_cand[r], (size_t)max_pairs[r] * 3 * pe * cand_elem));
+                VSHIP_CUDA_TRY(vship_malloc((void**)&s_part[r], (size_t)max_pairs[r] * 18 * geoms_h[r].tiles_total * 4));
             }
             cap_pitems += ((size_t)max_src[r] + max_pairs[r]) * (size_t)ceil_div(rw[r], kPyrTile) * (size_t)ceil_div(rh[r], kPyrTile);
             cap_sitems += (size_t)max_pairs[r] * geoms_h[r].tiles_total;
         }
-        VSHIP_CUDA_TRY(cudaMalloc(&geoms_d, sizeof(Ssimu2Geom) * nres));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&geoms_d, sizeof(Ssimu2Geom) * nres));
         VSHIP_CUDA_TRY(cudaMemcpy(geoms_d, geoms_h, sizeof(Ssimu2Geom) * nres, cudaMemcpyHostToDevice));
-        VSHIP_CUDA_TRY(cudaMalloc(&s_scores, sizeof(double) * pair_cap));
-        VSHIP_CUDA_TRY(cudaMalloc(&s_imgs_d, sizeof(Ssimu2MultiImage) * (src_cap + pair_cap)));
-        VSHIP_CUDA_TRY(cudaMallocHost(&s_imgs_h, sizeof(Ssimu2MultiImage) * (src_cap + pair_cap)));
-        VSHIP_CUDA_TRY(cudaMalloc(&s_pairs_d, sizeof(Ssimu2MultiPair) * pair_cap));
-        VSHIP_CUDA_TRY(cudaMalloc(&s_pitems_d, sizeof(int4) * std::max<size_t>(cap_pitems, 1)));
-        VSHIP_CUDA_TRY(cudaMalloc(&s_sitems_d, sizeof(int2) * std::max<size_t>(cap_sitems, 1)));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&s_scores, sizeof(double) * pair_cap));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&s_imgs_d, sizeof(Ssimu2MultiImage) * (src_cap + pair_cap)));
+        if (vship_malloc_host((void**)&s_imgs_h, sizeof(Ssimu2MultiImage) * (src_cap + pair_cap)) != cudaSuccess)
+            return E_OUT_OF_RAM;
+        VSHIP_CUDA_TRY(vship_malloc((void**)&s_pairs_d, sizeof(Ssimu2MultiPair) * pair_cap));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&s_pitems_d, sizeof(int4) * std::max<size_t>(cap_pitems, 1)));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&s_sitems_d, sizeof(int2) * std::max<size_t>(cap_sitems, 1)));
     }
     if (flags & MULTI_BUTTERAUGLI) {
         for (int r = 0; r < nres; r++) {
@@ -145,11 +146,12 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
             if (rc) return rc;
         }
         // a chunk image per pair plus its source at worst
-        VSHIP_CUDA_TRY(cudaMalloc(&b_frames_d, sizeof(FrameDesc) * 2 * pair_cap));
-        VSHIP_CUDA_TRY(cudaMallocHost(&b_frames_h, sizeof(FrameDesc) * 2 * pair_cap));
-        VSHIP_CUDA_TRY(cudaMalloc(&b_pimg_d, sizeof(int2) * pair_cap));
-        VSHIP_CUDA_TRY(cudaMalloc(&b_norms_d, sizeof(double) * 3 * pair_cap * 2));
-        VSHIP_CUDA_TRY(cudaMalloc(&b_perm_d, sizeof(int) * pair_cap));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&b_frames_d, sizeof(FrameDesc) * 2 * pair_cap));
+        if (vship_malloc_host((void**)&b_frames_h, sizeof(FrameDesc) * 2 * pair_cap) != cudaSuccess)
+            return E_OUT_OF_RAM;
+        VSHIP_CUDA_TRY(vship_malloc((void**)&b_pimg_d, sizeof(int2) * pair_cap));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&b_norms_d, sizeof(double) * 3 * pair_cap * 2));
+        VSHIP_CUDA_TRY(vship_malloc((void**)&b_perm_d, sizeof(int) * pair_cap));
     }
     return E_OK;
 }

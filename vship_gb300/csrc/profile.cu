@@ -1,8 +1,12 @@
 // profile.cu -- per-kernel event timing registry (see profile.h).
 #include "profile.h"
+#include "common.cuh"
+
+#include <nvtx3/nvToolsExt.h>
 
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -33,6 +37,35 @@ cudaEvent_t get_event() {
 }  // namespace
 
 bool prof_enabled() { return g_on.load(std::memory_order_relaxed); }
+
+namespace {
+std::atomic<long> g_dev_allocs{0}, g_pinned_allocs{0};
+
+// true when this allocation must fail: the variable is set and n allocations already passed
+bool injected(const char* var, std::atomic<long>& count) {
+    const char* e = getenv(var);
+    if (!e) {
+        count.store(0);
+        return false;
+    }
+    return count.fetch_add(1) >= atol(e);
+}
+}  // namespace
+
+cudaError_t vship_malloc(void** p, size_t bytes) {
+    if (injected("VSHIP_FAIL_DEVICE_ALLOC_AFTER", g_dev_allocs)) return cudaErrorMemoryAllocation;
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t vship_malloc_host(void** p, size_t bytes) {
+    if (injected("VSHIP_FAIL_PINNED_ALLOC_AFTER", g_pinned_allocs)) return cudaErrorMemoryAllocation;
+    return cudaMallocHost(p, bytes);
+}
+
+bool vship_alloc_injected_failure() { return injected("VSHIP_FAIL_DEVICE_ALLOC_AFTER", g_dev_allocs); }
+
+void prof_range_push(const char* name) { nvtxRangePushA(name); }
+void prof_range_pop() { nvtxRangePop(); }
 
 int prof_begin(const char* name, cudaStream_t st) {
     if (!prof_enabled()) return -1;

@@ -54,7 +54,7 @@ int Server::create(int nres_, const int* widths, const int* heights, int intype_
     rc = ssimu2_multi_stats_blocks_per_sm(!(flags & SERVE_FP32_CANDIDATES), &bps);
     if (rc) return rc;
     stats_grid = std::max(1, bps) * sms;
-    VSHIP_CUDA_TRY(cudaMalloc(&sgeom_d, sizeof(Ssimu2Geom) * nres));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&sgeom_d, sizeof(Ssimu2Geom) * nres));
     VSHIP_CUDA_TRY(cudaMemcpy(sgeom_d, sgeom, sizeof(Ssimu2Geom) * nres, cudaMemcpyHostToDevice));
     VSHIP_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     cudaMemPoolProps props{};
@@ -71,6 +71,7 @@ int Server::create(int nres_, const int* widths, const int* heights, int intype_
 
 void* Server::dev_alloc(size_t bytes) {
     void* p = nullptr;
+    if (vship_alloc_injected_failure()) return nullptr;
     if (cudaMallocFromPoolAsync(&p, bytes, pool, st) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
@@ -110,6 +111,26 @@ int Server::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, in
             return E_BAD_POINTER;
     std::lock_guard<std::mutex> g(mu);
     for (int r = 0; r < nres; r++) yuv_r[r] = p[r];
+    return E_OK;
+}
+
+int Server::cancel(uint64_t id) {
+    ServeReq* r = nullptr;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        for (auto it = queue.begin(); it != queue.end(); ++it)
+            if ((*it)->id == id) {
+                r = *it;
+                queue.erase(it);
+                break;
+            }
+        if (!r) return E_BAD_POINTER;
+        done.push_back(ServeDone{r->id, kCancelled, now_s() - r->t_submit});
+        n_completed++;
+        n_cancelled++;
+    }
+    delete r;
+    cv.notify_all();
     return E_OK;
 }
 
@@ -188,6 +209,7 @@ void Server::completer() {
             if (status == E_OK) std::memcpy(r->out, res + b->out_off[i], n * sizeof(double));
             fin.push_back(ServeDone{r->id, status, t - r->t_submit});
         }
+        if (status != E_OK) n_failed += b->reqs.size();
         if (b->done) cudaEventDestroy(b->done);
         {
             std::lock_guard<std::mutex> g(mu);
@@ -347,7 +369,7 @@ int Server::launch(Batch* b) {
     }
     if (!b->host) {
         b->host_cap = std::max<size_t>(host_need, 1 << 20);
-        if (cudaMallocHost(&b->host, b->host_cap) != cudaSuccess) {
+        if (vship_malloc_host((void**)&b->host, b->host_cap) != cudaSuccess) {
             cudaGetLastError();
             b->host = nullptr;
             b->host_cap = 0;
@@ -491,7 +513,8 @@ std::string Server::stats_json() {
       << ", \"admission_budget_bytes\": " << adm.budget() << ", \"cache_hits\": " << cache.hits()
       << ", \"cache_misses\": " << cache.misses() << ", \"cache_evictions\": " << cache.evictions()
       << ", \"cache_entries\": " << cache.size() << ", \"cache_bytes\": " << cache.bytes()
-      << ", \"uncached_sources\": " << n_uncached_sources << ", \"queued\": " << queue.size()
+      << ", \"uncached_sources\": " << n_uncached_sources << ", \"cancelled\": " << n_cancelled
+      << ", \"failed\": " << n_failed << ", \"queued\": " << queue.size()
       << ", \"inflight\": " << inflight.size() << "}";
     return o.str();
 }

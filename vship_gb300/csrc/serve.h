@@ -55,6 +55,10 @@ public:
     int create(int nres, const int* widths, const int* heights, int intype, uint64_t admission_bytes,
                uint64_t cache_bytes, int max_batch_pairs, int flags, int qnorm, float intensity);
     int submit(ServeReq* r);  // takes ownership (deleted after completion)
+    // Withdraws a request that is still queued (not yet in a batch): it completes at once with
+    // status kCancelled. E_BAD_POINTER when no queued request has this id.
+    int cancel(uint64_t id);
+    static constexpr int kCancelled = -1;
     int poll(ServeDone* out, int max, double timeout_s);
     // Format of IN_YUV frames for every resolution (make_yuv_params; matrix 2 resolves per height).
     int set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, int loc, int transfer = 1,
@@ -100,7 +104,7 @@ private:
 
     // counters
     uint64_t n_submitted = 0, n_completed = 0, n_batches = 0, n_pairs = 0, n_admission_waits = 0;
-    uint64_t n_uncached_sources = 0;
+    uint64_t n_uncached_sources = 0, n_cancelled = 0, n_failed = 0;
     int max_batch_seen = 0;
 
     void scheduler();

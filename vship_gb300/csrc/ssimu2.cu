@@ -615,9 +615,9 @@ int Ssimu2Engine::init(int64_t width, int64_t height, int max_pairs_) {
     int rc = upload_constants_once();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStatsSmem));
-    VSHIP_CUDA_TRY(cudaMalloc(&pyr, sizeof(float) * (size_t)geom.plane_elems * 3 * 2 * max_pairs));
-    VSHIP_CUDA_TRY(cudaMalloc(&partials, sizeof(float) * (size_t)geom.tiles_total * 18 * max_pairs));
-    VSHIP_CUDA_TRY(cudaMalloc(&scores, sizeof(double) * max_pairs));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&pyr, sizeof(float) * (size_t)geom.plane_elems * 3 * 2 * max_pairs));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&partials, sizeof(float) * (size_t)geom.tiles_total * 18 * max_pairs));
+    VSHIP_CUDA_TRY(vship_malloc((void**)&scores, sizeof(double) * max_pairs));
     return E_OK;
 }
 
