@@ -131,22 +131,13 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
     const FrameDesc fd = frames[img];
     const BScaleDev F = g.s[0], Hs = g.s[1];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    float in[4][3];  // loads of the thread's 4 rows in flight together
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ty + 8 * r;
-        in[r][0] = in[r][1] = in[r][2] = 0.f;
-        if (gx < F.w && gy < F.h) load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, in[r][0], in[r][1], in[r][2]);
-    }
 #pragma unroll
     for (int r = 0; r < 4; r++) {
         const int ly = ty + 8 * r;
         const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ly;
         float v[3] = {0.f, 0.f, 0.f};
         if (gx < F.w && gy < F.h) {
-            v[0] = in[r][0];
-            v[1] = in[r][1];
-            v[2] = in[r][2];
+            load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, v[0], v[1], v[2]);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 if (!(IT == IN_YUV && yp.linear_out)) v[c] = to_linear_fast(v[c]);

@@ -127,24 +127,13 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     {
         const Ssimu2Level L = g.lv[0];
-        // all samples of the thread's 4 rows are loaded before any is used, so the loads are in
-        // flight together (the stores below could alias the input for the compiler)
-        float in[4][3];
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-            const int gx = bx * 32 + tx, gy = by * 32 + ty + 8 * r;
-            in[r][0] = in[r][1] = in[r][2] = 0.f;
-            if (gx < L.w && gy < L.h) load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, in[r][0], in[r][1], in[r][2]);
-        }
 #pragma unroll
         for (int r = 0; r < 4; r++) {
             const int ly = ty + 8 * r;
             const int gx = bx * 32 + tx, gy = by * 32 + ly;
             float v0 = 0.f, v1 = 0.f, v2 = 0.f;
             if (gx < L.w && gy < L.h) {
-                v0 = in[r][0];
-                v1 = in[r][1];
-                v2 = in[r][2];
+                load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, v0, v1, v2);
                 if (!(IT == IN_YUV && yp.linear_out)) {  // frames converted to linear light skip x^2.4
                     v0 = to_linear_fast(v0);
                     v1 = to_linear_fast(v1);
