@@ -224,59 +224,6 @@ __device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const f
     }
 }
 
-// The same blur for two planes at once: their samples travel as float pairs through the f32x2
-// FMA (each lane one IEEE fma, in the same order, so the values are bitwise tile_blur_r8's),
-// halving the FMA issue slots. hb2 holds 2 * TB_HPL floats (float-pair plane, pitch TB_HP
-// pairs). The horizontal lane map is row 8 * warp + (lane & 7), outputs 8 * (lane >> 3) .. + 7,
-// which keeps the float4 raw reads and the float-pair stores bank-conflict free.
-template <int KI>
-__device__ __forceinline__ void tile_blur_r8_x2(const float* in0, const float* in1, float* hb2, const float rxy[6],
-                                                float out0[6], float out1[6]) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    f2_t k2[17];
-#pragma unroll
-    for (int i = 0; i < 17; i++) k2[i] = f2_pack(c_bk[KI][i], c_bk[KI][i]);
-    {
-        const int hr = 8 * warp + (lane & 7), hg = lane >> 3;
-        const float* r0 = in0 + hr * TB_IP + 8 * hg;
-        const float* r1 = in1 + hr * TB_IP + 8 * hg;
-        f2_t v[24];
-#pragma unroll
-        for (int j4 = 0; j4 < 6; j4++) {
-            const float4 a = *reinterpret_cast<const float4*>(r0 + 4 * j4);
-            const float4 b = *reinterpret_cast<const float4*>(r1 + 4 * j4);
-            v[4 * j4] = f2_pack(a.x, b.x);
-            v[4 * j4 + 1] = f2_pack(a.y, b.y);
-            v[4 * j4 + 2] = f2_pack(a.z, b.z);
-            v[4 * j4 + 3] = f2_pack(a.w, b.w);
-        }
-        f2_t* dst = reinterpret_cast<f2_t*>(hb2) + hr * TB_HP + 8 * hg;
-#pragma unroll
-        for (int o = 0; o < 8; o++) {
-            f2_t a = f2_pack(0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], k2[i], a);
-            dst[o] = a;
-        }
-    }
-    __syncthreads();
-    {
-        const int vc = tid & 31, vg = tid >> 5;
-        const f2_t* col = reinterpret_cast<const f2_t*>(hb2) + (6 * vg) * TB_HP + vc;
-        f2_t v[22];
-#pragma unroll
-        for (int j = 0; j < 22; j++) v[j] = col[j * TB_HP];
-#pragma unroll
-        for (int o = 0; o < 6; o++) {
-            f2_t a = f2_pack(0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], k2[i], a);
-            a = f2_mul(a, f2_pack(rxy[o], rxy[o]));
-            f2_unpack(a, out0[o], out1[o]);
-        }
-    }
-}
-
 template <int KI>
 __device__ __forceinline__ void tile_masses_r8(int x0, int y0, int w, int h, float rxy[6]) {
     const int tid = threadIdx.x;
@@ -313,7 +260,7 @@ __device__ __forceinline__ float b_gamma(float v) {
 __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* const* __restrict__ ib, BGeom g, int s,
                                                               float intensity) {
     extern __shared__ __align__(16) float sm[];
-    float* hb = sm + 3 * TB_RAW;  // float-pair plane (its first half serves the single blur)
+    float* hb = sm + 2 * TB_RAW;
     const int img = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
@@ -321,22 +268,25 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* const* __re
     tile_masses_r8<0>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float src[3][6], blr[3][6];
-    // R and G are blurred together as float pairs while B streams in
     tile_stage_r8(sm, iplane(ib, g, S, img, I_LIN), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, img, I_LIN + 1), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
-    tile_stage_r8(sm + 2 * TB_RAW, iplane(ib, g, S, img, I_LIN + 2), S.p, S.w, S.h, x0, y0);
-    cp_async_commit();
-    cp_async_wait<1>();
-    __syncthreads();
-    tile_blur_r8_x2<0>(sm, sm + TB_RAW, hb, rxy, blr[0], blr[1]);
-    cp_async_wait<0>();
-    __syncthreads();
-    tile_blur_r8<0>(sm + 2 * TB_RAW, hb, rxy, blr[2]);
 #pragma unroll
-    for (int c = 0; c < 3; c++)
+    for (int c = 0; c < 3; c++) {
+        float* in = sm + (c & 1) * TB_RAW;
+        if (c < 2) {
+            tile_stage_r8(sm + ((c + 1) & 1) * TB_RAW, iplane(ib, g, S, img, I_LIN + c + 1), S.p, S.w, S.h, x0,
+                          y0);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        tile_blur_r8<0>(in, hb, rxy, blr[c]);
 #pragma unroll
-        for (int o = 0; o < 6; o++) src[c][o] = sm[c * TB_RAW + (6 * vg + o + TB_R) * TB_IP + vc + TB_R];
+        for (int o = 0; o < 6; o++) src[c][o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
+        __syncthreads();
+    }
     float* ox = iplane(ib, g, S, img, I_XYB + 0);
     float* oy = iplane(ib, g, S, img, I_XYB + 1);
     float* oz = iplane(ib, g, S, img, I_XYB + 2);
@@ -561,7 +511,7 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restri
 // HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), nimages)
 __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
-    float* hb = sm + 2 * TB_RAW;  // float-pair plane
+    float* hb = sm + 2 * TB_RAW;
     const int img = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
@@ -573,15 +523,14 @@ __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restr
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
-    float blr2[2][6];
-    tile_blur_r8_x2<1>(sm, sm + TB_RAW, hb, rxy, blr2[0], blr2[1]);
 #pragma unroll
     for (int c = 0; c < 2; c++) {
         const float* in = sm + c * TB_RAW;
-        const float* blr = blr2[c];
-        float pre[6];
+        float blr[6], pre[6];
+        tile_blur_r8<1>(in, hb, rxy, blr);
 #pragma unroll
         for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
+        __syncthreads();
         float* hfp = iplane(ib, g, S, img, I_HF + c);
         float* uhfp = iplane(ib, g, S, img, I_UHF + c);
 #pragma unroll
@@ -846,7 +795,7 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
 __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* const* __restrict__ ib,
                                                                   const int2* __restrict__ pimg, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
-    float* hb = sm + 2 * TB_RAW;  // float-pair plane
+    float* hb = sm + 2 * TB_RAW;
     const int i1 = pimg[blockIdx.z].y;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
@@ -858,7 +807,11 @@ __global__ void __launch_bounds__(256, 3) butter_mask_blur_kernel(float* const* 
     cp_async_wait<0>();
     __syncthreads();
     float b[2][6];
-    tile_blur_r8_x2<2>(sm, sm + TB_RAW, hb, rxy, b[0], b[1]);
+#pragma unroll
+    for (int m = 0; m < 2; m++) {
+        tile_blur_r8<2>(sm + m * TB_RAW, hb, rxy, b[m]);
+        __syncthreads();
+    }
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float* b0 = iplane(ib, g, S, i1, Q_B0);
     float* sac = iplane(ib, g, S, i1, Q_SAC);
@@ -1115,8 +1068,6 @@ static DiffParams make_diff_params() {
 }
 
 constexpr int kTileSmem = (2 * TB_RAW + TB_HPL) * 4;
-constexpr int kTileSmem2 = (2 * TB_RAW + 2 * TB_HPL) * 4;  // two raw tiles and a float-pair plane
-constexpr int kOpsinSmem = (3 * TB_RAW + 2 * TB_HPL) * 4;  // three raw tiles and a float-pair plane
 
 __global__ void butter_identity_pairs_kernel(int2* pimg, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1127,7 +1078,6 @@ int butter_prepare_device() {
     int rc = upload_butter_tables();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_opsin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kOpsinSmem));
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
     const DiffParams P = make_diff_params();
@@ -1239,17 +1189,17 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
             const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), ni);
             const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 3 * ni);
             const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), ni);
-            { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kOpsinSmem, st>>>(ib, g, s, intensity); }
+            { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s, intensity); }
             { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
             { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(ib, g, s); }
             { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
             { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(ib, g, s); }
-            { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem2, st>>>(ib, g, s); }
+            { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s); }
         }
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
         { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s); }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
-        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem2, st>>>(ib, pimg, g, s); }
+        { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(ib, pimg, g, s); }
         const dim3 gf((unsigned)ceil_div(sw, DM_TW), (unsigned)ceil_div(sh, DM_TH), np);
         if (s == 1)
             { ProfScope ps_("butter_diffmap", st); butter_diffmap_kernel<false><<<gf, 256, 0, st>>>(ib, pimg, g, s, nullptr, partials, (float)qnorm); }
