@@ -319,17 +319,19 @@ __global__ void __launch_bounds__(256, 3) butter_opsin_kernel(float* const* __re
 }
 
 // ------------------------------------------------------------------------------------------
-// Separable horizontal pass, radius R (21 or 9): 128x16 tile per CTA; each thread makes 8
-// consecutive outputs. The input rows start at x0 - RA (RA = R rounded up to a multiple of 4, so
-// the cp.async chunks are 16-byte aligned) and are read back as float4 (pitch 180 = 45 quads:
-// conflict-free); the thread's window starts RA - R floats into its first quad.
-// grid (ceil(w/128), ceil(h/16), 3*nimages): z -> image = z/3, plane = src_id + z%3.
-constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180;
+// Separable horizontal pass, radius R (21 or 9): 128x16 row tiles; each thread makes 8
+// consecutive outputs of a tile. The input rows start at x0 - RA (RA = R rounded up to a multiple
+// of 4, so the cp.async chunks are 16-byte aligned) and are read back as float4 (pitch 180 = 45
+// quads: conflict-free); the thread's window starts RA - R floats into its first quad. A CTA
+// walks HB_NT row tiles down the column, staging tile t + 1 while it computes tile t, so the
+// global-load latency hides behind the taps of the previous tile.
+// grid (ceil(w/128), ceil(h/(16*HB_NT)), 3*nimages): z -> image = z/3, plane = src_id + z%3.
+constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180, HB_NT = 4;
 
 template <int KI, int R>
-__global__ void __launch_bounds__(256) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s, int src_id,
-                                                           int dst_id) {
-    __shared__ __align__(16) float in[HB_TH * HB_P];
+__global__ void __launch_bounds__(256, 3) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s,
+                                                              int src_id, int dst_id) {
+    __shared__ __align__(16) float in[2][HB_TH * HB_P];
     constexpr int RA = (R + 3) & ~3;
     constexpr int IW = HB_TW + 2 * RA;
     constexpr int OFF = RA - R;
@@ -339,38 +341,53 @@ __global__ void __launch_bounds__(256) butter_hblur_kernel(float* const* __restr
     const BScaleDev S = pick_scale(g, s);
     const float* src = iplane(ib, g, S, img, src_id + pl);
     float* dst = iplane(ib, g, S, img, dst_id + pl);
-    const int x0 = blockIdx.x * HB_TW, y0 = blockIdx.y * HB_TH;
-    stage_rows<256>(in, HB_P, src, S.p, S.w, S.h, x0 - RA, y0, HB_TH, IW / 4);
-    cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
+    const int x0 = blockIdx.x * HB_TW;
+    const int yt0 = blockIdx.y * (HB_TH * HB_NT);
+    const int nt = min(HB_NT, (S.h - yt0 + HB_TH - 1) / HB_TH);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = (warp >> 2) * 8 + (lane >> 2);
     const int col0 = (warp & 3) * 32 + 8 * (lane & 3);
-    const int gy = y0 + row;
-    if (gy >= S.h) return;
-    float v[4 * NV4];
-#pragma unroll
-    for (int j4 = 0; j4 < NV4; j4++) {
-        const float4 q = *reinterpret_cast<const float4*>(in + row * HB_P + col0 + 4 * j4);
-        v[4 * j4] = q.x;
-        v[4 * j4 + 1] = q.y;
-        v[4 * j4 + 2] = q.z;
-        v[4 * j4 + 3] = q.w;
-    }
-    float out[8], rx[8];
+    float rx[8];
     b_inv_mass_run<KI, R, 8>(x0 + col0, S.w, rx);
+    stage_rows<256>(in[0], HB_P, src, S.p, S.w, S.h, x0 - RA, yt0, HB_TH, IW / 4);
+    cp_async_commit();
+#pragma unroll 1
+    for (int t = 0; t < nt; t++) {
+        if (t + 1 < nt) {
+            stage_rows<256>(in[(t + 1) & 1], HB_P, src, S.p, S.w, S.h, x0 - RA, yt0 + (t + 1) * HB_TH, HB_TH, IW / 4);
+            cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();
+        const int gy = yt0 + t * HB_TH + row;
+        if (gy < S.h) {
+            const float* tin = in[t & 1];
+            float v[4 * NV4];
 #pragma unroll
-    for (int o = 0; o < 8; o++) {
-        float a = 0.f;
+            for (int j4 = 0; j4 < NV4; j4++) {
+                const float4 q = *reinterpret_cast<const float4*>(tin + row * HB_P + col0 + 4 * j4);
+                v[4 * j4] = q.x;
+                v[4 * j4 + 1] = q.y;
+                v[4 * j4 + 2] = q.z;
+                v[4 * j4 + 3] = q.w;
+            }
+            float out[8];
 #pragma unroll
-        for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[OFF + o + i], c_bk[KI][i], a);
-        out[o] = a * rx[o];
-    }
-    float* d = dst + (int64_t)gy * S.p + x0 + col0;
-    if (x0 + col0 + 8 <= S.p) {  // rows are padded to a multiple of 8 floats
-        *reinterpret_cast<float4*>(d) = make_float4(out[0], out[1], out[2], out[3]);
-        *reinterpret_cast<float4*>(d + 4) = make_float4(out[4], out[5], out[6], out[7]);
+            for (int o = 0; o < 8; o++) {
+                float a = 0.f;
+#pragma unroll
+                for (int i = 0; i < 2 * R + 1; i++) a = fmaf(v[OFF + o + i], c_bk[KI][i], a);
+                out[o] = a * rx[o];
+            }
+            float* d = dst + (int64_t)gy * S.p + x0 + col0;
+            if (x0 + col0 + 8 <= S.p) {  // rows are padded to a multiple of 8 floats
+                *reinterpret_cast<float4*>(d) = make_float4(out[0], out[1], out[2], out[3]);
+                *reinterpret_cast<float4*>(d + 4) = make_float4(out[4], out[5], out[6], out[7]);
+            }
+        }
+        __syncthreads();  // every thread is done with in[t & 1] before tile t + 2 is staged into it
     }
 }
 
@@ -1187,7 +1204,7 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
         const int64_t sw = g.s[s].w, sh = g.s[s].h;
         if (ni) {
             const dim3 gt((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), ni);
-            const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH), 3 * ni);
+            const dim3 gh((unsigned)ceil_div(sw, HB_TW), (unsigned)ceil_div(sh, HB_TH * HB_NT), 3 * ni);
             const dim3 gv((unsigned)ceil_div(sw, VB_TW), (unsigned)ceil_div(sh, VB_TH), ni);
             { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s, intensity); }
             { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
