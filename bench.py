@@ -239,8 +239,9 @@ def yuv_table(v, yuv, start, count):
     return v.device_frames_table(frames)
 
 
-def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None):
-    """Batched device-resident throughput; returns (seconds for `steps` steps, profile dict, launches)."""
+def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands=False):
+    """Batched device-resident throughput; returns (seconds for `steps` steps, profile dict, launches,
+    results). half_bands: Butteraugli with its MF, HF and UHF bands stored as FP16."""
     import torch
     if yuv is not None:
         yuvt, (w, h) = yuv
@@ -251,7 +252,7 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None):
         eng = v.SSIMU2Batch(w, h, chunk)
         out = torch.zeros(npairs, dtype=torch.float64, device="cuda")
     else:
-        eng = v.ButteraugliBatch(w, h, chunk, 2, 203.0)
+        eng = v.ButteraugliBatch(w, h, chunk, 2, 203.0, half_bands=half_bands)
         out = torch.zeros(npairs * 3, dtype=torch.float64, device="cuda")
     tables = []
     for s in range(0, npairs, chunk):
@@ -291,7 +292,7 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None):
     return sec, prof, launches, result
 
 
-def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
+def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None, half_bands=False):
     """Through the C ABI from pinned host memory, one handler per thread: the reference-facing
     float-RGB calls, or (yuv=...) the 4:2:0 extension calls."""
     import ctypes
@@ -327,7 +328,8 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
         if kind == "ssimu2":
             rc = L.Vship_SSIMU2Init(ctypes.byref(hd), w, h)
         else:
-            rc = L.Vship_ButteraugliInitv2(ctypes.byref(hd), w, h, 2, ctypes.c_float(203.0))
+            rc = L.Vship_ButteraugliInitEx(ctypes.byref(hd), w, h, 2, ctypes.c_float(203.0),
+                                           v.BUTTER_HALF_BANDS if half_bands else 0)
         if rc:
             raise v.VshipError(rc, "init")
         handlers.append(hd)
@@ -392,21 +394,34 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None):
     return sec, h2d, d2h, np.array(scores)
 
 
-def cpu_baseline(kind, ref, dst, sample_pairs, nthreads):
-    """The reference's math (FP32 restatement in oracle/) on the host cores for a bounded sample."""
+def cpu_baseline(kind, ref, dst, sample_pairs, nthreads, fp64_pairs=0):
+    """The reference's math (FP32 restatement in oracle/) on the host cores for a bounded sample.
+    With fp64_pairs > 0 the FP64 instantiation also scores the first pairs (untimed), the
+    reference against which the GPU results' error is stated."""
     import numpy as np
     import oracle
     t_total = 0.0
-    for t in range(sample_pairs):
+    exact = []
+    for t in range(max(sample_pairs, fp64_pairs)):
         a = [np.ascontiguousarray(ref[t, c].cpu().numpy()) for c in range(3)]
         b = [np.ascontiguousarray(dst[t, c].cpu().numpy()) for c in range(3)]
-        t0 = time.perf_counter()
-        if kind == "ssimu2":
-            oracle.ssimu2(a, b, precision=32, nthreads=nthreads)
-        else:
-            oracle.butteraugli(a, b, precision=32, nthreads=nthreads)
-        t_total += time.perf_counter() - t0
-    return sample_pairs / t_total, t_total
+        if t < sample_pairs:
+            t0 = time.perf_counter()
+            if kind == "ssimu2":
+                oracle.ssimu2(a, b, precision=32, nthreads=nthreads)
+            else:
+                oracle.butteraugli(a, b, precision=32, nthreads=nthreads)
+            t_total += time.perf_counter() - t0
+        if t < fp64_pairs:
+            if kind == "ssimu2":
+                exact.append(oracle.ssimu2(a, b, precision=64, nthreads=nthreads))
+            else:
+                exact.append(oracle.butteraugli(a, b, precision=64, nthreads=nthreads))
+    return sample_pairs / t_total, t_total, exact
+
+
+def rel_err(got, want):
+    return [abs(g - w) / max(abs(w), 1e-12) for g, w in zip(got, want)]
 
 
 def to_rgb48(x):
@@ -428,16 +443,30 @@ def bench_workload(v, kind, args, ws, rank):
     torch.cuda.synchronize()
     w, h = size
     # float32 R'G'B' planes
-    fsec, _, _, _ = run_device(v, kind, ref, dst, args.steps, args.warmup, ws, chunk)
+    fsec, _, _, fres = run_device(v, kind, ref, dst, args.steps, args.warmup, ws, chunk)
     fsec = max_over_ranks(fsec, ws)
+    hres = None
+    if kind != "ssimu2" and not args.skip_half_bands:
+        # the FP16-band storage form on the same float planes: its error against FP64 below
+        _, _, _, hres = run_device(v, kind, ref, dst, 1, 1, ws, chunk, half_bands=True)
     fe2e_sec, fh2d, d2h, _ = run_e2e(v, kind, ref, dst, args.e2e_steps, 1, args.e2e_threads)
     fe2e_sec = max_over_ranks(fe2e_sec, ws)
     cpu_res = None
     if rank == 0 and args.cpu_sample > 0:
         ns = args.cpu_sample if kind == "ssimu2" else max(1, args.cpu_sample // 4)
-        cv, csec = cpu_baseline(kind, ref, dst, ns, os.cpu_count() or 1)
+        nx = args.error_pairs if kind != "ssimu2" else 0
+        cv, csec, exact = cpu_baseline(kind, ref, dst, ns, os.cpu_count() or 1, fp64_pairs=nx)
         cpu_res = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
                    "sample": f"{ns} pairs of the same workload ({csec:.1f} s)"}
+        if exact:
+            # max over the checked pairs of the relative error of {Qnorm, 3-norm, inf-norm}
+            def worst(res):
+                r = res.numpy().reshape(-1, 3)
+                return [max(e) for e in zip(*[rel_err(r[t], exact[t]) for t in range(len(exact))])]
+            cpu_res["error_vs_fp64"] = {"pairs": len(exact), "input": "float32 R'G'B'",
+                                        "fp32_planes": worst(fres)}
+            if hres is not None:
+                cpu_res["error_vs_fp64"]["fp16_bands"] = worst(hres)
     # 16-bit R'G'B' (headline)
     ref16, dst16 = to_rgb48(ref), to_rgb48(dst)
     del ref, dst
@@ -473,6 +502,21 @@ def bench_workload(v, kind, args, ws, rank):
         fp32_roof = {"kernel": kname, "achieved": tf, "peak": pk, "unit": "TFLOP/s", "frac": tf / pk,
                      "flops_per_pair": ssimu2_stats_flops(w, h),
                      "peak_source": f"128 FP32 FMA lanes x SMs x {mhz:.0f} MHz (sampled clock)"}
+    half = None
+    if kind != "ssimu2" and not args.skip_half_bands:
+        hsec, hprof, _, _ = run_device(v, kind, ref16, dst16, args.steps, args.warmup, ws, chunk, half_bands=True)
+        hsec = max_over_ranks(hsec, ws)
+        he2e_sec, _, _, _ = run_e2e(v, kind, ref16, dst16, args.e2e_steps, 1, args.e2e_threads, half_bands=True)
+        he2e_sec = max_over_ranks(he2e_sec, ws)
+        L = v.lib()
+        half = {"value": npairs * ws * args.steps / hsec,
+                "e2e": {"value": npairs * ws * args.e2e_steps / he2e_sec, "unit": "frame-pairs/s",
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "call": "Vship_ComputeButteraugliUint16v3 (Vship_ButteraugliInitEx, Vship_ButterHalfBands)"},
+                "device_bytes_per_pair": int(L.Vship_ButteraugliDeviceBytesEx(w, h, 1, v.BUTTER_HALF_BANDS)),
+                "device_bytes_per_pair_fp32": int(L.Vship_ButteraugliDeviceBytes(w, h, 1)),
+                "kernel_ms": {k: round(t, 3) for k, (n, t) in sorted(hprof.items(), key=lambda x: -x[1][1])},
+                "note": "MF, HF and UHF bands stored as FP16, all arithmetic FP32; error in cpu_baseline"}
     del ref16, dst16
     torch.cuda.empty_cache()
     # 10-bit 4:2:0 planes converted on the GPU (a quarter of the bytes of float RGB)
@@ -506,6 +550,8 @@ def bench_workload(v, kind, args, ws, rank):
         "score_check": {"device_vs_e2e_max_abs": float(abs(
             (dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy()[0::3]) - host_scores).max())},
     }
+    if half:
+        res["fp16_bands"] = half
     if cpu_res:
         res["cpu_baseline"] = cpu_res
     torch.cuda.empty_cache()
@@ -924,7 +970,7 @@ def main_ours(args):
         out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e", "yuv420p10",
                                                    "float32_rgb", "input",
                                                    "roofline", "gpu_launches", "clocks", "kernel_share",
-                                                   "pipeline_bytes_per_pair", "score_check")
+                                                   "pipeline_bytes_per_pair", "score_check", "fp16_bands")
                                  if k in b}
         if "cpu_baseline" in b:
             out["butteraugli_4k"]["cpu_baseline"] = b["cpu_baseline"]
@@ -1000,6 +1046,9 @@ def main():
     ap.add_argument("--skip-ssimu2", action="store_true")
     ap.add_argument("--skip-multi", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
+    ap.add_argument("--skip-half-bands", action="store_true", help="skip the FP16-band Butteraugli run")
+    ap.add_argument("--error-pairs", type=int, default=1,
+                    help="Butteraugli pairs scored by the FP64 oracle for the error of each storage form")
     ap.add_argument("--serve-size", default=f"{W4K}x{H4K}")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-max-requests", type=int, default=400)

@@ -274,6 +274,27 @@ EXPORTPREPROCESS Vship_Exception Vship_ButteraugliComputeDeviceAsync(Vship_Butte
                                                                      float* distmaps_dev, void* stream);
 EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytes(int width, int height, int max_pairs);
 
+/* Butteraugli with FP16 band storage -- no counterpart in the reference, whose planes are all
+ * FP32 (src/butter/main.hpp:141-195 allocates them per call).
+ *
+ * With Vship_ButterHalfBands the MF, HF and UHF frequency bands of every image, which only the
+ * pair stage reads, are stored as FP16; every other plane and all arithmetic stay FP32. An image
+ * then takes 12.5 instead of 16 FP32-plane equivalents per scale (a 3840x2160 pair: 1.07 instead
+ * of 1.36 GB of device memory) at the same throughput, for an accuracy cost: the norms move by
+ * the FP16 rounding of the bands. Against the FP64 oracle: about 2e-6 relative for the 2- and
+ * 3-norm on blurred and noisy pairs (1e-7 with FP32 planes), up to 5e-5 on light block-DCT
+ * distortions, and up to 3e-4 for the inf-norm, which follows one pixel.
+ * Vship_ButteraugliInitEx is Vship_ButteraugliInitv2 with flags (host-buffer Compute calls);
+ * Vship_ButteraugliBatchInitEx is Vship_ButteraugliBatchInit with flags; flags = 0 gives the
+ * FP32 planes of the plain functions. Other flag bits are refused (Vship_BadPointer). */
+typedef enum { Vship_ButterHalfBands = 1 } Vship_ButterFlags;
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliInitEx(Vship_ButteraugliHandler* handler, int width, int height,
+                                                         int Qnorm, float intensity_multiplier, int flags);
+EXPORTPREPROCESS Vship_Exception Vship_ButteraugliBatchInitEx(Vship_ButteraugliHandler* handler, int width,
+                                                              int height, int Qnorm, float intensity_multiplier,
+                                                              int max_pairs, int flags);
+EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytesEx(int width, int height, int max_pairs, int flags);
+
 /* SSIMU2 for callers that cannot allocate GPU memory -- no counterpart in the reference.
  *
  * Programs that fix their GPU memory budget at start-up (real-time encoders, servers with a
@@ -326,6 +347,7 @@ typedef enum {
     Vship_MultiFp16 = 4,
     Vship_MultiNoGraph = 8,
     Vship_MultiAutotune = 16,
+    Vship_MultiButterHalfBands = 32, /* Butteraugli MF, HF and UHF bands as FP16 (Vship_ButterHalfBands) */
 } Vship_MultiFlags;
 EXPORTPREPROCESS Vship_Exception Vship_MultiInit(Vship_MultiHandler* handler, int nres, const int* widths,
                                                  const int* heights, const int* max_sources, const int* max_pairs,
@@ -367,6 +389,7 @@ typedef struct {
 } Vship_ServeHandler;
 typedef enum { Vship_ServeSSIMU2 = 0, Vship_ServeButteraugli = 1 } Vship_ServeMetric;
 #define Vship_ServeFp32Candidates 1
+#define Vship_ServeButterHalfBands 2 /* Butteraugli MF, HF and UHF bands as FP16 (Vship_ButterHalfBands) */
 typedef struct {
     uint64_t request_id;
     int metric;      /* Vship_ServeMetric */

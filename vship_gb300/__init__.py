@@ -28,6 +28,7 @@ EXCEPTION_NAMES = ["NoError", "OutOfVRAM", "OutOfRAM", "DifferingInputType", "No
 # Vship_InputType
 IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT, IN_YUV = 0, 1, 2, 3, 4
 IN_YUV420P10 = IN_YUV  # the default Y'CbCr format (10-bit 4:2:0, BT.709, limited, left siting)
+BUTTER_HALF_BANDS = 1  # Vship_ButterHalfBands: Butteraugli MF, HF and UHF bands stored as FP16
 
 
 class VshipError(RuntimeError):
@@ -140,6 +141,11 @@ SIGNATURES = {
     "Vship_ButteraugliComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                                  ctypes.c_void_p, ctypes.c_void_p]),
     "Vship_ButteraugliDeviceBytes": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_ButteraugliInitEx": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                     ctypes.c_int]),
+    "Vship_ButteraugliBatchInitEx": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_float, ctypes.c_int, ctypes.c_int]),
+    "Vship_ButteraugliDeviceBytesEx": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "Vship_ComputeSSIMU2DeviceNoAlloc": (_E, [ctypes.POINTER(DeviceFrame), ctypes.POINTER(DeviceFrame), ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
     "Vship_MultiInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, _IP, _IP, _IP, _IP, ctypes.c_int, ctypes.c_int,
@@ -342,14 +348,21 @@ class SSIMU2Handler:
 
 
 class ButteraugliHandler:
-    """One Butteraugli scorer (Vship_ButteraugliInitv2 / Compute*v3 / Free)."""
+    """One Butteraugli scorer (Vship_ButteraugliInitv2 / Compute*v3 / Free); half_bands=True stores
+    the MF, HF and UHF bands as FP16 (Vship_ButteraugliInitEx with Vship_ButterHalfBands)."""
 
-    def __init__(self, width: int, height: int, qnorm: int = 2, intensity_multiplier: float = 203.0):
+    def __init__(self, width: int, height: int, qnorm: int = 2, intensity_multiplier: float = 203.0,
+                 half_bands: bool = False):
         self.width, self.height = int(width), int(height)
         self.qnorm, self.intensity = int(qnorm), float(intensity_multiplier)
         h = Handler()
-        _check(lib().Vship_ButteraugliInitv2(ctypes.byref(h), self.width, self.height, self.qnorm,
-                                             ctypes.c_float(self.intensity)), "Vship_ButteraugliInitv2")
+        if half_bands:
+            _check(lib().Vship_ButteraugliInitEx(ctypes.byref(h), self.width, self.height, self.qnorm,
+                                                 ctypes.c_float(self.intensity), BUTTER_HALF_BANDS),
+                   "Vship_ButteraugliInitEx")
+        else:
+            _check(lib().Vship_ButteraugliInitv2(ctypes.byref(h), self.width, self.height, self.qnorm,
+                                                 ctypes.c_float(self.intensity)), "Vship_ButteraugliInitv2")
         self._h = h  # only a created handler is ever freed
 
     def compute(self, reference, distorted, distmap: bool = False):
@@ -447,12 +460,14 @@ class SSIMU2Batch:
 class ButteraugliBatch:
     """Batched device-resident Butteraugli (Vship_ButteraugliBatchInit / ComputeDeviceAsync)."""
 
-    def __init__(self, width: int, height: int, max_pairs: int, qnorm: int = 2, intensity_multiplier: float = 203.0):
+    def __init__(self, width: int, height: int, max_pairs: int, qnorm: int = 2, intensity_multiplier: float = 203.0,
+                 half_bands: bool = False):
         self.width, self.height, self.max_pairs = int(width), int(height), int(max_pairs)
         h = Handler()
-        _check(lib().Vship_ButteraugliBatchInit(ctypes.byref(h), self.width, self.height, int(qnorm),
-                                                ctypes.c_float(intensity_multiplier), self.max_pairs),
-               "Vship_ButteraugliBatchInit")
+        _check(lib().Vship_ButteraugliBatchInitEx(ctypes.byref(h), self.width, self.height, int(qnorm),
+                                                  ctypes.c_float(intensity_multiplier), self.max_pairs,
+                                                  BUTTER_HALF_BANDS if half_bands else 0),
+               "Vship_ButteraugliBatchInitEx")
         self._h = h  # only a created handler is ever freed
 
     def set_yuv_format(self, fmt: YuvFormat) -> None:
@@ -479,6 +494,7 @@ class ButteraugliBatch:
 
 
 MULTI_SSIMU2, MULTI_BUTTERAUGLI, MULTI_FP16, MULTI_NO_GRAPH, MULTI_AUTOTUNE = 1, 2, 4, 8, 16
+MULTI_BUTTER_HALF = 32  # Vship_MultiButterHalfBands
 
 
 def _ints(v):
@@ -555,6 +571,7 @@ class MultiScorer:
 SERVE_SSIMU2, SERVE_BUTTERAUGLI = 0, 1
 SERVE_CANCELLED = -1
 SERVE_FP32_CANDIDATES = 1
+SERVE_BUTTER_HALF_BANDS = 2  # Vship_ServeButterHalfBands
 
 
 class Server:

@@ -555,15 +555,17 @@ uint64_t Vship_SSIMU2DeviceBytes(int width, int height, int max_pairs) {
 // ----- Butteraugli ------------------------------------------------------------------------
 
 static Vship_Exception butter_init(Vship_ButteraugliHandler* handler, int width, int height, int Qnorm,
-                                   float intensity_multiplier, int max_pairs, bool host_io) {
+                                   float intensity_multiplier, int max_pairs, bool host_io, int flags = 0) {
     if (!handler) return Vship_BadPointer;
     if (width <= 0 || height <= 0 || max_pairs <= 0) return Vship_BadPointer;
+    if (flags & ~(int)Vship_ButterHalfBands) return Vship_BadPointer;
     int c = 0;
     int rc = check_gpu_count(&c);
     if (rc) return to_exc(rc);
     std::unique_ptr<ButterHandle> h(new ButterHandle());
     h->host_io = host_io;
     if (cudaGetDevice(&h->io.device) != cudaSuccess) return Vship_BadDeviceCode;
+    h->eng.half_bands = (flags & Vship_ButterHalfBands) != 0;
     rc = h->eng.init(width, height, Qnorm, intensity_multiplier, max_pairs);
     if (!rc && host_io) rc = h->io.init(width, height, 3 * sizeof(double));
     if (rc) return to_exc(rc);
@@ -603,6 +605,20 @@ Vship_Exception Vship_ButteraugliComputeDeviceAsync(Vship_ButteraugliHandler han
 
 uint64_t Vship_ButteraugliDeviceBytes(int width, int height, int max_pairs) {
     return (uint64_t)ButterEngine::device_bytes(width, height, max_pairs);
+}
+
+Vship_Exception Vship_ButteraugliInitEx(Vship_ButteraugliHandler* handler, int width, int height, int Qnorm,
+                                        float intensity_multiplier, int flags) {
+    return butter_init(handler, width, height, Qnorm, intensity_multiplier, 1, true, flags);
+}
+
+Vship_Exception Vship_ButteraugliBatchInitEx(Vship_ButteraugliHandler* handler, int width, int height, int Qnorm,
+                                             float intensity_multiplier, int max_pairs, int flags) {
+    return butter_init(handler, width, height, Qnorm, intensity_multiplier, max_pairs, false, flags);
+}
+
+uint64_t Vship_ButteraugliDeviceBytesEx(int width, int height, int max_pairs, int flags) {
+    return (uint64_t)ButterEngine::device_bytes(width, height, max_pairs, (flags & Vship_ButterHalfBands) != 0);
 }
 
 Vship_Exception Vship_ButteraugliInit(Vship_ButteraugliHandler* handler, int width, int height,

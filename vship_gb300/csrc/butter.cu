@@ -109,12 +109,34 @@ struct BScaleDev {
 struct BGeom {
     BScaleDev s[2];  // 0 = full, 1 = half
     int64_t img_floats;
+    int half_bands;  // MF, HF and UHF stored as FP16 (hplane); the other planes stay FP32
     int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x32) at full scale
 };
 
 // ib[img] = that image's workspace (both scales); the launch's image list indexes it
 __device__ __forceinline__ float* iplane(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id) {
     return ib[img] + S.base + (int64_t)id * S.n;
+}
+// Half-band storage: the MF, HF and UHF bands, which only the pair stage reads, are kept as FP16
+// in a block after the nine FP32 planes (linear RGB / horizontal-pass scratch, XYB / D / HF_pre,
+// LF vals); plane `id` in [I_MF, I_UHF + 1] is the (id - I_MF)-th half plane of the block, with
+// the FP32 planes' element pitch.
+__device__ __forceinline__ __half* hplane(float* const* ib, const BScaleDev& S, int img, int id) {
+    return reinterpret_cast<__half*>(ib[img] + S.base + (int64_t)I_MF * S.n) + (int64_t)(id - I_MF) * S.n;
+}
+template <bool HB>
+__device__ __forceinline__ void band_store(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id,
+                                           int64_t i, float v) {
+    if (HB)
+        hplane(ib, S, img, id)[i] = __float2half_rn(v);
+    else
+        iplane(ib, g, S, img, id)[i] = v;
+}
+template <bool HB>
+__device__ __forceinline__ float band_load(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id,
+                                           int64_t i) {
+    if (HB) return __half2float(__ldg(hplane(ib, S, img, id) + i));
+    return __ldg(iplane(ib, g, S, img, id) + i);
 }
 // Select a scale with constant indices only, so the parameter struct is never copied to the
 // stack for a dynamic index.
@@ -490,6 +512,7 @@ __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
 // MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
 // written over the D planes (separatefrequencies.hpp:37-99,160-187).
 constexpr int kVMfSmem = (3 * (VB_TH + 18) * VB_TW + 2 * VB_TH * VB_TW) * 4;
+template <bool HB>
 __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* ctr = sm + 3 * (VB_TH + 18) * VB_TW;
@@ -503,9 +526,6 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restri
     if (x >= S.w) return;
     float* d0 = iplane(ib, g, S, img, I_XYB + 0);
     float* d1 = iplane(ib, g, S, img, I_XYB + 1);
-    float* m0 = iplane(ib, g, S, img, I_MF + 0);
-    float* m1 = iplane(ib, g, S, img, I_MF + 1);
-    float* m2 = iplane(ib, g, S, img, I_MF + 2);
     const float sx = 0.653020556257f, yw = 46.0f;
 #pragma unroll
     for (int o = 0; o < 8; o++) {
@@ -518,14 +538,15 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restri
             hx *= sx + (yw * (1.0f - sx)) / (yw + hy * hy);
             d0[i] = hx;
             d1[i] = hy;
-            m0[i] = remove_range(mf[0][o], 0.29f);
-            m1[i] = amplify_range(mf[1][o], 0.1f);
-            m2[i] = mf[2][o];
+            band_store<HB>(ib, g, S, img, I_MF + 0, i, remove_range(mf[0][o], 0.29f));
+            band_store<HB>(ib, g, S, img, I_MF + 1, i, amplify_range(mf[1][o], 0.1f));
+            band_store<HB>(ib, g, S, img, I_MF + 2, i, mf[2][o]);
         }
     }
 }
 
 // HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), nimages)
+template <bool HB>
 __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
@@ -548,8 +569,6 @@ __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restr
 #pragma unroll
         for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
         __syncthreads();
-        float* hfp = iplane(ib, g, S, img, I_HF + c);
-        float* uhfp = iplane(ib, g, S, img, I_UHF + c);
 #pragma unroll
         for (int o = 0; o < 6; o++) {
             const int x = x0 + vc, y = y0 + 6 * vg + o;
@@ -568,8 +587,8 @@ __global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restr
                     hf = amplify_range(hf, 0.132f);
                 }
                 const int64_t i = (int64_t)y * S.p + x;
-                hfp[i] = hf;
-                uhfp[i] = uhf;
+                band_store<HB>(ib, g, S, img, I_HF + c, i, hf);
+                band_store<HB>(ib, g, S, img, I_UHF + c, i, uhf);
             }
         }
     }
@@ -681,13 +700,20 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 // The six maps' raw (l0, l1) tiles are staged with cp.async, double-buffered across maps;
 // samples outside the image arrive as zeros, for which malta_pre returns exactly 0, the
 // reference's padding value (maltaDiff.hpp:549-553).
+// With half-band storage the raw tiles are FP16 rows of DFH_P halves staged from x0 - 8 (16-byte
+// chunks of 8 halves), and the window's column c sits at half c + 4 of its row.
 constexpr int DF_RAW = DF_IH * DF_IW;
 constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW) * 4;
+constexpr int DFH_P = 56;                   // 48 staged halves + 8 of padding (7 quads per row)
+constexpr int DFH_RAWF = DF_IH * DFH_P / 2;  // one FP16 raw tile, in floats
+constexpr int kDiffSmemH = (4 * DFH_RAWF + DF_RAW) * 4;
 
+template <bool HB>
 __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
                                                              BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
-    float* Dt = sm + 4 * DF_RAW;
+    constexpr int RAWF = HB ? DFH_RAWF : DF_RAW;  // floats per raw tile
+    float* Dt = sm + 4 * RAWF;
     const int2 pi = pimg[blockIdx.z];
     const int i0 = pi.x, i1 = pi.y;
     const BScaleDev S = pick_scale(g, s);
@@ -701,22 +727,26 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
     }
     // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X
     auto plane_id = [](int m) { return (m < 2 ? I_UHF : m < 4 ? I_HF : I_MF) + 1 - (m & 1); };
-    stage_rows<256>(sm, DF_IW, iplane(ib, g, S, i0, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
-                    DF_IW / 4);
-    stage_rows<256>(sm + DF_RAW, DF_IW, iplane(ib, g, S, i1, plane_id(0)), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
-                    DF_IH, DF_IW / 4);
+    auto stage = [&](float* dst, int img, int id) {
+        if (HB)
+            stage_rows_h<256>(reinterpret_cast<__half*>(dst), DFH_P, hplane(ib, S, img, id), S.p, S.w, S.h, x0 - 8,
+                              y0 - DF_H, DF_IH, 6);
+        else
+            stage_rows<256>(dst, DF_IW, iplane(ib, g, S, img, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
+                            DF_IW / 4);
+    };
+    stage(sm, i0, plane_id(0));
+    stage(sm + RAWF, i1, plane_id(0));
     cp_async_commit();
 #pragma unroll 1
     for (int m = 0; m < 6; m++) {
-        const float* r0 = sm + (m & 1) * 2 * DF_RAW;
-        const float* r1 = r0 + DF_RAW;
+        const float* r0 = sm + (m & 1) * 2 * RAWF;
+        const float* r1 = r0 + RAWF;
         if (m < 5) {
-            float* n0 = sm + ((m + 1) & 1) * 2 * DF_RAW;
+            float* n0 = sm + ((m + 1) & 1) * 2 * RAWF;
             const int id = plane_id(m + 1);
-            stage_rows<256>(n0, DF_IW, iplane(ib, g, S, i0, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
-                            DF_IW / 4);
-            stage_rows<256>(n0 + DF_RAW, DF_IW, iplane(ib, g, S, i1, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H,
-                            DF_IH, DF_IW / 4);
+            stage(n0, i0, id);
+            stage(n0 + RAWF, i1, id);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -724,10 +754,26 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         }
         __syncthreads();
         const MaltaMap mm = c_dp.mm[m];
+        if (HB) {
+            // two neighbouring samples per thread: one half2 load and conversion per image
+            constexpr int NP = DF_IH * DF_IW / 2;
 #pragma unroll
-        for (int k = 0; k < (DF_RAW + 255) / 256; k++) {
-            const int e = threadIdx.x + 256 * k;
-            if (e < DF_RAW) Dt[e] = malta_pre(r0[e], r1[e], mm);
+            for (int k = 0; k < (NP + 255) / 256; k++) {
+                const int e2 = threadIdx.x + 256 * k;
+                if (e2 < NP) {
+                    const int r = e2 / (DF_IW / 2), c = 2 * (e2 - r * (DF_IW / 2));
+                    const int hi = r * DFH_P + c + 4;
+                    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(r0) + hi));
+                    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(r1) + hi));
+                    *reinterpret_cast<float2*>(Dt + r * DF_IW + c) = make_float2(malta_pre(a.x, b.x, mm), malta_pre(a.y, b.y, mm));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < (DF_RAW + 255) / 256; k++) {
+                const int e = threadIdx.x + 256 * k;
+                if (e < DF_RAW) Dt[e] = malta_pre(r0[e], r1[e], mm);
+            }
         }
         __syncthreads();
         float res[8];
@@ -761,12 +807,12 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
                 const int im = m ? i1 : i0;
 #pragma unroll
                 for (int c = 0; c < 2; c++) {
-                    hf[m][c] = __ldg(iplane(ib, g, S, im, I_HF + c) + i);
-                    uhf[m][c] = __ldg(iplane(ib, g, S, im, I_UHF + c) + i);
+                    hf[m][c] = band_load<HB>(ib, g, S, im, I_HF + c, i);
+                    uhf[m][c] = band_load<HB>(ib, g, S, im, I_UHF + c, i);
                 }
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    mf[m][c] = __ldg(iplane(ib, g, S, im, I_MF + c) + i);
+                    mf[m][c] = band_load<HB>(ib, g, S, im, I_MF + c, i);
                     lf[m][c] = __ldg(iplane(ib, g, S, im, I_LFV + c) + i);
                 }
             }
@@ -1024,8 +1070,9 @@ __global__ void __launch_bounds__(256) butter_finalize_kernel(const float* __res
 // ------------------------------------------------------------------------------------------
 // Host side
 
-static BGeom make_bgeom(int64_t w, int64_t h) {
+static BGeom make_bgeom(int64_t w, int64_t h, bool half_bands) {
     BGeom g{};
+    g.half_bands = half_bands ? 1 : 0;
     int64_t off = 0;
     int64_t cw = w, ch = h;
     for (int s = 0; s < 2; s++) {
@@ -1035,7 +1082,9 @@ static BGeom make_bgeom(int64_t w, int64_t h) {
         S.p = (int)round_up(cw, 8);
         S.n = round_up((int64_t)S.p * ch, 64);
         S.base = off;
-        off += S.n * NIMG;
+        // S.n is a multiple of 64, so the FP16 block (NIMG - I_MF half planes) keeps the next
+        // scale's base 256-byte aligned
+        off += half_bands ? S.n * I_MF + S.n * (NIMG - I_MF) / 2 : S.n * NIMG;
         cw = half_dim(cw);
         ch = half_dim(ch);
     }
@@ -1095,15 +1144,19 @@ int butter_prepare_device() {
     int rc = upload_butter_tables();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmemH));
     const DiffParams P = make_diff_params();
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
     return E_OK;
 }
 
-size_t butter_image_floats(int64_t w, int64_t h) { return (size_t)make_bgeom(w, h).img_floats; }
-int butter_norm_tiles(int64_t w, int64_t h) { return make_bgeom(w, h).norm_tiles; }
+size_t butter_image_floats(int64_t w, int64_t h, bool half_bands) {
+    return (size_t)make_bgeom(w, h, half_bands).img_floats;
+}
+int butter_norm_tiles(int64_t w, int64_t h) { return make_bgeom(w, h, false).norm_tiles; }
 
 int ButterEngine::init(int64_t width, int64_t height, int qnorm_, float intensity_, int max_pairs_) {
     int rc = init_images(width, height, qnorm_, intensity_, 2 * max_pairs_, max_pairs_, true);
@@ -1124,7 +1177,7 @@ int ButterEngine::init_images(int64_t width, int64_t height, int qnorm_, float i
     max_images = max_images_;
     max_pairs = max_pairs_;
     if (max_images <= 0 || max_pairs <= 0) return E_BAD_POINTER;
-    BGeom g = make_bgeom(w, h);
+    BGeom g = make_bgeom(w, h, half_bands);
     for (int s = 0; s < 2; s++) {
         sc[s].w = g.s[s].w;
         sc[s].h = g.s[s].h;
@@ -1160,10 +1213,12 @@ void ButterEngine::destroy() {
     ibase = nullptr;
 }
 
-size_t ButterEngine::image_bytes(int64_t w, int64_t h) { return sizeof(float) * (size_t)make_bgeom(w, h).img_floats; }
+size_t ButterEngine::image_bytes(int64_t w, int64_t h, bool half_bands) {
+    return sizeof(float) * (size_t)make_bgeom(w, h, half_bands).img_floats;
+}
 
-size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs) {
-    BGeom g = make_bgeom(w, h);
+size_t ButterEngine::device_bytes(int64_t w, int64_t h, int pairs, bool half_bands) {
+    BGeom g = make_bgeom(w, h, half_bands);
     return (sizeof(float) * 2 * (size_t)g.img_floats + sizeof(float) * 3 * (size_t)g.norm_tiles +
             sizeof(float) * (size_t)w * h + sizeof(double) * 3 + sizeof(int2) + 2 * sizeof(float*)) *
            pairs;
@@ -1179,15 +1234,15 @@ int ButterEngine::launch_images(const FrameDesc* frames_dev, int nimages, const 
                                 double* norms_out, float* distmap_out, cudaStream_t st, const YuvParams* yuv) {
     if (nimages <= 0 || nimages > max_images || npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
     return butter_enqueue(w, h, qnorm, intensity, ibase, frames_dev, nimages, pimg, npairs, intype, partials,
-                          norms_out ? norms_out : norms, distmap_out, st, yuv);
+                          norms_out ? norms_out : norms, distmap_out, st, yuv, half_bands);
 }
 
 int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
                    int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
-                   float* distmap_out, cudaStream_t st, const YuvParams* yuv) {
+                   float* distmap_out, cudaStream_t st, const YuvParams* yuv, bool half_bands) {
     if (npairs <= 0 || nstage < 0) return E_BAD_POINTER;
     const YuvParams yp = yuv ? *yuv : yuv420p10_params();
-    const BGeom g = make_bgeom(w, h);
+    const BGeom g = make_bgeom(w, h, half_bands);
     const unsigned ni = (unsigned)nstage, np = (unsigned)npairs;
     if (ni) {
         dim3 gr((unsigned)ceil_div(w, 32), (unsigned)ceil_div(h, 32), ni);
@@ -1210,11 +1265,23 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
             { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
             { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(ib, g, s); }
             { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
-            { ProfScope ps_("butter_mf_v", st); butter_mf_v_kernel<<<gv, 256, kVMfSmem, st>>>(ib, g, s); }
-            { ProfScope ps_("butter_hf", st); butter_hf_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s); }
+            {
+                ProfScope ps_("butter_mf_v", st);
+                if (half_bands) butter_mf_v_kernel<true><<<gv, 256, kVMfSmem, st>>>(ib, g, s);
+                else butter_mf_v_kernel<false><<<gv, 256, kVMfSmem, st>>>(ib, g, s);
+            }
+            {
+                ProfScope ps_("butter_hf", st);
+                if (half_bands) butter_hf_kernel<true><<<gt, 256, kTileSmem, st>>>(ib, g, s);
+                else butter_hf_kernel<false><<<gt, 256, kTileSmem, st>>>(ib, g, s);
+            }
         }
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
-        { ProfScope ps_("butter_diff", st); butter_diff_kernel<<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s); }
+        {
+            ProfScope ps_("butter_diff", st);
+            if (half_bands) butter_diff_kernel<true><<<gd, 256, kDiffSmemH, st>>>(ib, pimg, g, s);
+            else butter_diff_kernel<false><<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s);
+        }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);
         { ProfScope ps_("butter_mask_blur", st); butter_mask_blur_kernel<<<gm, 256, kTileSmem, st>>>(ib, pimg, g, s); }
         const dim3 gf((unsigned)ceil_div(sw, DM_TW), (unsigned)ceil_div(sh, DM_TH), np);

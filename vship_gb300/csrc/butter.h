@@ -25,6 +25,9 @@ public:
     int qnorm = 2;
     float intensity = 203.f;
     int max_pairs = 0, max_images = 0;
+    // Keep the MF, HF and UHF bands as FP16 (set before init): 12.5 instead of 16 planes per
+    // image and scale; the norms move by the bands' FP16 rounding (the inf-norm by up to ~3e-4)
+    bool half_bands = false;
     ButterScale sc[2]{};
     float* work = nullptr;          // all intermediate planes, [image][scale][plane]
     size_t img_floats = 0;          // per image
@@ -50,21 +53,22 @@ public:
     // (device); distmap_out: null or npairs maps.
     int launch_images(const FrameDesc* frames_dev, int nimages, const int2* pimg, int npairs, int intype,
                       double* norms_out, float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr);
-    static size_t device_bytes(int64_t w, int64_t h, int pairs);
-    static size_t image_bytes(int64_t w, int64_t h);
+    static size_t device_bytes(int64_t w, int64_t h, int pairs, bool half_bands = false);
+    static size_t image_bytes(int64_t w, int64_t h, bool half_bands = false);
 };
 
 // Engine-free form (the serving runtime places images anywhere): upload this device's tables and
 // kernel attributes; floats of one image's workspace; norm partials per pair (x3 floats).
 int butter_prepare_device();
-size_t butter_image_floats(int64_t w, int64_t h);
+size_t butter_image_floats(int64_t w, int64_t h, bool half_bands = false);
 int butter_norm_tiles(int64_t w, int64_t h);
 // ib: device table of image workspaces; images [0, nstage) run their own stage (frames_dev[i]
 // is image i's frame), then every pair of pimg (indices into ib) runs the pair stage. partials:
 // npairs x 3 x norm_tiles floats; norms_out: npairs x 3 doubles; distmap_out: null or npairs maps;
-// yuv: format of IN_YUV frames (null: 10-bit 4:2:0 BT.709 limited, left siting).
+// yuv: format of IN_YUV frames (null: 10-bit 4:2:0 BT.709 limited, left siting); half_bands:
+// the images' layout (butter_image_floats).
 int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
                    int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
-                   float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr);
+                   float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr, bool half_bands = false);
 
 }  // namespace vship

@@ -41,8 +41,9 @@ static size_t butter_chunk_budget() {
     return (size_t)6 << 30;
 }
 
-static void butter_caps(int64_t w, int64_t h, int max_src, int max_pairs, int* cap_img, int* cap_pair) {
-    const size_t one = ButterEngine::image_bytes(w, h);
+static void butter_caps(int64_t w, int64_t h, int max_src, int max_pairs, bool half_bands, int* cap_img,
+                        int* cap_pair) {
+    const size_t one = ButterEngine::image_bytes(w, h, half_bands);
     const int fit = (int)std::min<size_t>(1 << 20, std::max<size_t>(2, butter_chunk_budget() / one));
     *cap_img = std::min(fit, std::max(2, max_src + max_pairs));
     *cap_pair = std::max(1, std::min(max_pairs, *cap_img - 1));
@@ -64,8 +65,9 @@ size_t MultiEngine::device_bytes(int nres, const int* widths, const int* heights
         }
         if ((flags & MULTI_BUTTERAUGLI) && max_pairs[r] > 0) {
             int ci = 0, cp = 0;
-            butter_caps(widths[r], heights[r], max_sources[r], max_pairs[r], &ci, &cp);
-            total += ButterEngine::image_bytes(widths[r], heights[r]) * ci +
+            const bool hb = (flags & MULTI_BUTTER_HALF) != 0;
+            butter_caps(widths[r], heights[r], max_sources[r], max_pairs[r], hb, &ci, &cp);
+            total += ButterEngine::image_bytes(widths[r], heights[r], hb) * ci +
                      (size_t)cp * (3 * 4 * (size_t)butter_norm_tiles(widths[r], heights[r]) + 24);
         }
     }
@@ -141,7 +143,9 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
     if (flags & MULTI_BUTTERAUGLI) {
         for (int r = 0; r < nres; r++) {
             if (!max_pairs[r]) continue;
-            butter_caps(rw[r], rh[r], max_src[r], max_pairs[r], &b_cap_img[r], &b_cap_pair[r]);
+            butter_caps(rw[r], rh[r], max_src[r], max_pairs[r], (flags & MULTI_BUTTER_HALF) != 0, &b_cap_img[r],
+                        &b_cap_pair[r]);
+            b_eng[r].half_bands = (flags & MULTI_BUTTER_HALF) != 0;
             int rc = b_eng[r].init_images(rw[r], rh[r], qnorm, intensity, b_cap_img[r], b_cap_pair[r], false);
             if (rc) return rc;
         }

@@ -39,7 +39,7 @@ int Server::create(int nres_, const int* widths, const int* heights, int intype_
         rw[r] = widths[r];
         rh[r] = heights[r];
         sgeom[r] = make_ssimu2_geom(rw[r], rh[r]);
-        bimg_floats[r] = butter_image_floats(rw[r], rh[r]);
+        bimg_floats[r] = butter_image_floats(rw[r], rh[r], (flags & SERVE_BUTTER_HALF_BANDS) != 0);
         bnorm_tiles[r] = butter_norm_tiles(rw[r], rh[r]);
         yuv_r[r] = yuv420p10_params();
     }
@@ -492,7 +492,7 @@ int Server::launch(Batch* b) {
                             reinterpret_cast<const FrameDesc*>(dtab + G.t_fr), G.nstage,
                             reinterpret_cast<const int2*>(dtab + G.t_pi), G.npairs, intype,
                             reinterpret_cast<float*>(block + G.part), dres + b->out_off[G.reqs[0]], nullptr, st,
-                            &yuv[G.res]);
+                            &yuv[G.res], (flags & SERVE_BUTTER_HALF_BANDS) != 0);
     }
     if (!rc && cudaMemcpyAsync(h + b->res_off, dres, res_doubles * sizeof(double), cudaMemcpyDeviceToHost, st) !=
                    cudaSuccess)
