@@ -203,22 +203,29 @@ __global__ void __launch_bounds__(256) ssimu2_pyramid_kernel(const FrameDesc* __
 // Kernel 2: fused moment blur + SSIM/edge maps + per-CTA pooling, all scales in one launch.
 // grid (tiles_total, npairs), 256 threads, dynamic smem kStatsSmem, three CTAs per SM.
 //
-// Per CTA: one 32x48 output tile of one scale. For each channel the raw I1 and I2 tiles with an
-// 8-px halo (64 rows x 48 columns) are staged with cp.async (bytes outside the image are
-// zero-filled); one CTA's loads overlap the arithmetic of the other CTAs on its SM. The
-// horizontal pass reads the raw rows as float4 (row pitch 52 floats: the 8 lanes of each
-// quarter-warp phase hit distinct bank quads), forms the shifted samples and their products in
-// registers and scatters them into 8 outputs x 5 moments; the vertical pass gathers 22 rows per
-// thread and evaluates the maps.
+// Per CTA: one segment of one scale -- a 32-column strip, ST_SEG rows tall -- walked down in
+// chunks of 48 output rows. For each channel and chunk the raw I1 and I2 rows (8-px halo) are
+// staged with cp.async (bytes outside the image are zero-filled); one CTA's loads overlap the
+// arithmetic of the other CTAs on its SM. The horizontal pass reads the raw rows as float4 (row
+// pitch 52 floats: the 8 lanes of each quarter-warp phase hit distinct bank quads), forms the
+// shifted samples and their products in registers and scatters them into 8 outputs x 4 moments,
+// into a ring of horizontal-pass rows; the vertical pass gathers 22 ring rows per thread and
+// evaluates the maps. The ring keeps the 16 rows a chunk shares with the next, so the vertical
+// halo is blurred horizontally once per segment instead of once per chunk (64 instead of 48
+// horizontal rows per 48 output rows).
 constexpr int ST_TW = 32, ST_TH = 48, ST_R = 8;
+constexpr int ST_SEG = 4 * ST_TH;        // segment height (output rows)
 constexpr int ST_IW = ST_TW + 2 * ST_R;  // 48 input columns
-constexpr int ST_IH = ST_TH + 2 * ST_R;  // 64 input rows
+constexpr int ST_IH = ST_TH + 2 * ST_R;  // 64 raw rows per chunk (image rows ty0 - 8 ..)
 constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte multiple, 13 quads)
-constexpr int ST_HP = 33;                // horizontal-pass output pitch
+constexpr int ST_HP = 33;                // horizontal-pass row pitch (float pairs)
 constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
-constexpr int ST_HPLANE = ST_IH * ST_HP;
-// smem: the 2 raw images, the horizontal pass as two float-pair planes {m1, m2} and
-// {s11 + s22, s12}, and the per-warp pools: 61 KB, so that three CTAs share an SM
+constexpr int ST_RING = 64;              // ring slots (power of two): row h of a segment -> h & 63
+constexpr int ST_WIN = ST_TH / 8 + 2 * ST_R;             // 22 ring rows per vertical window
+constexpr int ST_HROWS = ST_RING + ST_WIN;               // slots [0, 22) mirrored at [64, 86)
+constexpr int ST_HPLANE = ST_HROWS * ST_HP;
+// smem: the 2 raw images, the ring as two float-pair planes {m1, m2} and {s11 + s22, s12}, and
+// the per-warp pools: 71 KB, so that three CTAs share an SM
 constexpr int kStatsSmem = (2 * ST_RAW + 4 * ST_HPLANE + 3 * 8 * 6) * 4;
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
@@ -228,10 +235,10 @@ __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     return 1.0f / (c_s2_I[end] - c_s2_I[beg]);
 }
 
-// Stage the 64x48 halo tile of one plane: 768 16-byte chunks, 3 per thread. The tile's first
-// column (tile x - 8) is a multiple of 4 floats and every row starts 32-byte aligned, so each
-// chunk is either fully outside the image, fully inside, or cut by the right edge (partial
-// source size, the rest zero-filled).
+// Stage the 64x48 halo tile of one plane (row r = image row y0 - 8 + r): 768 16-byte chunks, 3
+// per thread. The tile's first column (tile x - 8) is a multiple of 4 floats and every row starts
+// 32-byte aligned, so each chunk is either fully outside the image, fully inside, or cut by the
+// right edge (partial source size, the rest zero-filled).
 __device__ __forceinline__ void stage_tile(float* dst, const float* __restrict__ plane, int pitch, int w, int h,
                                            int x0, int y0) {
 #pragma unroll
@@ -267,194 +274,220 @@ __device__ __forceinline__ void stage_tile_h(__half* dst, const __half* __restri
     }
 }
 
-// One 32x48 output tile of one scale: the five moments, the maps and 18 pooled sums written to
-// out[pool * stride] (pool = map * 2 + norm, times 3 channels). im1 / im2 point at the tile's scale
-// in the channel-0 plane; DELTA: im2 holds FP16 differences against im1.
+// One segment (32 columns x up to ST_SEG rows) of one scale: the four moments, the maps and 18
+// pooled sums written to out[pool * stride] (pool = map * 2 + norm, times 3 channels). im1 / im2
+// point at the tile's scale in the channel-0 plane; DELTA: im2 holds FP16 differences against im1.
 template <bool DELTA>
 __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const void* __restrict__ im2v, int64_t pe,
                                            const Ssimu2Level& L, int lt, float* __restrict__ out, int stride) {
     extern __shared__ __align__(16) float sm[];
     float* raw = sm;                   // [image][64][52]
-    float* hb = sm + 2 * ST_RAW;       // [4][64][33]
+    float* hb = sm + 2 * ST_RAW;       // [2 pair planes][86][33 pairs]
     float* red = hb + 4 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
     const float* im2 = static_cast<const float*>(im2v);
     const __half* im2h = static_cast<const __half*>(im2v);
     const int tx0 = (lt % L.tiles_x) * ST_TW;
-    const int ty0 = (lt / L.tiles_x) * ST_TH;
+    const int sy0 = (lt / L.tiles_x) * ST_SEG;
+    const int nchunk = (min(ST_SEG, L.h - sy0) + ST_TH - 1) / ST_TH;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool interior = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h;
+    const bool x_inside = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w;
 
-    // H pass mapping: row hr (0..63), output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23).
-    // A warp covers 8 consecutive rows x 4 column groups, which keeps the float4 raw reads, the
-    // float-pair stores (pitch 33 pairs) and the float stores (pitch 33) bank-conflict free.
-    const int hr = 8 * warp + (lane & 7), hg = lane >> 3;
-    // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5. Both passes' border
-    // renormalisations (out / tot, gaussianblur.hpp:63-92) are applied here as one product.
+    // H pass mapping: output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23) of 8 consecutive raw
+    // rows per warp x 4 column groups, which keeps the float4 raw reads and the float-pair stores
+    // (pitch 33 pairs) bank-conflict free.
+    const int hg = lane >> 3;
+    // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5 of the chunk. Both passes'
+    // border renormalisations (out / tot, gaussianblur.hpp:63-92) are applied here as one product.
     const int vc = tid & 31, vg = tid >> 5;
     const float rxv = s2_inv_mass(tx0 + vc, L.w);
-    float rxy[6];
-#pragma unroll
-    for (int o = 0; o < 6; o++) rxy[o] = rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
+    const float rx_in = rxv * (1.0f / (c_s2_I[17] - c_s2_I[0]));  // rows whose window is inside
+    float* r1 = raw;
+    float* r2 = raw + ST_RAW;
 
 #pragma unroll 1
     for (int c = 0; c < 3; c++) {
-        // one stage: the channel's two raw tiles; the loads of one CTA overlap the arithmetic of
-        // the SM's other two
-        float* r1 = raw;
-        float* r2 = raw + ST_RAW;
-        stage_tile(r1, im1 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
-        if (DELTA)
-            stage_tile_h(reinterpret_cast<__half*>(r2), im2h + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
-        else
-            stage_tile(r2, im2 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
-        cp_async_commit();
-        cp_async_wait<0>();
-        __syncthreads();
-        // Moments are formed on values shifted by one per-tile constant (the reference image's
-        // value at the tile origin). The blur is normalised, so sigma = E[(x-s)^2] - (E[x]-s)^2
-        // is unchanged, while the FP32 cancellation of E[x^2] - E[x]^2 shrinks by the square of
-        // |x| / |x - s|. Samples outside the image must carry nothing: on border tiles their
-        // slots are set to the shift itself, so that x - s is exactly zero there.
-        const float shift = r1[ST_R * ST_RP + ST_R];
-        if (!interior) {
-            for (int e = tid; e < ST_IH * ST_IW; e += 256) {
-                const int r = e / ST_IW, col = e - r * ST_IW;
-                const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
-                if (gx < 0 || gx >= L.w || gy < 0 || gy >= L.h) {
-                    r1[r * ST_RP + col] = shift;
-                    if (!DELTA) r2[r * ST_RP + col] = shift;  // FP16 deltas arrive as zeros there
-                }
-            }
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float shift = 0.f;
+#pragma unroll 1
+        for (int k = 0; k < nchunk; k++) {
+            const int ty0 = sy0 + k * ST_TH;
+            stage_tile(r1, im1 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+            if (DELTA)
+                stage_tile_h(reinterpret_cast<__half*>(r2), im2h + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+            else
+                stage_tile(r2, im2 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+            cp_async_commit();
+            cp_async_wait<0>();
             __syncthreads();
-        }
-        {
-            // Horizontal pass. Lane mapping: row hr = 8*warp + (lane & 7), outputs 8*hg..+7 with
-            // hg = lane >> 3. The SSIM map needs the two variances only as their sum
-            // (score.hpp:147), so four moments are blurred: {a, b} and {a^2 + b^2, a*b}, each pair
-            // through the f32x2 FMA with a shared weight.
-            f2_t h1[8], h2[8];
-            const f2_t z2 = f2_pack(0.f, 0.f);
-#pragma unroll
-            for (int o = 0; o < 8; o++) {
-                h1[o] = z2;
-                h2[o] = z2;
-            }
-            const float* ra = r1 + hr * ST_RP + 8 * hg;
-            const float* rb = r2 + hr * ST_RP + 8 * hg;
-            float dl[24];  // DELTA: the 24 deltas of this thread's window
-            if (DELTA) {
-                const __half* rd = reinterpret_cast<const __half*>(r2) + hr * ST_DP + 8 * hg;
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    const uint4 q = *reinterpret_cast<const uint4*>(rd + 8 * k);
-                    const __half2* hq = reinterpret_cast<const __half2*>(&q);
-#pragma unroll
-                    for (int u = 0; u < 4; u++) {
-                        const float2 f = __half22float2(hq[u]);
-                        dl[8 * k + 2 * u] = f.x;
-                        dl[8 * k + 2 * u + 1] = f.y;
+            // Moments are formed on values shifted by one per-segment constant (the reference
+            // image's value at the segment origin). The blur is normalised, so sigma =
+            // E[(x-s)^2] - (E[x]-s)^2 is unchanged, while the FP32 cancellation of E[x^2] - E[x]^2
+            // shrinks by the square of |x| / |x - s|. Samples outside the image must carry
+            // nothing: on border chunks their slots are set to the shift itself, so that x - s is
+            // exactly zero there.
+            if (k == 0) shift = r1[ST_R * ST_RP + ST_R];
+            if (!(x_inside && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h)) {
+                for (int e = tid; e < ST_IH * ST_IW; e += 256) {
+                    const int r = e / ST_IW, col = e - r * ST_IW;
+                    const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
+                    if (gx < 0 || gx >= L.w || gy < 0 || gy >= L.h) {
+                        r1[r * ST_RP + col] = shift;
+                        if (!DELTA) r2[r * ST_RP + col] = shift;  // FP16 deltas arrive as zeros there
                     }
                 }
+                __syncthreads();
             }
+            // Horizontal pass over the raw rows whose ring row is new: rows 0..63 of the first
+            // chunk (8 warps), rows 16..63 later (6 warps, the two idle ones rotating with the
+            // chunk so that the SM's four schedulers share the work evenly). Segment row
+            // h = 48k + r goes to ring slot h & 63, and to slot 64 + (h & 63) as well when that is
+            // below 22. The SSIM map needs the two variances only as their sum (score.hpp:147), so
+            // four moments are blurred: {a, b} and {a^2 + b^2, a*b}, each pair through the f32x2
+            // FMA with a shared weight.
+            const int rr = k == 0 ? 8 * warp + (lane & 7) : 2 * ST_R + 8 * ((warp + 2 * k) & 7) + (lane & 7);
+            if (rr < ST_IH) {
+                f2_t h1[8], h2[8];
+                const f2_t z2 = f2_pack(0.f, 0.f);
 #pragma unroll
-            for (int j4 = 0; j4 < 6; j4++) {
-                const float4 va = *reinterpret_cast<const float4*>(ra + 4 * j4);
-                float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (!DELTA) vb = *reinterpret_cast<const float4*>(rb + 4 * j4);
-                const float la[4] = {va.x, va.y, va.z, va.w};
-                const float lb[4] = {vb.x, vb.y, vb.z, vb.w};
+                for (int o = 0; o < 8; o++) {
+                    h1[o] = z2;
+                    h2[o] = z2;
+                }
+                const float* ra = r1 + rr * ST_RP + 8 * hg;
+                const float* rb = r2 + rr * ST_RP + 8 * hg;
+                float dl[24];  // DELTA: the 24 deltas of this thread's window
+                if (DELTA) {
+                    const __half* rd = reinterpret_cast<const __half*>(r2) + rr * ST_DP + 8 * hg;
 #pragma unroll
-                for (int u = 0; u < 4; u++) {
-                    const int j = 4 * j4 + u;
-                    const float a = la[u] - shift;
-                    const float b = DELTA ? a + dl[j] : lb[u] - shift;
-                    const f2_t p1 = f2_pack(a, b);
-                    const f2_t p2 = f2_pack(fmaf(a, a, b * b), a * b);
+                    for (int q = 0; q < 3; q++) {
+                        const uint4 v4 = *reinterpret_cast<const uint4*>(rd + 8 * q);
+                        const __half2* hq = reinterpret_cast<const __half2*>(&v4);
 #pragma unroll
-                    for (int o = 0; o < 8; o++) {
-                        const int i = j - o;  // tap index
-                        if (i >= 0 && i < 17) {
-                            h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
-                            h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
+                        for (int u = 0; u < 4; u++) {
+                            const float2 f = __half22float2(hq[u]);
+                            dl[8 * q + 2 * u] = f.x;
+                            dl[8 * q + 2 * u + 1] = f.y;
                         }
                     }
                 }
-            }
-            f2_t* d1 = reinterpret_cast<f2_t*>(hb) + hr * ST_HP + 8 * hg;
-            f2_t* d2 = reinterpret_cast<f2_t*>(hb + 2 * ST_HPLANE) + hr * ST_HP + 8 * hg;
 #pragma unroll
-            for (int o = 0; o < 8; o++) {
-                d1[o] = h1[o];
-                d2[o] = h2[o];
-            }
-        }
-        __syncthreads();
-        // vertical pass + maps (column vc, rows 6*vg .. 6*vg+5)
-        float m[4][6];  // mu1, mu2, E[a^2 + b^2], E[a b] (shifted)
-        {
-            const f2_t* c1 = reinterpret_cast<const f2_t*>(hb) + (6 * vg) * ST_HP + vc;
-            const f2_t* c2 = reinterpret_cast<const f2_t*>(hb + 2 * ST_HPLANE) + (6 * vg) * ST_HP + vc;
+                for (int j4 = 0; j4 < 6; j4++) {
+                    const float4 va = *reinterpret_cast<const float4*>(ra + 4 * j4);
+                    float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (!DELTA) vb = *reinterpret_cast<const float4*>(rb + 4 * j4);
+                    const float la[4] = {va.x, va.y, va.z, va.w};
+                    const float lb[4] = {vb.x, vb.y, vb.z, vb.w};
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const f2_t* col = q == 0 ? c1 : c2;
-                f2_t v[22];
+                    for (int u = 0; u < 4; u++) {
+                        const int j = 4 * j4 + u;
+                        const float a = la[u] - shift;
+                        const float b = DELTA ? a + dl[j] : lb[u] - shift;
+                        const f2_t p1 = f2_pack(a, b);
+                        const f2_t p2 = f2_pack(fmaf(a, a, b * b), a * b);
 #pragma unroll
-                for (int j = 0; j < 22; j++) v[j] = col[j * ST_HP];
+                        for (int o = 0; o < 8; o++) {
+                            const int i = j - o;  // tap index
+                            if (i >= 0 && i < 17) {
+                                h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
+                                h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
+                            }
+                        }
+                    }
+                }
+                const int slot = (k * ST_TH + rr) & (ST_RING - 1);
+                f2_t* d1 = reinterpret_cast<f2_t*>(hb) + slot * ST_HP + 8 * hg;
+                f2_t* d2 = reinterpret_cast<f2_t*>(hb + 2 * ST_HPLANE) + slot * ST_HP + 8 * hg;
 #pragma unroll
-                for (int o = 0; o < 6; o++) {
-                    f2_t a = f2_pack(0.f, 0.f);
+                for (int o = 0; o < 8; o++) {
+                    d1[o] = h1[o];
+                    d2[o] = h2[o];
+                }
+                if (slot < ST_WIN) {
 #pragma unroll
-                    for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], c_s2_k2[i], a);
-                    a = f2_mul(a, f2_pack(rxy[o], rxy[o]));
-                    f2_unpack(a, m[2 * q][o], m[2 * q + 1][o]);
+                    for (int o = 0; o < 8; o++) {
+                        d1[ST_RING * ST_HP + o] = h1[o];
+                        d2[ST_RING * ST_HP + o] = h2[o];
+                    }
                 }
             }
-        }
-        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            __syncthreads();
+            // vertical pass + maps (column vc, chunk rows 6*vg .. 6*vg+5): the window is ring rows
+            // s0 .. s0+21 with s0 = (48k + 6*vg) & 63, never past the mirrored slots
+            float rxy[6];
+            if (ty0 + 6 * vg >= ST_R && ty0 + 6 * vg + 5 + ST_R < L.h) {
 #pragma unroll
-        for (int o = 0; o < 6; o++) {
-            const int y = ty0 + 6 * vg + o, x = tx0 + vc;
-            if (x < L.w && y < L.h) {
-                const int so = (6 * vg + o + ST_R) * ST_RP + vc + ST_R;
-                const float i1 = r1[so] - shift;  // shifted samples
-                const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(6 * vg + o + ST_R) * ST_DP +
-                                                                                                 vc + ST_R])
-                                       : r2[so] - shift;
-                const float m1 = m[0][o], m2 = m[1][o];                 // shifted means
-                // SSIM map (score.hpp:141-148) as max((den - num) / den, 0), the same quantity
-                // as max(1 - num / den, 0) without the cancellation; sigma11 + sigma22 as
-                // (S/2 - m1^2) + (S/2 - m2^2) with S = E[a^2 + b^2]. Explicit fma: identical
-                // frames give S/2 == E[ab] exactly (a^2 + b^2 = 2ab), so num == den bitwise
-                const float md = m1 - m2;
-                const float num_m = fmaf(md, -md, 1.0f);
-                const float hs = 0.5f * m[2][o];
-                const float s12 = fmaf(-m1, m2, m[3][o]);
-                const float s11 = fmaf(-m1, m1, hs);
-                const float s22 = fmaf(-m2, m2, hs);
-                const float num_s = fmaf(s12, 2.0f, 0.0009f);
-                const float denom = (s11 + s22) + 0.0009f;
-                const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
-                // edge maps (score.hpp:151-153): (|I2-m2| + 1) / (|I1-m1| + 1) - 1 written as
-                // (|I2-m2| - |I1-m1|) / (|I1-m1| + 1); |I - mu| is shift-invariant
-                const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
-                const float v1 = __fdividef(e2 - e1, e1 + 1.0f);
-                const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
-                const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
-                acc[0] += d0;
-                acc[1] += q0 * q0;
-                acc[2] += d1;
-                acc[3] += q1 * q1;
-                acc[4] += d2;
-                acc[5] += q2 * q2;
+                for (int o = 0; o < 6; o++) rxy[o] = rx_in;
+            } else {
+#pragma unroll
+                for (int o = 0; o < 6; o++) rxy[o] = rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
             }
+            float m[4][6];  // mu1, mu2, E[a^2 + b^2], E[a b] (shifted)
+            {
+                const int s0 = (k * ST_TH + 6 * vg) & (ST_RING - 1);
+                const f2_t* c1 = reinterpret_cast<const f2_t*>(hb) + s0 * ST_HP + vc;
+                const f2_t* c2 = reinterpret_cast<const f2_t*>(hb + 2 * ST_HPLANE) + s0 * ST_HP + vc;
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const f2_t* col = q == 0 ? c1 : c2;
+                    f2_t v[ST_WIN];
+#pragma unroll
+                    for (int j = 0; j < ST_WIN; j++) v[j] = col[j * ST_HP];
+#pragma unroll
+                    for (int o = 0; o < 6; o++) {
+                        f2_t a = f2_pack(0.f, 0.f);
+#pragma unroll
+                        for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], c_s2_k2[i], a);
+                        a = f2_mul(a, f2_pack(rxy[o], rxy[o]));
+                        f2_unpack(a, m[2 * q][o], m[2 * q + 1][o]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 6; o++) {
+                const int y = ty0 + 6 * vg + o, x = tx0 + vc;
+                if (x < L.w && y < L.h) {
+                    const int so = (6 * vg + o + ST_R) * ST_RP + vc + ST_R;
+                    const float i1 = r1[so] - shift;  // shifted samples
+                    const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(6 * vg + o + ST_R) * ST_DP +
+                                                                                                     vc + ST_R])
+                                           : r2[so] - shift;
+                    const float m1 = m[0][o], m2 = m[1][o];  // shifted means
+                    // SSIM map (score.hpp:141-148) as max((den - num) / den, 0), the same quantity
+                    // as max(1 - num / den, 0) without the cancellation; sigma11 + sigma22 as
+                    // (S/2 - m1^2) + (S/2 - m2^2) with S = E[a^2 + b^2]. Explicit fma: identical
+                    // frames give S/2 == E[ab] exactly (a^2 + b^2 = 2ab), so num == den bitwise
+                    const float md = m1 - m2;
+                    const float num_m = fmaf(md, -md, 1.0f);
+                    const float hs = 0.5f * m[2][o];
+                    const float s12 = fmaf(-m1, m2, m[3][o]);
+                    const float s11 = fmaf(-m1, m1, hs);
+                    const float s22 = fmaf(-m2, m2, hs);
+                    const float num_s = fmaf(s12, 2.0f, 0.0009f);
+                    const float denom = (s11 + s22) + 0.0009f;
+                    const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
+                    // edge maps (score.hpp:151-153): (|I2-m2| + 1) / (|I1-m1| + 1) - 1 written as
+                    // (|I2-m2| - |I1-m1|) / (|I1-m1| + 1); |I - mu| is shift-invariant
+                    const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
+                    const float v1 = __fdividef(e2 - e1, e1 + 1.0f);
+                    const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
+                    const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
+                    acc[0] += d0;
+                    acc[1] += q0 * q0;
+                    acc[2] += d1;
+                    acc[3] += q1 * q1;
+                    acc[4] += d2;
+                    acc[5] += q2 * q2;
+                }
+            }
+            __syncthreads();  // the raw tiles and ring slots are rewritten by the next chunk
         }
 #pragma unroll
         for (int i = 0; i < 6; i++) {
             const float v = warp_sum(acc[i]);
             if (lane == 0) red[(c * 8 + warp) * 6 + i] = v;
         }
-        __syncthreads();
     }
+    __syncthreads();
     // pools: out[(pool * 3 + channel) * stride], pool = map * 2 + norm
     if (tid < 18) {
         const int pool = tid / 3, c = tid - pool * 3;
@@ -584,7 +617,7 @@ Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h) {
         L.off = off;
         off += round_up((int64_t)L.pitch * ch, 64);
         L.tiles_x = (int)ceil_div(cw, ST_TW);
-        L.tiles_y = (int)ceil_div(ch, ST_TH);
+        L.tiles_y = (int)ceil_div(ch, ST_SEG);
         g.tile_begin[s] = tiles;
         tiles += L.tiles_x * L.tiles_y;
         cw = half_dim(cw);

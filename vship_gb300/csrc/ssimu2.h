@@ -19,7 +19,8 @@ struct Ssimu2Level {
     int64_t off;  // element offset of the level inside one channel plane
 };
 
-// Geometry of the 6-scale pyramid and of the stats-kernel tiling (32x48 output tiles).
+// Geometry of the 6-scale pyramid and of the stats-kernel tiling (segments of 32 columns x
+// 192 rows, one CTA each).
 struct Ssimu2Geom {
     Ssimu2Level lv[6];
     int tile_begin[7];
