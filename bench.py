@@ -84,6 +84,28 @@ def butter_diff_bytes(w, h):
     return 24 * 4 * (n + nh)
 
 
+def kernel_bytes_per_pair(kind, w, h, in_bytes):
+    """Algorithmic DRAM bytes each kernel moves per frame pair with FP32 planes: every plane it
+    must read or write, once (halos and re-reads not counted); in_bytes = input bytes per pixel
+    of one frame (6 for RGB48)."""
+    if kind == "ssimu2":
+        t = total_scale_pixels(w, h)
+        return {"ssimu2_pyramid": 2 * in_bytes * w * h + 2 * 12 * t, "ssimu2_stats": 2 * 12 * t}
+    n = w * h
+    nh = ((w - 1) // 2 + 1) * ((h - 1) // 2 + 1)
+    ns = n + nh
+    return {"butter_decode": 2 * in_bytes * n + 2 * 12 * ns,  # linear RGB at both scales
+            "butter_opsin": 2 * 24 * ns,      # linear RGB in, XYB out
+            "butter_hblur_lf": 2 * 24 * ns,   # 3 planes in, 3 out
+            "butter_lf_v": 2 * 48 * ns,       # 3 blurred + 3 XYB in, D and LF vals out
+            "butter_hblur_mf": 2 * 24 * ns,
+            "butter_mf_v": 2 * 40 * ns,       # 3 blurred + 2 D in, 2 HF_pre + 3 MF out
+            "butter_hf": 2 * 24 * ns,         # 2 HF_pre in, HF and UHF out
+            "butter_diff": 96 * ns,           # 20 band planes in, 4 pair planes out
+            "butter_mask_blur": 20 * ns,      # 2 mask precomputes + AC in, blurred mask + AC out
+            "butter_diffmap": 16 * ns + 4 * nh}
+
+
 # Whole-pipeline algorithmic bytes per pair (b_in = 3 B/px for 16-bit 4:2:0 input; FP32 planes).
 def ssimu2_pair_bytes(w, h):
     return 2 * 3 * w * h + 2 * 12 * total_scale_pixels(w, h) * 2
@@ -420,6 +442,30 @@ def cpu_baseline(kind, ref, dst, sample_pairs, nthreads, fp64_pairs=0):
     return sample_pairs / t_total, t_total, exact
 
 
+def host_link_gbs():
+    """Pinned host -> device copy bandwidth (256 MiB, best of 3, CUDA events): the ceiling of
+    every e2e number, whose inputs cross this link each step."""
+    import torch
+    n = 256 << 20
+    src = torch.empty(n, dtype=torch.uint8).pin_memory()
+    dst = torch.empty(n, dtype=torch.uint8, device="cuda")
+    best = 0.0
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        dst.copy_(src, non_blocking=True)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, n / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    del src, dst
+    return best
+
+
+def link_frac(link, e2e, npairs):
+    """An e2e run's host->device bytes per second as a fraction of the measured link bandwidth."""
+    return round(e2e["h2d_bytes_per_step"] / npairs * e2e["value"] / 1e9 / link, 3)
+
+
 def rel_err(got, want):
     return [abs(g - w) / max(abs(w), 1e-12) for g, w in zip(got, want)]
 
@@ -483,6 +529,12 @@ def bench_workload(v, kind, args, ws, rank):
     kname = "ssimu2_stats" if kind == "ssimu2" else "butter_diff"
     per_pair = ssimu2_stats_bytes(w, h) if kind == "ssimu2" else butter_diff_bytes(w, h)
     peak, peak_kind = measured_peaks()
+    # every kernel's algorithmic bytes over its summed CUDA-event time, against the HBM peak
+    kroof = {}
+    for k, kb in kernel_bytes_per_pair(kind, w, h, 6).items():
+        if k in prof and prof[k][1] > 0:
+            gbs = kb * npairs * args.steps / (prof[k][1] / 1e3) / 1e9
+            kroof[k] = {"gbs": round(gbs, 1), "frac": round(gbs / peak, 3)}
     n_launch, tot_ms = prof.get(kname, (0, 0.0))
     # algorithmic bytes moved by this kernel over the timed region / its summed launch time
     # (for Butteraugli the per-pair figure covers both scales, i.e. two launches per batch)
@@ -538,6 +590,7 @@ def bench_workload(v, kind, args, ws, rank):
                 "threads": args.e2e_threads, "steps": args.e2e_steps,
                 "call": "Vship_ComputeSSIMU2Uint16" if kind == "ssimu2" else "Vship_ComputeButteraugliUint16v3"},
         "fp32_roofline": fp32_roof,
+        "kernel_roofline": kroof,
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "traffic": traffic * pairs_per_launch if traffic is not None else None,
@@ -944,6 +997,7 @@ def main_ours(args):
         from vship_gb300 import build
         build.build()
     v.lib()
+    link = host_link_gbs()
     out = {"metric": "frame-pairs/s (1080p SSIMU2)", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "gpu_launches": 0}
     s2 = {}
@@ -960,17 +1014,26 @@ def main_ours(args):
         "e2e": s2["e2e"], "roofline": s2["roofline"], "fp32_roofline": s2["fp32_roofline"],
         "gpu_launches": s2["gpu_launches"], "clocks": s2["clocks"],
         "kernel_share": s2["kernel_share"], "pipeline_bytes_per_pair": s2["pipeline_bytes_per_pair"],
+        "kernel_roofline": s2["kernel_roofline"],
         "yuv420p10": s2["yuv420p10"], "float32_rgb": s2["float32_rgb"], "input": s2["input"],
         "score_check": s2["score_check"],
         })
     if "cpu_baseline" in s2:
         out["cpu_baseline"] = s2["cpu_baseline"]
+    out["host_link"] = {"h2d_gbs": round(link, 1),
+                        "note": "pinned host -> device copy, 256 MiB; e2e frac = its h2d bytes/s over this"}
+    if s2:
+        n = s2["pairs_per_step"]
+        out["host_link"]["ssimu2_e2e_frac"] = {"rgb48": link_frac(link, s2["e2e"], n),
+                                              "float32_rgb": link_frac(link, s2["float32_rgb"]["e2e"], n),
+                                              "yuv420p10": link_frac(link, s2["yuv420p10"]["e2e"], n)}
     if not args.skip_butter:
         b = bench_workload(v, "butter", args, ws, rank)
         out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e", "yuv420p10",
                                                    "float32_rgb", "input",
                                                    "roofline", "gpu_launches", "clocks", "kernel_share",
-                                                   "pipeline_bytes_per_pair", "score_check", "fp16_bands")
+                                                   "pipeline_bytes_per_pair", "score_check", "fp16_bands",
+                                                   "kernel_roofline")
                                  if k in b}
         if "cpu_baseline" in b:
             out["butteraugli_4k"]["cpu_baseline"] = b["cpu_baseline"]
