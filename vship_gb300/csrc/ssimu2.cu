@@ -6,11 +6,12 @@
 //                        from shared memory (the pyramid is tile-local: a 2^k-aligned level-0
 //                        tile maps exactly onto its level-k tile, edge clamp included).
 //                        Reference: ssimu2/main.hpp:15-32, makeXYB.hpp:4-98, downsample.hpp:3-31.
-//   2. ssimu2_stats    : all six scales in one launch. Per 32x48 output tile it stages I1, I2,
-//                        I1^2, I2^2, I1*I2 (8-px halo, zero outside) in shared memory, runs the
-//                        17-tap separable Gaussian (border-renormalised) for the five moments with
-//                        register blocking, forms the SSIM / artifact / detail-loss maps and emits
-//                        18 partial sums (6 pools x 3 channels) per CTA.
+//   2. ssimu2_stats    : all six scales in one launch. Per 32x192 segment, in 48-row chunks,
+//                        it stages I1 and I2 (8-px halo, zero outside) in shared memory, runs the
+//                        17-tap separable Gaussian (border-renormalised) for four moments (mu1,
+//                        mu2, E[I1^2 + I2^2], E[I1 I2]) with register blocking and a ring of
+//                        horizontal-pass rows, forms the SSIM / artifact / detail-loss maps and
+//                        emits 18 partial sums (6 pools x 3 channels) per CTA.
 //                        Reference: ssimu2/score.hpp:95-196, gaussianblur.hpp:24-92.
 //   3. ssimu2_finalize : FP64 combine of the partial sums, 4th roots, the 108-feature permutation,
 //                        weighted sum and score mapping (score.hpp:198-401, main.hpp:83-98).
