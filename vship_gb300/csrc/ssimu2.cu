@@ -126,21 +126,23 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
     __shared__ float smB[3 * 16 * 17];
     const int64_t pe = g.plane_elems;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    // R'G'B' planes whose rows allow it: each thread loads 4 consecutive samples of one row per
-    // plane with one vector load (8 bytes of uint16, 16 of float) and stores its 4 level-0
-    // outputs per channel as one float4 (level rows are 16-byte aligned, columns a multiple of 4)
-    constexpr bool kVecType = (IT == IN_UINT16 || IT == IN_FLOAT) && !DELTA;
+    // Level 0 four pixels per thread (4 consecutive columns of one row): R'G'B' planes whose rows
+    // allow it load them with one vector load per plane (8 bytes of uint16, 16 of float), Y'CbCr
+    // loads each chroma sample once for the four (yuv_rgb4); FP32 pyramids store the 4 outputs
+    // per channel as one float4 (level rows are 16-byte aligned, columns a multiple of 4).
+    constexpr bool kRgbVec = IT == IN_UINT16 || IT == IN_FLOAT;
     constexpr unsigned kVecAlign = IT == IN_FLOAT ? 16u : 8u;
-    const bool vec = kVecType &&
-                     (((uintptr_t)fd.plane[0] | (uintptr_t)fd.plane[1] | (uintptr_t)fd.plane[2] |
-                       (uintptr_t)fd.stride) & (kVecAlign - 1)) == 0;
-    if (vec) {
+    const bool vec = kRgbVec && (((uintptr_t)fd.plane[0] | (uintptr_t)fd.plane[1] | (uintptr_t)fd.plane[2] |
+                                  (uintptr_t)fd.stride) & (kVecAlign - 1)) == 0;
+    if (IT == IN_YUV || vec) {
         const Ssimu2Level L = g.lv[0];
         const int ly = threadIdx.x >> 3, lx = 4 * (threadIdx.x & 7);
         const int gx = bx * 32 + lx, gy = by * 32 + ly;
         float v[3][4] = {};
         if (gy < L.h && gx < L.w) {
-            if (gx + 3 < L.w) {
+            if (IT == IN_YUV) {
+                yuv_rgb4(fd, yp, gx, gy, L.w, L.h, v[0], v[1], v[2]);
+            } else if (gx + 3 < L.w) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
                     const uint8_t* row = fd.plane[c] + (int64_t)gy * fd.stride;
@@ -167,7 +169,10 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
 #pragma unroll
             for (int i = 0; i < 4; i++) {
 #pragma unroll
-                for (int c = 0; c < 3; c++) v[c][i] = gx + i < L.w ? to_linear_fast(v[c][i]) : 0.f;
+                for (int c = 0; c < 3; c++) {
+                    const float lin = (IT == IN_YUV && yp.linear_out) ? v[c][i] : to_linear_fast(v[c][i]);
+                    v[c][i] = gx + i < L.w ? lin : 0.f;  // frames converted to linear light skip x^2.4
+                }
                 float X = v[0][i], Y = v[1][i], B = v[2][i];
                 positive_xyb(X, Y, B);
                 o[0][i] = X;
@@ -175,14 +180,14 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
                 o[2][i] = B;
             }
             const int64_t e = L.off + (int64_t)gy * L.pitch + gx;
-            if (gx + 3 < L.w) {
+            if (!DELTA && gx + 3 < L.w) {
 #pragma unroll
                 for (int c = 0; c < 3; c++)
                     *reinterpret_cast<float4*>(out.f32 + c * pe + e) = make_float4(o[c][0], o[c][1], o[c][2], o[c][3]);
             } else {
 #pragma unroll
                 for (int i = 0; i < 4; i++)
-                    if (gx + i < L.w) pyr_store<false>(out, pe, e + i, o[0][i], o[1][i], o[2][i]);
+                    if (gx + i < L.w) pyr_store<DELTA>(out, pe, e + i, o[0][i], o[1][i], o[2][i]);
             }
         }
 #pragma unroll
@@ -255,7 +260,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
 
 // grid (tiles_x0, tiles_y0, 2*npairs)
 template <int IT>
-__global__ void __launch_bounds__(256, 8) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
+__global__ void __launch_bounds__(256, IT == IN_YUV ? 4 : 8) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
                                                              float* __restrict__ pyr, Ssimu2Geom g, YuvParams yp) {
     const int img = blockIdx.z;  // pair*2 + image
     const FrameDesc fd = frames[img];
@@ -629,7 +634,7 @@ __global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __res
 // Work-list kernels of the batched multi-resolution form (Ssimu2MultiEngine).
 // one 32x32 level-0 tile per CTA: items {image, tile x, tile y, unused}
 template <int IT, bool DELTA>
-__global__ void __launch_bounds__(256, 8) ssimu2_multi_pyramid_kernel(const Ssimu2MultiImage* __restrict__ imgs,
+__global__ void __launch_bounds__(256, IT == IN_YUV ? 4 : 8) ssimu2_multi_pyramid_kernel(const Ssimu2MultiImage* __restrict__ imgs,
                                                                    const int4* __restrict__ items,
                                                                    const Ssimu2Geom* __restrict__ geoms) {
     const int4 it = items[blockIdx.x];
