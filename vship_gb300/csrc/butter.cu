@@ -152,22 +152,51 @@ __global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __r
     const int img = blockIdx.z;
     const FrameDesc fd = frames[img];
     const BScaleDev F = g.s[0], Hs = g.s[1];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-#pragma unroll
-    for (int r = 0; r < 4; r++) {
-        const int ly = ty + 8 * r;
-        const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ly;
-        float v[3] = {0.f, 0.f, 0.f};
+    const bool vec = rgb4_vectorizable<IT>(fd);
+    if (IT == IN_YUV || vec) {
+        // four adjacent pixels of one row per thread (load_rgb4), stored as one float4 per plane
+        const int ly = threadIdx.x >> 3, lx = 4 * (threadIdx.x & 7);
+        const int gx = blockIdx.x * 32 + lx, gy = blockIdx.y * 32 + ly;
+        float v[3][4] = {};
         if (gx < F.w && gy < F.h) {
-            load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, v[0], v[1], v[2]);
+            load_rgb4<IT>(fd, yp, gx, gy, F.w, F.h, vec, v);
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                if (!(IT == IN_YUV && yp.linear_out)) v[c] = to_linear_fast(v[c]);
-                iplane(ib, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+                    if (!(IT == IN_YUV && yp.linear_out)) v[c][i] = gx + i < F.w ? to_linear_fast(v[c][i]) : 0.f;
+                float* d = iplane(ib, g, F, img, I_LIN + c) + (int64_t)gy * F.p + gx;
+                if (gx + 3 < F.w) {
+                    *reinterpret_cast<float4*>(d) = make_float4(v[c][0], v[c][1], v[c][2], v[c][3]);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+                        if (gx + i < F.w) d[i] = v[c][i];
+                }
             }
         }
 #pragma unroll
-        for (int c = 0; c < 3; c++) sm[c][ly][tx] = v[c];
+        for (int c = 0; c < 3; c++)
+#pragma unroll
+            for (int i = 0; i < 4; i++) sm[c][ly][lx + i] = v[c][i];
+    } else {
+        const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int ly = ty + 8 * r;
+            const int gx = blockIdx.x * 32 + tx, gy = blockIdx.y * 32 + ly;
+            float v[3] = {0.f, 0.f, 0.f};
+            if (gx < F.w && gy < F.h) {
+                load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, v[0], v[1], v[2]);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    if (!(IT == IN_YUV && yp.linear_out)) v[c] = to_linear_fast(v[c]);
+                    iplane(ib, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; c++) sm[c][ly][tx] = v[c];
+        }
     }
     __syncthreads();
     const int lx = threadIdx.x & 15, ly = threadIdx.x >> 4;

@@ -130,41 +130,14 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
     // allow it load them with one vector load per plane (8 bytes of uint16, 16 of float), Y'CbCr
     // loads each chroma sample once for the four (yuv_rgb4); FP32 pyramids store the 4 outputs
     // per channel as one float4 (level rows are 16-byte aligned, columns a multiple of 4).
-    constexpr bool kRgbVec = IT == IN_UINT16 || IT == IN_FLOAT;
-    constexpr unsigned kVecAlign = IT == IN_FLOAT ? 16u : 8u;
-    const bool vec = kRgbVec && (((uintptr_t)fd.plane[0] | (uintptr_t)fd.plane[1] | (uintptr_t)fd.plane[2] |
-                                  (uintptr_t)fd.stride) & (kVecAlign - 1)) == 0;
+    const bool vec = rgb4_vectorizable<IT>(fd);
     if (IT == IN_YUV || vec) {
         const Ssimu2Level L = g.lv[0];
         const int ly = threadIdx.x >> 3, lx = 4 * (threadIdx.x & 7);
         const int gx = bx * 32 + lx, gy = by * 32 + ly;
         float v[3][4] = {};
         if (gy < L.h && gx < L.w) {
-            if (IT == IN_YUV) {
-                yuv_rgb4(fd, yp, gx, gy, L.w, L.h, v[0], v[1], v[2]);
-            } else if (gx + 3 < L.w) {
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    const uint8_t* row = fd.plane[c] + (int64_t)gy * fd.stride;
-                    if (IT == IN_UINT16) {
-                        const uint2 q = __ldg(reinterpret_cast<const uint2*>(row + 2 * (int64_t)gx));
-                        v[c][0] = div_by<65535>((float)(q.x & 0xffffu));
-                        v[c][1] = div_by<65535>((float)(q.x >> 16));
-                        v[c][2] = div_by<65535>((float)(q.y & 0xffffu));
-                        v[c][3] = div_by<65535>((float)(q.y >> 16));
-                    } else {
-                        const float4 q = __ldg(reinterpret_cast<const float4*>(row + 4 * (int64_t)gx));
-                        v[c][0] = q.x;
-                        v[c][1] = q.y;
-                        v[c][2] = q.z;
-                        v[c][3] = q.w;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-                    if (gx + i < L.w) load_rgb<IT>(fd, yp, gx + i, gy, L.w, L.h, v[0][i], v[1][i], v[2][i]);
-            }
+            load_rgb4<IT>(fd, yp, gx, gy, L.w, L.h, vec, v);
             float o[3][4];
 #pragma unroll
             for (int i = 0; i < 4; i++) {
