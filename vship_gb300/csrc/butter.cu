@@ -231,7 +231,7 @@ constexpr int TB_HPL = TB_IH * TB_HP;
 
 __device__ __forceinline__ void tile_stage_r8(float* dst, const float* __restrict__ plane, int pitch, int w, int h,
                                               int x0, int y0) {
-    stage_rows<256>(dst, TB_IP, plane, pitch, w, h, x0 - TB_R, y0 - TB_R, TB_IH, TB_IW / 4);
+    stage_tile_t<TB_IH, TB_IW / 4>(dst, TB_IP, plane, pitch, w, h, x0 - TB_R, y0 - TB_R);
 }
 
 template <int KI>
@@ -400,12 +400,12 @@ __global__ void __launch_bounds__(256, 3) butter_hblur_kernel(float* const* __re
     const int col0 = (warp & 3) * 32 + 8 * (lane & 3);
     float rx[8];
     b_inv_mass_run<KI, R, 8>(x0 + col0, S.w, rx);
-    stage_rows<256>(in[0], HB_P, src, S.p, S.w, S.h, x0 - RA, yt0, HB_TH, IW / 4);
+    stage_tile_t<HB_TH, IW / 4>(in[0], HB_P, src, S.p, S.w, S.h, x0 - RA, yt0);
     cp_async_commit();
 #pragma unroll 1
     for (int t = 0; t < nt; t++) {
         if (t + 1 < nt) {
-            stage_rows<256>(in[(t + 1) & 1], HB_P, src, S.p, S.w, S.h, x0 - RA, yt0 + (t + 1) * HB_TH, HB_TH, IW / 4);
+            stage_tile_t<HB_TH, IW / 4>(in[(t + 1) & 1], HB_P, src, S.p, S.w, S.h, x0 - RA, yt0 + (t + 1) * HB_TH);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -455,12 +455,12 @@ __device__ __forceinline__ void vblur3(float* in, float* ctr, float* const* __re
     constexpr int IH = VB_TH + 2 * R;
 #pragma unroll
     for (int c = 0; c < 3; c++)
-        stage_rows<256>(in + c * IH * VB_TW, VB_TW, iplane(ib, g, S, img, src_id + c), S.p, S.w, S.h, x0, y0 - R,
-                        IH, VB_TW / 4);
+        stage_tile_t<IH, VB_TW / 4>(in + c * IH * VB_TW, VB_TW, iplane(ib, g, S, img, src_id + c), S.p, S.w, S.h, x0,
+                                    y0 - R);
     // the epilogue's own-pixel planes, staged with the blur input so their latency overlaps
     for (int c = 0; c < nctr; c++)
-        stage_rows<256>(ctr + c * VB_TH * VB_TW, VB_TW, iplane(ib, g, S, img, ctr_id + c), S.p, S.w, S.h, x0, y0,
-                        VB_TH, VB_TW / 4);
+        stage_tile_t<VB_TH, VB_TW / 4>(ctr + c * VB_TH * VB_TW, VB_TW, iplane(ib, g, S, img, ctr_id + c), S.p, S.w,
+                                       S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -758,11 +758,11 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
     auto plane_id = [](int m) { return (m < 2 ? I_UHF : m < 4 ? I_HF : I_MF) + 1 - (m & 1); };
     auto stage = [&](float* dst, int img, int id) {
         if (HB)
-            stage_rows_h<256>(reinterpret_cast<__half*>(dst), DFH_P, hplane(ib, S, img, id), S.p, S.w, S.h, x0 - 8,
-                              y0 - DF_H, DF_IH, 6);
+            stage_tile_t<DF_IH, 6>(reinterpret_cast<__half*>(dst), DFH_P, (const __half*)hplane(ib, S, img, id), S.p,
+                                   S.w, S.h, x0 - 8, y0 - DF_H);
         else
-            stage_rows<256>(dst, DF_IW, iplane(ib, g, S, img, id), S.p, S.w, S.h, x0 - DF_H, y0 - DF_H, DF_IH,
-                            DF_IW / 4);
+            stage_tile_t<DF_IH, DF_IW / 4>(dst, DF_IW, (const float*)iplane(ib, g, S, img, id), S.p, S.w, S.h,
+                                           x0 - DF_H, y0 - DF_H);
     };
     stage(sm, i0, plane_id(0));
     stage(sm + RAWF, i1, plane_id(0));
@@ -978,10 +978,10 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* const* __res
     const int i1 = pimg[pair].y;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * DM_TW, y0 = blockIdx.y * DM_TH;
-    // 1-D block of 256 (stage_rows distributes chunks over threadIdx.x)
+    // 1-D block of 256 (stage_tile_t distributes chunks over threadIdx.x)
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
     const float* b0 = iplane(ib, g, S, i1, Q_B0);
-    stage_rows<256>(bt, DM_IW, b0, S.p, S.w, S.h, x0 - DM_HX, y0 - DM_HY, DM_IH, DM_IW / 4);
+    stage_tile_t<DM_IH, DM_IW / 4>(bt, DM_IW, b0, S.p, S.w, S.h, x0 - DM_HX, y0 - DM_HY);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();

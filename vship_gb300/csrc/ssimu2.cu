@@ -277,44 +277,8 @@ __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     return 1.0f / (c_s2_I[end] - c_s2_I[beg]);
 }
 
-// Stage the 64x48 halo tile of one plane (row r = image row y0 - 8 + r): 768 16-byte chunks, 3
-// per thread. The tile's first column (tile x - 8) is a multiple of 4 floats and every row starts
-// 32-byte aligned, so each chunk is either fully outside the image, fully inside, or cut by the
-// right edge (partial source size, the rest zero-filled).
-__device__ __forceinline__ void stage_tile(float* dst, const float* __restrict__ plane, int pitch, int w, int h,
-                                           int x0, int y0) {
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        const int ch = threadIdx.x + 256 * k;  // 0..767
-        const int r = ch / 12, q = ch - r * 12;
-        const int gx = x0 - ST_R + 4 * q, gy = y0 - ST_R + r;
-        int bytes = 0;
-        const float* src = plane;
-        if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
-            bytes = min(w - gx, 4) * 4;
-            src = plane + (int64_t)gy * pitch + gx;
-        }
-        cp_async16(dst + r * ST_RP + 4 * q, src, bytes);
-    }
-}
-
 // FP16 delta tile: 64 rows x 48 halves, row pitch 56 halves (7 quads: conflict-free 16-byte reads)
 constexpr int ST_DP = 56;
-
-__device__ __forceinline__ void stage_tile_h(__half* dst, const __half* __restrict__ plane, int pitch, int w, int h,
-                                             int x0, int y0) {
-    for (int ch = threadIdx.x; ch < ST_IH * 6; ch += 256) {
-        const int r = ch / 6, q = ch - r * 6;
-        const int gx = x0 - ST_R + 8 * q, gy = y0 - ST_R + r;
-        int bytes = 0;
-        const __half* src = plane;
-        if (gy >= 0 && gy < h && gx >= 0 && gx < w) {
-            bytes = min(w - gx, 8) * 2;
-            src = plane + (int64_t)gy * pitch + gx;
-        }
-        cp_async16(reinterpret_cast<float*>(dst + r * ST_DP + 8 * q), reinterpret_cast<const float*>(src), bytes);
-    }
-}
 
 // One segment (32 columns x up to ST_SEG rows) of one scale: the four moments, the maps and 18
 // pooled sums written to out[pool * stride] (pool = map * 2 + norm, times 3 channels). im1 / im2
@@ -353,11 +317,12 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
 #pragma unroll 1
         for (int k = 0; k < nchunk; k++) {
             const int ty0 = sy0 + k * ST_TH;
-            stage_tile(r1, im1 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+            stage_tile_t<ST_IH, 12>(r1, ST_RP, im1 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0 - ST_R, ty0 - ST_R);
             if (DELTA)
-                stage_tile_h(reinterpret_cast<__half*>(r2), im2h + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+                stage_tile_t<ST_IH, 6>(reinterpret_cast<__half*>(r2), ST_DP, im2h + (int64_t)c * pe, L.pitch, L.w, L.h,
+                                       tx0 - ST_R, ty0 - ST_R);
             else
-                stage_tile(r2, im2 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0, ty0);
+                stage_tile_t<ST_IH, 12>(r2, ST_RP, im2 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0 - ST_R, ty0 - ST_R);
             cp_async_commit();
             cp_async_wait<0>();
             __syncthreads();
