@@ -1103,7 +1103,7 @@ def main():
     ap.add_argument("--butter-pairs", type=int, default=60)
     ap.add_argument("--butter-chunk", type=int, default=4)
     ap.add_argument("--e2e-threads", type=int, default=8)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--cpu-sample", type=int, default=4)
     ap.add_argument("--skip-butter", action="store_true")
     ap.add_argument("--skip-ssimu2", action="store_true")
