@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(256, 4) butter_opsin_kernel(float* const* __re
 constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180, HB_NT = 4;
 
 template <int KI, int R>
-__global__ void __launch_bounds__(256, 3) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s,
+__global__ void __launch_bounds__(256, R == 9 ? 6 : 3) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s,
                                                               int src_id, int dst_id) {
     __shared__ __align__(16) float in[2][HB_TH * HB_P];
     constexpr int RA = (R + 3) & ~3;
