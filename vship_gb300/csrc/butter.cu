@@ -732,10 +732,10 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 // With half-band storage the raw tiles are FP16 rows of DFH_P halves staged from x0 - 8 (16-byte
 // chunks of 8 halves), and the window's column c sits at half c + 4 of its row.
 constexpr int DF_RAW = DF_IH * DF_IW;
-constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW) * 4;
+constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW + 8 * 256) * 4;
 constexpr int DFH_P = 56;                   // 48 staged halves + 8 of padding (7 quads per row)
 constexpr int DFH_RAWF = DF_IH * DFH_P / 2;  // one FP16 raw tile, in floats
-constexpr int kDiffSmemH = (4 * DFH_RAWF + DF_RAW) * 4;
+constexpr int kDiffSmemH = (4 * DFH_RAWF + DF_RAW + 8 * 256) * 4;
 
 template <bool HB>
 __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
@@ -748,13 +748,14 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * DF_TW, y0 = blockIdx.y * DF_TH;
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    float acX[8], acY[8];
+    float* accY = Dt + DF_RAW;  // [8][256]: the Y maps' sums while the X maps run
+    float ac[8];
 #pragma unroll
-    for (int o = 0; o < 8; o++) {
-        acX[o] = 0.f;
-        acY[o] = 0.f;
-    }
-    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X
+    for (int o = 0; o < 8; o++) ac[o] = 0.f;
+    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X. Each channel's
+    // three maps are summed in that order, so the Y maps run first (m = 0, 2, 4) and the X maps
+    // after (1, 3, 5): the same sums, with one channel's accumulators live at a time.
+    auto map_of = [](int t) { return t < 3 ? 2 * t : 2 * (t - 3) + 1; };
     auto plane_id = [](int m) { return (m < 2 ? I_UHF : m < 4 ? I_HF : I_MF) + 1 - (m & 1); };
     auto stage = [&](float* dst, int img, int id) {
         if (HB)
@@ -768,12 +769,13 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
     stage(sm + RAWF, i1, plane_id(0));
     cp_async_commit();
 #pragma unroll 1
-    for (int m = 0; m < 6; m++) {
-        const float* r0 = sm + (m & 1) * 2 * RAWF;
+    for (int t = 0; t < 6; t++) {
+        const int m = map_of(t);
+        const float* r0 = sm + (t & 1) * 2 * RAWF;
         const float* r1 = r0 + RAWF;
-        if (m < 5) {
-            float* n0 = sm + ((m + 1) & 1) * 2 * RAWF;
-            const int id = plane_id(m + 1);
+        if (t < 5) {
+            float* n0 = sm + ((t + 1) & 1) * 2 * RAWF;
+            const int id = plane_id(map_of(t + 1));
             stage(n0, i0, id);
             stage(n0 + RAWF, i1, id);
             cp_async_commit();
@@ -808,12 +810,14 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         float res[8];
         if (m < 2) malta_column<true>(Dt, 8 * vg, vc, res);
         else malta_column<false>(Dt, 8 * vg, vc, res);
-        if (m & 1) {
 #pragma unroll
-            for (int o = 0; o < 8; o++) acX[o] += res[o];
-        } else {
+        for (int o = 0; o < 8; o++) ac[o] += res[o];
+        if (t == 2) {
 #pragma unroll
-            for (int o = 0; o < 8; o++) acY[o] += res[o];
+            for (int o = 0; o < 8; o++) {
+                accY[o * 256 + threadIdx.x] = ac[o];
+                ac[o] = 0.f;
+            }
         }
     }
     const int x = x0 + vc;
@@ -828,7 +832,7 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         const int y = y0 + 8 * vg + o;
         if (y < S.h) {
             const int64_t i = (int64_t)y * S.p + x;
-            float ac[3] = {acX[o], acY[o], 0.f};
+            float acc[3] = {ac[o], accY[o * 256 + threadIdx.x], 0.f};
             float dc[3] = {0.f, 0.f, 0.f};
             float hf[2][2], uhf[2][2], mf[2][3], lf[2][3];
 #pragma unroll
@@ -850,24 +854,24 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
                 if (c < 2) {  // L2AsymDiff (simplerdiff.hpp:263-293)
                     const float s1 = hf[0][c], s2 = hf[1][c];
                     const float diff = s1 - s2;
-                    ac[c] += P.l2asym_gt[c] * diff * diff;
+                    acc[c] += P.l2asym_gt[c] * diff * diff;
                     const float fabs0 = fabsf(s1);
                     const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
                     const float wl = P.l2asym_lt[c];
                     if (s1 < 0) {
-                        if (s2 > -too_small) { const float v = s2 + too_small; ac[c] += wl * v * v; }
-                        else if (s2 < -too_big) { const float v = -s2 - too_big; ac[c] += wl * v * v; }
+                        if (s2 > -too_small) { const float v = s2 + too_small; acc[c] += wl * v * v; }
+                        else if (s2 < -too_big) { const float v = -s2 - too_big; acc[c] += wl * v * v; }
                     } else {
-                        if (s2 < too_small) { const float v = too_small - s2; ac[c] += wl * v * v; }
-                        else if (s2 > too_big) { const float v = s2 - too_big; ac[c] += wl * v * v; }
+                        if (s2 < too_small) { const float v = too_small - s2; acc[c] += wl * v * v; }
+                        else if (s2 > too_big) { const float v = s2 - too_big; acc[c] += wl * v * v; }
                     }
                 }
                 const float dm = mf[0][c] - mf[1][c];
-                ac[c] += P.wmf[c] * dm * dm;
+                acc[c] += P.wmf[c] * dm * dm;
                 const float dl = lf[0][c] - lf[1][c];
                 dc[c] += P.wlf[c] * dl * dl;
             }
-            iplane(ib, g, S, i1, Q_SAC)[i] = ac[0] + ac[1] + ac[2];
+            iplane(ib, g, S, i1, Q_SAC)[i] = acc[0] + acc[1] + acc[2];
             iplane(ib, g, S, i1, Q_SDC)[i] = dc[0] + dc[1] + dc[2];
             // maskinit + diffPrecompute (maskPsycho.hpp:3-40). sqrt(m + b) - sqrt(b) is evaluated
             // as m / (sqrt(m + b) + sqrt(b)): the same value without the cancellation.
