@@ -639,7 +639,7 @@ __constant__ DiffParams c_dp;
 __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) {
     const float absval = 0.5f * fabsf(a) + 0.5f * fabsf(b);
     const float diff = a - b;
-    const float inv = __frcp_rn(m.norm1 + absval);  // one reciprocal for both scalers
+    const float inv = rcp_nr(m.norm1 + absval);  // one reciprocal for both scalers (norm1 >= 5)
     const float scaler = m.n2gt * inv;
     float v = scaler * diff;
     const float scaler2 = m.n2lt * inv;
