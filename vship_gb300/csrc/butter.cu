@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restri
             const int ci = (8 * vg + o) * VB_TW + vc;
             float hx = ctr[ci] - mf[0][o];
             const float hy = ctr[VB_TH * VB_TW + ci] - mf[1][o];
-            hx *= sx + (yw * (1.0f - sx)) / (yw + hy * hy);
+            hx *= sx + div_nr(yw * (1.0f - sx), yw + hy * hy);
             d0[i] = hx;
             d1[i] = hy;
             band_store<HB>(ib, g, S, img, I_MF + 0, i, remove_range(mf[0][o], 0.29f));
@@ -880,7 +880,7 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
                 const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
                 const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
                 const float mk = mul * sqrtf(xd * xd + yd * yd);
-                iplane(ib, g, S, i1, Q_PRE0 + m)[i] = mk / (sqrtf(mk + bias) + sqb);
+                iplane(ib, g, S, i1, Q_PRE0 + m)[i] = div_nr(mk, sqrtf(mk + bias) + sqb);
             }
         }
     }
@@ -923,12 +923,6 @@ __global__ void __launch_bounds__(256, 4) butter_mask_blur_kernel(float* const* 
     }
 }
 
-// One reciprocal and a residual correction (Markstein): num / den to within rounding.
-__device__ __forceinline__ float div_fast(float num, float den) {
-    const float r = __frcp_rn(den);
-    const float q = num * r;
-    return fmaf(fmaf(-q, den, num), r, q);
-}
 
 // combineMasks.hpp:3-19
 __device__ __forceinline__ float mask_common(float c) {
@@ -943,10 +937,10 @@ __device__ __forceinline__ float mask_common(float c) {
     return r * r;
 }
 __device__ __forceinline__ float mask_y(float delta) {
-    return mask_common(div_fast(2.5485944793f, (0.451936922203f * delta) + 0.829591754942f));
+    return mask_common(div_nr(2.5485944793f, (0.451936922203f * delta) + 0.829591754942f));
 }
 __device__ __forceinline__ float mask_dc_y(float delta) {
-    return mask_common(div_fast(0.505054525019f, (3.87449418804f * delta) + 0.20025578522f));
+    return mask_common(div_nr(0.505054525019f, (3.87449418804f * delta) + 0.20025578522f));
 }
 // maskPsycho.hpp:42-55
 __device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float& m2) {
