@@ -879,8 +879,8 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
             for (int m = 0; m < 2; m++) {
                 const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
                 const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
-                const float mk = mul * sqrtf(xd * xd + yd * yd);
-                iplane(ib, g, S, i1, Q_PRE0 + m)[i] = div_nr(mk, sqrtf(mk + bias) + sqb);
+                const float mk = mul * sqrt_nr(xd * xd + yd * yd);
+                iplane(ib, g, S, i1, Q_PRE0 + m)[i] = div_nr(mk, sqrt_nr(mk + bias) + sqb);
             }
         }
     }
@@ -1012,7 +1012,7 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* const* __res
             store_min3(c[R], m0, m1, m2);
             const float mask = 0.45f * m0 + 0.3f * m1 + 0.25f * m2;
             const int64_t i = (int64_t)y * S.p + x;
-            float d = sqrtf(mask_y(mask) * __ldg(sac + i) + mask_dc_y(mask) * __ldg(sdc + i));
+            float d = sqrt_nr(mask_y(mask) * __ldg(sac + i) + mask_dc_y(mask) * __ldg(sdc + i));
             if (!FINAL) {
                 iplane(ib, g, S, i1, Q_DIFF)[i] = d;
             } else {
