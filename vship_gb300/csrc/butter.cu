@@ -942,20 +942,15 @@ __device__ __forceinline__ float mask_y(float delta) {
 __device__ __forceinline__ float mask_dc_y(float delta) {
     return mask_common(div_nr(0.505054525019f, (3.87449418804f * delta) + 0.20025578522f));
 }
-// maskPsycho.hpp:42-55
+// maskPsycho.hpp:42-55: keep the three smallest values, m0 <= m1 <= m2. As min/max insertion
+// into the sorted triple: the same values as the reference's branches, ties included, and +inf
+// leaves the triple unchanged.
 __device__ __forceinline__ void store_min3(float v, float& m0, float& m1, float& m2) {
-    if (v < m2) {
-        if (v < m0) {
-            m2 = m1;
-            m1 = m0;
-            m0 = v;
-        } else if (v < m1) {
-            m2 = m1;
-            m1 = v;
-        } else {
-            m2 = v;
-        }
-    }
+    const float n2 = fminf(m2, fmaxf(m1, v));
+    const float n1 = fminf(m1, fmaxf(m0, v));
+    m0 = fminf(m0, v);
+    m1 = n1;
+    m2 = n2;
 }
 
 // Fuzzy erosion + diffmap; FINAL also folds in the half-scale map, stores the distortion map
