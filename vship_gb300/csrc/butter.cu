@@ -526,16 +526,9 @@ __device__ __forceinline__ float amplify_range(float x, float w) { return x > w 
 __device__ __forceinline__ float remove_range(float x, float w) { return x > w ? x - w : x < -w ? x + w : 0.0f; }
 __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
     const float kMul = 0.688059627878f;
-    if (v >= maxval) {
-        v -= maxval;
-        v *= kMul;
-        v += maxval;
-    } else if (v < -maxval) {
-        v += maxval;
-        v *= kMul;
-        v -= maxval;
-    }
-    return v;
+    const float hi = fmaf(v - maxval, kMul, maxval);   // v >= maxval
+    const float lo = fmaf(v + maxval, kMul, -maxval);  // v < -maxval
+    return v >= maxval ? hi : (v < -maxval ? lo : v);
 }
 
 // MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
@@ -858,13 +851,12 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
                     const float fabs0 = fabsf(s1);
                     const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
                     const float wl = P.l2asym_lt[c];
-                    if (s1 < 0) {
-                        if (s2 > -too_small) { const float v = s2 + too_small; acc[c] += wl * v * v; }
-                        else if (s2 < -too_big) { const float v = -s2 - too_big; acc[c] += wl * v * v; }
-                    } else {
-                        if (s2 < too_small) { const float v = too_small - s2; acc[c] += wl * v * v; }
-                        else if (s2 > too_big) { const float v = s2 - too_big; acc[c] += wl * v * v; }
-                    }
+                    // the two sign branches as one on s2 mirrored to s1's side (as in malta_pre):
+                    // s2 + too_small == too_small - (-s2) and -s2 - too_big are the same IEEE
+                    // operations; outside both ranges v = 0 adds exactly nothing
+                    const float s2m = s1 < 0 ? -s2 : s2;
+                    const float v = s2m < too_small ? too_small - s2m : (s2m > too_big ? s2m - too_big : 0.0f);
+                    acc[c] += wl * v * v;
                 }
                 const float dm = mf[0][c] - mf[1][c];
                 acc[c] += P.wmf[c] * dm * dm;
