@@ -233,7 +233,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
 
 // grid (tiles_x0, tiles_y0, 2*npairs)
 template <int IT>
-__global__ void __launch_bounds__(256, IT == IN_YUV ? 4 : 8) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
+__global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) ssimu2_pyramid_kernel(const FrameDesc* __restrict__ frames,
                                                              float* __restrict__ pyr, Ssimu2Geom g, YuvParams yp) {
     const int img = blockIdx.z;  // pair*2 + image
     const FrameDesc fd = frames[img];
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __res
 // Work-list kernels of the batched multi-resolution form (Ssimu2MultiEngine).
 // one 32x32 level-0 tile per CTA: items {image, tile x, tile y, unused}
 template <int IT, bool DELTA>
-__global__ void __launch_bounds__(256, IT == IN_YUV ? 4 : 8) ssimu2_multi_pyramid_kernel(const Ssimu2MultiImage* __restrict__ imgs,
+__global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) ssimu2_multi_pyramid_kernel(const Ssimu2MultiImage* __restrict__ imgs,
                                                                    const int4* __restrict__ items,
                                                                    const Ssimu2Geom* __restrict__ geoms) {
     const int4 it = items[blockIdx.x];
