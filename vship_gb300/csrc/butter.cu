@@ -146,7 +146,7 @@ __device__ __forceinline__ BScaleDev pick_scale(const BGeom& g, int s) { return 
 // Kernel: decode + linearise at full resolution + 2x2 box to half resolution.
 // grid (ceil(w/32), ceil(h/32), nimages), 256 threads; frames[image].
 template <int IT>
-__global__ void __launch_bounds__(256) butter_decode_kernel(const FrameDesc* __restrict__ frames,
+__global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) butter_decode_kernel(const FrameDesc* __restrict__ frames,
                                                             float* const* __restrict__ ib, BGeom g, YuvParams yp) {
     __shared__ float sm[3][32][33];
     const int img = blockIdx.z;
