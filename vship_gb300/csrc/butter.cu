@@ -647,8 +647,12 @@ __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) 
     return diff < 0.0f ? v - impact : v + impact;
 }
 
-// The 16 line patterns, as (dx, dy) taps in summation order (maltaDiff.hpp:4-512, after google
-// butteraugli). W(dx,dy) reads the register window at output row o.
+// The 16 line patterns, as (dx, dy) taps in the reference's order (maltaDiff.hpp:4-512, after
+// google butteraugli). W(dx,dy) reads the register window at output row o. In the 5-tap bodies,
+// parentheses group the centre triples that three patterns share, so each is formed once per
+// output (14 of the 64 additions; the sums differ from the reference's left-to-right FP32 order
+// by rounding only). The 9-tap bodies keep the reference's order: grouping their shared runs
+// too holds more partial sums live than the 80 registers allow and measured slower.
 #define W(dx, dy) win[(o) + 4 + (dy)][4 + (dx)]
 #define SQ(expr)          \
     {                     \
@@ -672,23 +676,23 @@ __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) 
     SQ(W(-4, -2) + W(-3, -2) + W(-2, -1) + W(-1, -1) + W(0, 0) + W(1, 0) + W(2, 1) + W(3, 1))              \
     SQ(W(-2, -4) + W(-2, -3) + W(-1, -2) + W(-1, -1) + W(0, 0) + W(0, 1) + W(1, 2) + W(1, 3))              \
     SQ(W(2, -4) + W(2, -3) + W(1, -2) + W(1, -1) + W(0, 0) + W(0, 1) + W(-1, 2) + W(-1, 3))
-#define MALTA_LF_BODY                                           \
-    SQ(W(-4, 0) + W(-2, 0) + W(0, 0) + W(2, 0) + W(4, 0))       \
-    SQ(W(0, -4) + W(0, -2) + W(0, 0) + W(0, 2) + W(0, 4))       \
-    SQ(W(-3, -3) + W(-2, -2) + W(0, 0) + W(2, 2) + W(3, 3))     \
-    SQ(W(3, -3) + W(2, -2) + W(0, 0) + W(-2, 2) + W(-3, 3))     \
-    SQ(W(1, -4) + W(1, -2) + W(0, 0) + W(-1, 2) + W(-1, 4))     \
-    SQ(W(-1, -4) + W(-1, -2) + W(0, 0) + W(1, 2) + W(1, 4))     \
-    SQ(W(-4, -1) + W(-2, -1) + W(0, 0) + W(2, 1) + W(4, 1))     \
-    SQ(W(-4, 1) + W(-2, 1) + W(0, 0) + W(2, -1) + W(4, -1))     \
-    SQ(W(-2, -3) + W(-1, -2) + W(0, 0) + W(1, 2) + W(2, 3))     \
-    SQ(W(2, -3) + W(1, -2) + W(0, 0) + W(-1, 2) + W(-2, 3))     \
-    SQ(W(-3, -2) + W(-2, -1) + W(0, 0) + W(2, 1) + W(3, 2))     \
-    SQ(W(3, -2) + W(2, -1) + W(0, 0) + W(-2, 1) + W(-3, 2))     \
-    SQ(W(-4, 2) + W(-2, 1) + W(0, 0) + W(2, -1) + W(4, -2))     \
-    SQ(W(-4, -2) + W(-2, -1) + W(0, 0) + W(2, 1) + W(4, 2))     \
-    SQ(W(-2, -4) + W(-1, -2) + W(0, 0) + W(1, 2) + W(2, 4))     \
-    SQ(W(2, -4) + W(1, -2) + W(0, 0) + W(-1, 2) + W(-2, 4))
+#define MALTA_LF_BODY                                         \
+    SQ(W(-4, 0) + W(-2, 0) + W(0, 0) + W(2, 0) + W(4, 0))     \
+    SQ(W(0, -4) + W(0, -2) + W(0, 0) + W(0, 2) + W(0, 4))     \
+    SQ(W(-3, -3) + W(-2, -2) + W(0, 0) + W(2, 2) + W(3, 3))   \
+    SQ(W(3, -3) + W(2, -2) + W(0, 0) + W(-2, 2) + W(-3, 3))   \
+    SQ(W(1, -4) + (W(1, -2) + W(0, 0) + W(-1, 2)) + W(-1, 4)) \
+    SQ(W(-1, -4) + (W(-1, -2) + W(0, 0) + W(1, 2)) + W(1, 4)) \
+    SQ(W(-4, -1) + (W(-2, -1) + W(0, 0) + W(2, 1)) + W(4, 1)) \
+    SQ(W(-4, 1) + (W(-2, 1) + W(0, 0) + W(2, -1)) + W(4, -1)) \
+    SQ(W(-2, -3) + (W(-1, -2) + W(0, 0) + W(1, 2)) + W(2, 3)) \
+    SQ(W(2, -3) + (W(1, -2) + W(0, 0) + W(-1, 2)) + W(-2, 3)) \
+    SQ(W(-3, -2) + (W(-2, -1) + W(0, 0) + W(2, 1)) + W(3, 2)) \
+    SQ(W(3, -2) + W(2, -1) + W(0, 0) + W(-2, 1) + W(-3, 2))   \
+    SQ(W(-4, 2) + (W(-2, 1) + W(0, 0) + W(2, -1)) + W(4, -2)) \
+    SQ(W(-4, -2) + (W(-2, -1) + W(0, 0) + W(2, 1)) + W(4, 2)) \
+    SQ(W(-2, -4) + (W(-1, -2) + W(0, 0) + W(1, 2)) + W(2, 4)) \
+    SQ(W(2, -4) + (W(1, -2) + W(0, 0) + W(-1, 2)) + W(-2, 4))
 
 constexpr int DF_TW = 32, DF_TH = 64, DF_H = 4;
 constexpr int DF_IW = DF_TW + 2 * DF_H, DF_IH = DF_TH + 2 * DF_H;  // 40 x 72
