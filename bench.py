@@ -126,14 +126,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM bytes per frame pair (read + write, both scales for Butteraugli) measured by ncu on the
+# bench's own launch shapes (profiles/dram_traffic_bench_config.md): ssimu2_stats reads each
+# pyramid once (66.38 MB per 1080p pair, equal to its algorithmic bytes); butter_diff at the
+# 4-pair 3840x2160 batch reads its band planes about 1.18x (tile halos, epilogue re-reads).
+NCU_DRAM_BYTES_PER_PAIR = {
+    "ssimu2_stats": 66.39e6,
+    "butter_diff": (785.9e6 + 146.6e6 + 3146.3e6 + 613.7e6) / 4,
+}
+
+
 def ncu_traffic(kernel: str):
-    """DRAM bytes per launch for `kernel` from the committed ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
-    if not os.path.exists(p):
-        return None
-    with open(p) as f:
-        d = json.load(f)
-    return d.get(kernel)
+    """DRAM bytes per pair for `kernel` from the committed ncu measurement, if one exists."""
+    return NCU_DRAM_BYTES_PER_PAIR.get(kernel)
 
 
 class ClockSampler:
