@@ -193,14 +193,15 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
     __syncthreads();
     float* cur = smA;
     float* nxt = smB;
-    // levels 1..5: the tile side halves each level (16, 8, 4, 2, 1), so indices are shifts
-#pragma unroll
-    for (int k = 1; k < 6; k++) {
+    // levels 1..5: the tile side halves each level (16, 8, 4, 2, 1), so indices are shifts.
+    // Level 1 (256 samples) takes every thread; levels 2..5 (85 samples) are warp 0's alone,
+    // ordered by warp barriers, so the other seven warps leave and free their slots.
+    auto level = [&](int k, int nthreads) {
         const int cside = 32 >> (k - 1), nside = 32 >> k, lg = 5 - k;
         const Ssimu2Level L = g.lv[k], P = g.lv[k - 1];
         const int ox = bx * nside, oy = by * nside;
         const int pox = bx * cside, poy = by * cside;
-        for (int i = threadIdx.x; i < nside * nside; i += 256) {
+        for (int i = threadIdx.x; i < nside * nside; i += nthreads) {
             const int lx = i & (nside - 1), ly = i >> lg;
             const int gx = ox + lx, gy = oy + ly;
             float v[3] = {0.f, 0.f, 0.f};
@@ -224,10 +225,18 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
 #pragma unroll
             for (int c = 0; c < 3; c++) nxt[c * nside * (nside + 1) + ly * (nside + 1) + lx] = v[c];
         }
-        __syncthreads();
         float* t = cur;
         cur = nxt;
         nxt = t;
+    };
+    level(1, 256);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int k = 2; k < 6; k++) {
+            level(k, 32);
+            __syncwarp();
+        }
     }
 }
 
