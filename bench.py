@@ -502,22 +502,14 @@ def bench_workload(v, kind, args, ws, rank):
         _, _, _, hres = run_device(v, kind, ref, dst, 1, 1, ws, chunk, half_bands=True)
     fe2e_sec, fh2d, d2h, _ = run_e2e(v, kind, ref, dst, args.e2e_steps, 1, args.e2e_threads)
     fe2e_sec = max_over_ranks(fe2e_sec, ws)
-    cpu_res = None
+    # the CPU leg runs after every GPU measurement (an all-core run before them measurably slowed
+    # the host side of the e2e calls); keep the frames it needs on the host
+    ns = nx = 0
     if rank == 0 and args.cpu_sample > 0:
         ns = args.cpu_sample if kind == "ssimu2" else max(1, args.cpu_sample // 4)
         nx = args.error_pairs if kind != "ssimu2" else 0
-        cv, csec, exact = cpu_baseline(kind, ref, dst, ns, os.cpu_count() or 1, fp64_pairs=nx)
-        cpu_res = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
-                   "sample": f"{ns} pairs of the same workload ({csec:.1f} s)"}
-        if exact:
-            # max over the checked pairs of the relative error of {Qnorm, 3-norm, inf-norm}
-            def worst(res):
-                r = res.numpy().reshape(-1, 3)
-                return [max(e) for e in zip(*[rel_err(r[t], exact[t]) for t in range(len(exact))])]
-            cpu_res["error_vs_fp64"] = {"pairs": len(exact), "input": "float32 R'G'B'",
-                                        "fp32_planes": worst(fres)}
-            if hres is not None:
-                cpu_res["error_vs_fp64"]["fp16_bands"] = worst(hres)
+    ncpu = max(ns, nx)
+    ref_cpu, dst_cpu = ref[:ncpu].cpu(), dst[:ncpu].cpu()
     # 16-bit R'G'B' (headline)
     ref16, dst16 = to_rgb48(ref), to_rgb48(dst)
     del ref, dst
@@ -610,7 +602,19 @@ def bench_workload(v, kind, args, ws, rank):
     }
     if half:
         res["fp16_bands"] = half
-    if cpu_res:
+    if ns > 0:
+        cv, csec, exact = cpu_baseline(kind, ref_cpu, dst_cpu, ns, os.cpu_count() or 1, fp64_pairs=nx)
+        cpu_res = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+                   "sample": f"{ns} pairs of the same workload ({csec:.1f} s)"}
+        if exact:
+            # max over the checked pairs of the relative error of {Qnorm, 3-norm, inf-norm}
+            def worst(r_):
+                r = r_.numpy().reshape(-1, 3)
+                return [max(e) for e in zip(*[rel_err(r[t], exact[t]) for t in range(len(exact))])]
+            cpu_res["error_vs_fp64"] = {"pairs": len(exact), "input": "float32 R'G'B'",
+                                        "fp32_planes": worst(fres)}
+            if hres is not None:
+                cpu_res["error_vs_fp64"]["fp16_bands"] = worst(hres)
         res["cpu_baseline"] = cpu_res
     torch.cuda.empty_cache()
     return res
