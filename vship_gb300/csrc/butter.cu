@@ -36,6 +36,7 @@ namespace vship {
 // radius {8, 8, 8, 9, 21}.
 __constant__ float c_bk[5][43];
 __constant__ float c_bI[5][44];
+__constant__ float c_bInvIn[5];  // 1 / (full window mass): the renormalisation of interior outputs
 
 static int upload_butter_tables() {
     static const double sig[5] = {1.2, 1.56416327805, 2.7, 3.22489901262, 7.15593339443};
@@ -55,6 +56,12 @@ static int upload_butter_tables() {
     }
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bk, k, sizeof(k)));
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bI, I, sizeof(I)));
+    float inv[5];
+    for (int t = 0; t < 5; t++) {
+        const int n = 2 * std::max((int)(sig[t] * 3), 8) + 1;
+        inv[t] = 1.0f / (I[t][n] - I[t][0]);  // the same float division b_inv_mass makes
+    }
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bInvIn, inv, sizeof(inv)));
     return E_OK;
 }
 
@@ -65,11 +72,11 @@ __device__ __forceinline__ float b_inv_mass(int pos, int extent) {
     return 1.0f / (c_bI[KI][end] - c_bI[KI][beg]);
 }
 // The same for n consecutive positions p0 .. p0+n-1: positions whose whole window lies inside
-// the extent share the interior value (beg = 0, end = 2R + 1), computed once.
+// the extent share the interior value (beg = 0, end = 2R + 1), divided once on the host.
 template <int KI, int R, int N>
 __device__ __forceinline__ void b_inv_mass_run(int p0, int extent, float out[N]) {
     if (p0 >= R && p0 + N - 1 + R < extent) {
-        const float v = 1.0f / (c_bI[KI][2 * R + 1] - c_bI[KI][0]);
+        const float v = c_bInvIn[KI];
 #pragma unroll
         for (int o = 0; o < N; o++) out[o] = v;
     } else {
@@ -278,7 +285,8 @@ __device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const f
 template <int KI>
 __device__ __forceinline__ void tile_masses_r8(int x0, int y0, int w, int h, float rxy[6]) {
     const int tid = threadIdx.x;
-    const float rx = b_inv_mass<KI, 8>(x0 + (tid & 31), w);
+    const int x = x0 + (tid & 31);
+    const float rx = (x >= 8 && x + 8 < w) ? c_bInvIn[KI] : b_inv_mass<KI, 8>(x, w);
     float ry[6];
     b_inv_mass_run<KI, 8, 6>(y0 + 6 * (tid >> 5), h, ry);
 #pragma unroll
