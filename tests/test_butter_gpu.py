@@ -133,3 +133,19 @@ def test_init_rejects_bad_sizes(vlib):
     for w, hh in [(0, 10), (10, 0), (-4, 8)]:
         assert L.Vship_ButteraugliInitv2(ctypes.byref(h), w, hh, 2, ctypes.c_float(203.0)) == vlib.BadPointer
         assert L.Vship_SSIMU2Init(ctypes.byref(h), w, hh) == vlib.BadPointer
+
+
+def test_near_identical_frames_stay_finite(vlib, orc):
+    # differences of one float ulp around mid-grey: the band differences and the arguments of the
+    # diff kernel's square roots get tiny; the norms must stay finite and match the oracle
+    rs = np.random.default_rng(5)
+    a = [np.full((96, 128), 0.5, np.float32) + rs.uniform(-0.1, 0.1, (96, 128)).astype(np.float32)
+         for _ in range(3)]
+    b = [np.nextafter(p, np.float32(2.0)) if c == 1 else p.copy() for c, p in enumerate(a)]
+    with vlib.ButteraugliHandler(128, 96) as hd:
+        got, dm = hd.compute(a, b, distmap=True)
+    assert all(np.isfinite(x) for x in got) and np.isfinite(dm).all()
+    # the norms are ~1e-5 here, where FP32 rounding alone (the FP32 oracle) moves them 2-6x: an
+    # absolute bound, far below any visible distortion
+    want = orc.butteraugli(a, b, precision=64)
+    assert all(abs(g - w) <= 1e-4 for g, w in zip(got, want)), (got, want)
