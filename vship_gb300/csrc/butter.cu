@@ -892,7 +892,7 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
 
 // Blur both mask planes (sigma 2.7); store B0 and add 10*(B0-B1)^2 to the AC sum.
 // grid (ceil(w/32), ceil(h/48), npairs)
-__global__ void __launch_bounds__(256, 5) butter_mask_blur_kernel(float* const* __restrict__ ib,
+__global__ void __launch_bounds__(256, 6) butter_mask_blur_kernel(float* const* __restrict__ ib,
                                                                   const int2* __restrict__ pimg, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
