@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restri
 
 // HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), nimages)
 template <bool HB>
-__global__ void __launch_bounds__(256, 3) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
+__global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
     const int img = blockIdx.z;
