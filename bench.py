@@ -875,7 +875,7 @@ def run_serving(v, stream, pool_frames, res_index, admission, cache):
     """Drive the serving runtime with the stream; returns (latencies s, wall s, stats)."""
     import numpy as np
     srv = v.Server([pool_frames["size"]], v.IN_YUV420P10, admission_bytes=admission, cache_bytes=cache,
-                   max_batch_pairs=256)
+                   max_batch_pairs=32)
     done = {}
     stop = threading.Event()
 

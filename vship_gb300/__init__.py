@@ -580,7 +580,7 @@ class Server:
     referenced here until their completion is polled)."""
 
     def __init__(self, resolutions, input_type=4, admission_bytes=64 << 30, cache_bytes=16 << 30,
-                 max_batch_pairs=256, flags=0, qnorm=2, intensity_multiplier=203.0):
+                 max_batch_pairs=32, flags=0, qnorm=2, intensity_multiplier=203.0):
         self.resolutions = [(int(w), int(h)) for w, h in resolutions]
         h = Handler()
         self._live = {}
