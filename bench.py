@@ -126,13 +126,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# DRAM bytes per frame pair (read + write, both scales for Butteraugli) measured by ncu on the
-# bench's own launch shapes (profiles/dram_traffic_bench_config.md): ssimu2_stats reads each
-# pyramid once (66.38 MB per 1080p pair, equal to its algorithmic bytes); butter_diff at the
-# 4-pair 3840x2160 batch reads its band planes about 1.18x (tile halos, epilogue re-reads).
+# DRAM bytes per frame pair (read + write, both scales for Butteraugli) measured by ncu
+# (profiles/dram_traffic_bench_config.md): ssimu2_stats reads each pyramid once (66.38 MB per
+# 1080p pair, equal to its algorithmic bytes); butter_diff reads its band planes about 1.18x
+# (tile halos, epilogue re-reads) once a batch's planes exceed L2, as every batch of 4 or more
+# 3840x2160 pairs does.
 NCU_DRAM_BYTES_PER_PAIR = {
-    "ssimu2_stats": 66.39e6,
-    "butter_diff": (785.9e6 + 146.6e6 + 3146.3e6 + 613.7e6) / 4,
+    "ssimu2_stats": (7962.84e6 + 7.55e6) / 120,
+    "butter_diff": (2933.67e6 + 568.13e6 + 11811.06e6 + 2325.37e6) / 15,
 }
 
 
@@ -593,6 +594,7 @@ def bench_workload(v, kind, args, ws, rank):
                               "h2d_bytes_per_step": yh2d, "d2h_bytes_per_step": d2h,
                               "trials": [round(x, 1) for x in ytrials]}},
         "pairs_per_step": npairs,
+        "launch_chunk_pairs": chunk,
         "e2e": {"value": e2e_value, "unit": "frame-pairs/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "threads": args.e2e_threads, "steps": args.e2e_steps, "warmup": args.e2e_warmup,
                 "trials": [round(x, 1) for x in trials], "of_trials": "median",
@@ -1049,7 +1051,8 @@ def main_ours(args):
                                               "yuv420p10": link_frac(link, s2["yuv420p10"]["e2e"], n)}
     if not args.skip_butter:
         b = bench_workload(v, "butter", args, ws, rank)
-        out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "e2e", "yuv420p10",
+        out["butteraugli_4k"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "pairs_per_step", "launch_chunk_pairs",
+                                                   "e2e", "yuv420p10",
                                                    "float32_rgb", "input",
                                                    "roofline", "gpu_launches", "clocks", "kernel_share",
                                                    "pipeline_bytes_per_pair", "score_check", "fp16_bands",
@@ -1119,9 +1122,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--pairs", type=int, default=240)
-    ap.add_argument("--chunk", type=int, default=24)
+    ap.add_argument("--chunk", type=int, default=120, help="SSIMU2 pairs per batched launch")
     ap.add_argument("--butter-pairs", type=int, default=60)
-    ap.add_argument("--butter-chunk", type=int, default=4)
+    ap.add_argument("--butter-chunk", type=int, default=15, help="Butteraugli pairs per batched launch")
     ap.add_argument("--e2e-threads", type=int, default=8)
     ap.add_argument("--e2e-steps", type=int, default=8)
     ap.add_argument("--e2e-warmup", type=int, default=4,
