@@ -15,7 +15,8 @@ Workloads (seeded synthetic frames, vship_gb300.synth; no dataset is available o
   * serving      : Poisson request arrivals at 50..2000 req/s against the serving runtime.
 
 A step scores every pair of the workload once.
-  value : inputs resident in HBM, batched device entry points (Vship_*ComputeDeviceAsync), CUDA
+  value : inputs resident in HBM, batched device entry points (Vship_*ComputeDeviceAsync) in
+          launches of --chunk SSIMU2 / --butter-chunk Butteraugli pairs (120 / 15), CUDA
           events on the launching stream around the K timed steps. Inputs (6-12 GB per workload)
           are far larger than L2, so no flush is needed between steps.
   e2e   : the reference-facing C ABI (Vship_ComputeSSIMU2Uint16 / Vship_ComputeButteraugliUint16v3)
