@@ -88,6 +88,16 @@ def test_distmap_stride(vlib):
                                              ctypes.cast(a2, vlib._PP), a[0].strides[0], b[0].strides[0]) == 0
     assert np.array_equal(out[:, : 70 * 4].view(np.float32), dm)
     assert (out[:, 70 * 4:] == 0xEE).all()
+    # a distmap stride shorter than a row is refused before any work, and leaves the buffer and
+    # the handler as they were
+    out[:] = 0xEE
+    assert L.Vship_ComputeButteraugliFloatv3(hd._h, norms, out.ctypes.data, 70 * 4 - 4, ctypes.cast(a1, vlib._PP),
+                                             ctypes.cast(a2, vlib._PP), a[0].strides[0],
+                                             b[0].strides[0]) == vlib.BadPointer
+    assert (out == 0xEE).all()
+    assert L.Vship_ComputeButteraugliFloatv3(hd._h, norms, out.ctypes.data, stride, ctypes.cast(a1, vlib._PP),
+                                             ctypes.cast(a2, vlib._PP), a[0].strides[0], b[0].strides[0]) == 0
+    assert np.array_equal(out[:, : 70 * 4].view(np.float32), dm)
     hd.free()
 
 

@@ -314,6 +314,7 @@ int butter_compute(int id, double norms[3], const uint8_t* dstp, int64_t dststri
                    const int64_t* ystr1 = nullptr, const int64_t* ystr2 = nullptr, bool yuv_fixed = false) {
     ButterHandle* h = g_butter.get(id);
     if (!h || !h->host_io) return E_BAD_HANDLER;
+    if (dstp && dststride < h->eng.w * 4) return E_BAD_POINTER;  // checked before any work is queued
     std::lock_guard<std::mutex> lk(h->io.mu);
     DeviceGuard dg(h->io.device);
     const int bps = intype == IN_FLOAT ? 4 : 2;
@@ -326,7 +327,6 @@ int butter_compute(int id, double norms[3], const uint8_t* dstp, int64_t dststri
     if (rc) return rc;
     if (dstp) {
         const int64_t row = h->eng.w * 4;
-        if (dststride < row) return E_BAD_POINTER;
         TRY_CUDA(cudaMemcpy2DAsync((void*)dstp, dststride, h->eng.distmap, row, row, h->eng.h, cudaMemcpyDeviceToHost,
                                    h->io.stream));
     }

@@ -650,9 +650,13 @@ __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) 
     // reference's b + too_small and -b - too_big are too_small - (-b) and (-b) - too_big, the same
     // IEEE operations, so the value is bitwise the same without divergent branches
     const float bm = a < 0.0f ? -b : b;
-    float impact = bm < too_small ? too_small - bm : (bm > too_big ? bm - too_big : 0.0f);
-    impact *= scaler2;
-    return diff < 0.0f ? v - impact : v + impact;
+    // bm < too_small <= too_big gives (too_small - bm) + 0, bm > too_big gives 0 + (bm - too_big),
+    // anything between 0 + 0: the reference's nested selects, term for term
+    const float impact = (fmaxf(too_small - bm, 0.0f) + fmaxf(bm - too_big, 0.0f)) * scaler2;
+    // v - impact for diff < 0, else v + impact, as one add of impact with diff's sign (impact >= 0;
+    // the two forms differ only for diff == -0, where impact is 0 and only the sign of a zero
+    // changes)
+    return v + copysignf(impact, diff);
 }
 
 // The 16 line patterns, as (dx, dy) taps in the reference's order (maltaDiff.hpp:4-512, after
