@@ -530,13 +530,19 @@ __global__ void __launch_bounds__(256) butter_lf_v_kernel(float* const* __restri
     }
 }
 
-__device__ __forceinline__ float amplify_range(float x, float w) { return x > w ? x + w : x < -w ? x - w : 2.0f * x; }
-__device__ __forceinline__ float remove_range(float x, float w) { return x > w ? x - w : x < -w ? x + w : 0.0f; }
+// The range operators (separatefrequencies.hpp) through the clamp c of x to [-w, w]: above w the
+// reference's x + w / x - w, below -w its x - w / x + w (x + (-w), x - (-w): the same IEEE
+// operations), inside 2x == x + x and x - x == 0. Same values for finite x, three instructions
+// instead of six.
+__device__ __forceinline__ float amplify_range(float x, float w) { return x + fminf(fmaxf(x, -w), w); }
+__device__ __forceinline__ float remove_range(float x, float w) { return x - fminf(fmaxf(x, -w), w); }
+// MaximumClamp (separatefrequencies.hpp) on the same clamp c: above maxval the reference's
+// fma(v - maxval, kMul, maxval), below -maxval fma(v + maxval, kMul, -maxval) (v - (-maxval) is
+// v + maxval), inside fma(0, kMul, v) == v (a zero's sign aside).
 __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
     const float kMul = 0.688059627878f;
-    const float hi = fmaf(v - maxval, kMul, maxval);   // v >= maxval
-    const float lo = fmaf(v + maxval, kMul, -maxval);  // v < -maxval
-    return v >= maxval ? hi : (v < -maxval ? lo : v);
+    const float c = fminf(fmaxf(v, -maxval), maxval);
+    return fmaf(v - c, kMul, c);
 }
 
 // MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
