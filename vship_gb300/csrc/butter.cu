@@ -800,25 +800,31 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         }
         __syncthreads();
         const MaltaMap mm = c_dp.mm[m];
-        if (HB) {
-            // two neighbouring samples per thread: one half2 load and conversion per image
-            constexpr int NP = DF_IH * DF_IW / 2;
+        // four neighbouring samples per thread (rows of 40 floats hold 10 whole quads): one 16-byte
+        // load per image (8 bytes of halves with FP16 bands) and one 16-byte store
+        constexpr int NQ = DF_IH * DF_IW / 4;
 #pragma unroll
-            for (int k = 0; k < (NP + 255) / 256; k++) {
-                const int e2 = threadIdx.x + 256 * k;
-                if (e2 < NP) {
-                    const int r = e2 / (DF_IW / 2), c = 2 * (e2 - r * (DF_IW / 2));
-                    const int hi = r * DFH_P + c + 4;
-                    const float2 a = __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(r0) + hi));
-                    const float2 b = __half22float2(*reinterpret_cast<const __half2*>(reinterpret_cast<const __half*>(r1) + hi));
-                    *reinterpret_cast<float2*>(Dt + r * DF_IW + c) = make_float2(malta_pre(a.x, b.x, mm), malta_pre(a.y, b.y, mm));
+        for (int k = 0; k < (NQ + 255) / 256; k++) {
+            const int q = threadIdx.x + 256 * k;
+            if (q < NQ) {
+                float4 a, b;
+                if (HB) {
+                    const int r = q / (DF_IW / 4), c = 4 * (q - r * (DF_IW / 4));
+                    const int hi = r * DFH_P + c + 4;  // a multiple of 4 halves: 8-byte aligned
+                    const uint2 ua = *reinterpret_cast<const uint2*>(reinterpret_cast<const __half*>(r0) + hi);
+                    const uint2 ub = *reinterpret_cast<const uint2*>(reinterpret_cast<const __half*>(r1) + hi);
+                    const float2 a0 = __half22float2(*reinterpret_cast<const __half2*>(&ua.x));
+                    const float2 a1 = __half22float2(*reinterpret_cast<const __half2*>(&ua.y));
+                    const float2 b0 = __half22float2(*reinterpret_cast<const __half2*>(&ub.x));
+                    const float2 b1 = __half22float2(*reinterpret_cast<const __half2*>(&ub.y));
+                    a = make_float4(a0.x, a0.y, a1.x, a1.y);
+                    b = make_float4(b0.x, b0.y, b1.x, b1.y);
+                } else {
+                    a = reinterpret_cast<const float4*>(r0)[q];
+                    b = reinterpret_cast<const float4*>(r1)[q];
                 }
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < (DF_RAW + 255) / 256; k++) {
-                const int e = threadIdx.x + 256 * k;
-                if (e < DF_RAW) Dt[e] = malta_pre(r0[e], r1[e], mm);
+                reinterpret_cast<float4*>(Dt)[q] = make_float4(malta_pre(a.x, b.x, mm), malta_pre(a.y, b.y, mm),
+                                                               malta_pre(a.z, b.z, mm), malta_pre(a.w, b.w, mm));
             }
         }
         __syncthreads();
