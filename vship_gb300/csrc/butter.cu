@@ -226,15 +226,18 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) butter_decode_kerne
 // ------------------------------------------------------------------------------------------
 // 2-D tile blur, radius 8: 32x48 outputs per 256-thread CTA. The 64x48 input tile (8-px halo,
 // zero outside the image) is staged with cp.async into rows of TB_IP floats; the horizontal pass
-// reads each thread's 24 inputs as six float4 (pitch 52 = 13 quads: the 8 lanes of a
-// quarter-warp phase hit distinct bank quads) and writes 64x32 sums to `hb`; each thread then
-// returns the 6 vertical outputs of column (tid & 31), rows 6*(tid>>5)+o, scaled by the product
-// of both passes' border renormalisations (gaussianblur.hpp:94-186 divides after each pass).
+// reads each thread's 24 inputs as six float4 (a warp takes 32 consecutive rows of one column
+// group; pitch 52 = 13 quads: the 8 lanes of a quarter-warp phase hit distinct bank quads) and
+// writes its 8 sums into the column-major buffer `hb` (column x at hb[x * TB_HC], pitch 66: the
+// warp's stores hit 32 consecutive words); each thread then reads the 22 rows of column
+// (tid & 31) it needs as 11 float2 (66 / 2 odd: a half-warp's 8-byte loads cover all 32 banks) and
+// returns the 6 vertical outputs, rows 6*(tid>>5)+o, scaled by the product of both passes'
+// border renormalisations (gaussianblur.hpp:94-186 divides after each pass).
 constexpr int TB_TW = 32, TB_TH = 48, TB_R = 8;
 constexpr int TB_IW = TB_TW + 2 * TB_R, TB_IH = TB_TH + 2 * TB_R;
-constexpr int TB_IP = 52, TB_HP = 33;
+constexpr int TB_IP = 52, TB_HC = 66;
 constexpr int TB_RAW = TB_IH * TB_IP;
-constexpr int TB_HPL = TB_IH * TB_HP;
+constexpr int TB_HPL = TB_TW * TB_HC;
 
 __device__ __forceinline__ void tile_stage_r8(float* dst, const float* __restrict__ plane, int pitch, int w, int h,
                                               int x0, int y0) {
@@ -245,7 +248,7 @@ template <int KI>
 __device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const float rxy[6], float out[6]) {
     const int tid = threadIdx.x;
     {
-        const int hr = tid >> 2, hg = tid & 3;
+        const int hr = 32 * ((tid >> 5) & 1) + (tid & 31), hg = tid >> 6;
         const float* row = in + hr * TB_IP + 8 * hg;
         float v[24];
 #pragma unroll
@@ -256,22 +259,26 @@ __device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const f
             v[4 * j4 + 2] = q.z;
             v[4 * j4 + 3] = q.w;
         }
-        float* dst = hb + hr * TB_HP + 8 * hg;
+        float* dst = hb + (8 * hg) * TB_HC + hr;
 #pragma unroll
         for (int o = 0; o < 8; o++) {
             float a = 0.f;
 #pragma unroll
             for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
-            dst[o] = a;
+            dst[o * TB_HC] = a;
         }
     }
     __syncthreads();
     {
         const int vc = tid & 31, vg = tid >> 5;
-        const float* col = hb + (6 * vg) * TB_HP + vc;
+        const float2* col = reinterpret_cast<const float2*>(hb + vc * TB_HC + 6 * vg);
         float v[22];
 #pragma unroll
-        for (int j = 0; j < 22; j++) v[j] = col[j * TB_HP];
+        for (int j = 0; j < 11; j++) {
+            const float2 q = col[j];
+            v[2 * j] = q.x;
+            v[2 * j + 1] = q.y;
+        }
 #pragma unroll
         for (int o = 0; o < 6; o++) {
             float a = 0.f;
