@@ -269,14 +269,17 @@ constexpr int ST_SEG = 4 * ST_TH;        // segment height (output rows)
 constexpr int ST_IW = ST_TW + 2 * ST_R;  // 48 input columns
 constexpr int ST_IH = ST_TH + 2 * ST_R;  // 64 raw rows per chunk (image rows ty0 - 8 ..)
 constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte multiple, 13 quads)
-constexpr int ST_HP = 33;                // horizontal-pass row pitch (float pairs)
 constexpr int ST_RAW = ST_IH * ST_RP;    // one raw tile
 constexpr int ST_RING = 64;              // ring slots (power of two): row h of a segment -> h & 63
 constexpr int ST_WIN = ST_TH / 8 + 2 * ST_R;             // 22 ring rows per vertical window
 constexpr int ST_HROWS = ST_RING + ST_WIN;               // slots [0, 22) mirrored at [64, 86)
-constexpr int ST_HPLANE = ST_HROWS * ST_HP;
+// The ring is column-major: column x of a ring plane starts at float pair x * ST_HROWS + 8 * (x / 8)
+// (the 8-pair gap between column groups makes a half-warp's 8-byte stores of two groups hit
+// disjoint banks), so the vertical pass reads its 22 slots as 11 16-byte loads (43 quads per
+// column, odd: 8 neighbouring columns hit distinct bank quads).
+constexpr int ST_HPLANE = ST_TW * ST_HROWS + 8 * (ST_TW / 8 - 1);  // float pairs per ring plane
 // smem: the 2 raw images, the ring as two float-pair planes {m1, m2} and {s11 + s22, s12}, and
-// the per-warp pools: 71 KB, so that three CTAs share an SM
+// the per-warp pools: 70 KB, so that three CTAs share an SM
 constexpr int kStatsSmem = (2 * ST_RAW + 4 * ST_HPLANE + 3 * 8 * 6) * 4;
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
@@ -297,7 +300,7 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                                            const Ssimu2Level& L, int lt, float* __restrict__ out, int stride) {
     extern __shared__ __align__(16) float sm[];
     float* raw = sm;                   // [image][64][52]
-    float* hb = sm + 2 * ST_RAW;       // [2 pair planes][86][33 pairs]
+    float* hb = sm + 2 * ST_RAW;       // [2 pair planes][32 columns of 86 slots, 8-pair gaps]
     float* red = hb + 4 * ST_HPLANE;   // [3 channels][8 warps][6 pools]
     const float* im2 = static_cast<const float*>(im2v);
     const __half* im2h = static_cast<const __half*>(im2v);
@@ -309,7 +312,7 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
 
     // H pass mapping: output columns 8*hg .. 8*hg+7 (inputs 8*hg .. 8*hg+23) of 8 consecutive raw
     // rows per warp x 4 column groups, which keeps the float4 raw reads and the float-pair stores
-    // (pitch 33 pairs) bank-conflict free.
+    // into the column-major ring bank-conflict free.
     const int hg = lane >> 3;
     // V pass mapping: column vc (0..31), output rows 6*vg .. 6*vg+5 of the chunk. Both passes'
     // border renormalisations (out / tot, gaussianblur.hpp:63-92) are applied here as one product.
@@ -411,18 +414,18 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                     }
                 }
                 const int slot = (k * ST_TH + rr) & (ST_RING - 1);
-                f2_t* d1 = reinterpret_cast<f2_t*>(hb) + slot * ST_HP + 8 * hg;
-                f2_t* d2 = reinterpret_cast<f2_t*>(hb + 2 * ST_HPLANE) + slot * ST_HP + 8 * hg;
+                f2_t* d1 = reinterpret_cast<f2_t*>(hb) + 8 * hg * (ST_HROWS + 1) + slot;
+                f2_t* d2 = reinterpret_cast<f2_t*>(hb + 2 * ST_HPLANE) + 8 * hg * (ST_HROWS + 1) + slot;
 #pragma unroll
                 for (int o = 0; o < 8; o++) {
-                    d1[o] = h1[o];
-                    d2[o] = h2[o];
+                    d1[o * ST_HROWS] = h1[o];
+                    d2[o * ST_HROWS] = h2[o];
                 }
                 if (slot < ST_WIN) {
 #pragma unroll
                     for (int o = 0; o < 8; o++) {
-                        d1[ST_RING * ST_HP + o] = h1[o];
-                        d2[ST_RING * ST_HP + o] = h2[o];
+                        d1[o * ST_HROWS + ST_RING] = h1[o];
+                        d2[o * ST_HROWS + ST_RING] = h2[o];
                     }
                 }
             }
@@ -440,14 +443,19 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
             float m[4][6];  // mu1, mu2, E[a^2 + b^2], E[a b] (shifted)
             {
                 const int s0 = (k * ST_TH + 6 * vg) & (ST_RING - 1);
-                const f2_t* c1 = reinterpret_cast<const f2_t*>(hb) + s0 * ST_HP + vc;
-                const f2_t* c2 = reinterpret_cast<const f2_t*>(hb + 2 * ST_HPLANE) + s0 * ST_HP + vc;
+                const int cb = vc * ST_HROWS + 8 * (vc >> 3) + s0;  // even: 16-byte aligned
+                const f2_t* c1 = reinterpret_cast<const f2_t*>(hb) + cb;
+                const f2_t* c2 = reinterpret_cast<const f2_t*>(hb + 2 * ST_HPLANE) + cb;
 #pragma unroll
                 for (int q = 0; q < 2; q++) {
                     const f2_t* col = q == 0 ? c1 : c2;
                     f2_t v[ST_WIN];
 #pragma unroll
-                    for (int j = 0; j < ST_WIN; j++) v[j] = col[j * ST_HP];
+                    for (int j = 0; j < ST_WIN / 2; j++) {
+                        const ulonglong2 p2 = reinterpret_cast<const ulonglong2*>(col)[j];
+                        v[2 * j] = p2.x;
+                        v[2 * j + 1] = p2.y;
+                    }
 #pragma unroll
                     for (int o = 0; o < 6; o++) {
                         f2_t a = f2_pack(0.f, 0.f);
