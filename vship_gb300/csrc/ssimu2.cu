@@ -74,8 +74,15 @@ static int upload_constants_once() {
 }
 
 // ------------------------------------------------------------------------------------------
-// positive XYB (ssimu2/makeXYB.hpp:4-50)
-__device__ __forceinline__ void positive_xyb(float& r, float& g, float& b) {
+// XYB (ssimu2/makeXYB.hpp:4-50) as the metric sees it. The reference adds positive offsets at the
+// end (X * 14 + 0.42, Y + 0.01, B - Y + 0.55); every SSIMULACRA2 map is invariant under one
+// constant added to a channel of both images (the means' difference, the variances, the
+// covariance and |I - mu| all cancel it), so these planes hold X * 14, Y - 0.4 and B - Y instead,
+// three adds fewer per sample and level (the offsets are double constants, each an add pair in
+// FP32). The stats kernel still shifts each segment's samples by one of its own values: that
+// keeps flat areas and frames of a few pixels exact, where a blur's border renormalisation leaves
+// a few ulps of x^2 in E[x^2] - E[x]^2.
+__device__ __forceinline__ void centred_xyb(float& r, float& g, float& b) {
     const float bias = 0.0037930734f;
     float ox = fmaf(0.30f, r, fmaf(0.622f, g, fmaf(0.078f, b, bias)));
     float oy = fmaf(0.23f, r, fmaf(0.692f, g, fmaf(0.078f, b, bias)));
@@ -87,10 +94,9 @@ __device__ __forceinline__ void positive_xyb(float& r, float& g, float& b) {
     float X = 0.5f * (ox - oy);
     float Y = X + oy;
     float B = oz;
-    constexpr DConst k055 = dconst(0.55), k042 = dconst(0.42), k001 = dconst(0.01);
-    r = add_dc(X * 14.0f, k042);
-    g = add_dc(Y, k001);
-    b = add_dc(B - Y, k055);
+    r = X * 14.0f;
+    g = Y - 0.4f;
+    b = B - Y;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -147,7 +153,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
                     v[c][i] = gx + i < L.w ? lin : 0.f;  // frames converted to linear light skip x^2.4
                 }
                 float X = v[0][i], Y = v[1][i], B = v[2][i];
-                positive_xyb(X, Y, B);
+                centred_xyb(X, Y, B);
                 o[0][i] = X;
                 o[1][i] = Y;
                 o[2][i] = B;
@@ -182,7 +188,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
                     v2 = to_linear_fast(v2);
                 }
                 float X = v0, Y = v1, B = v2;
-                positive_xyb(X, Y, B);
+                centred_xyb(X, Y, B);
                 pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);
             }
             smA[(0 * 32 + ly) * 33 + tx] = v0;
@@ -219,7 +225,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
                     v[c] = s * 0.25f;
                 }
                 float X = v[0], Y = v[1], B = v[2];
-                positive_xyb(X, Y, B);
+                centred_xyb(X, Y, B);
                 pyr_store<DELTA>(out, pe, L.off + (int64_t)gy * L.pitch + gx, X, Y, B);
             }
 #pragma unroll
