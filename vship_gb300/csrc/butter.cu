@@ -316,10 +316,11 @@ __device__ __forceinline__ void b_opsin(float& x, float& y, float& z, bool clamp
     z = oz;
 }
 __device__ __forceinline__ float b_gamma(float v) {
-    constexpr DConst kOff = dconst(9.9710635769299145);
     // logf(x) as log2(x) * ln 2 (x >= 9.97 here, so the approximation's absolute log2 error of
-    // ~2^-22 is ~1e-7 relative)
-    return fmaf(19.245013259874995f, lg2_approx(add_dc(v, kOff)) * 0.69314718055994531f, -23.16046239805755f);
+    // ~2^-22 is ~1e-7 relative). The reference adds the double literal and rounds the sum to
+    // float; the float sum here is at most 1 ulp from it, below the log approximation's error.
+    return fmaf(19.245013259874995f, lg2_approx(v + 9.9710635769299145f) * 0.69314718055994531f,
+                -23.16046239805755f);
 }
 
 // grid (ceil(w/32), ceil(h/48), nimages); the three channels' tiles are double-buffered.
@@ -953,14 +954,9 @@ __global__ void __launch_bounds__(256, 6) butter_mask_blur_kernel(float* const* 
 
 // combineMasks.hpp:3-19
 __device__ __forceinline__ float mask_common(float c) {
-    constexpr DConst kK = dconst(1.0 / (double)(0.79079917404f * 17.83f));
-    // (float)((1.0 + c) * K) with 1 + c kept exact as a float pair
-    const float s = 1.0f + c;
-    const float bb = s - 1.0f;
-    const float e = (1.0f - (s - bb)) + (c - bb);
-    const float p = s * kK.hi;
-    const float pe = fmaf(s, kK.hi, -p);
-    const float r = p + (pe + fmaf(s, kK.lo, e * kK.hi));
+    // the reference's (float)((1.0 + c) * K) in double, here in FP32: within 2 ulp of it
+    constexpr float kK = (float)(1.0 / (double)(0.79079917404f * 17.83f));
+    const float r = (1.0f + c) * kK;
     return r * r;
 }
 __device__ __forceinline__ float mask_y(float delta) {
