@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) butter_decode_kerne
             for (int c = 0; c < 3; c++) {
 #pragma unroll
                 for (int i = 0; i < 4; i++)
-                    if (!(IT == IN_YUV && yp.linear_out)) v[c][i] = gx + i < F.w ? to_linear_fast(v[c][i]) : 0.f;
+                    if (!(IT == IN_YUV && yp.linear_out)) v[c][i] = gx + i < F.w ? to_linear_fast<IT>(v[c][i]) : 0.f;
                 float* d = iplane(ib, g, F, img, I_LIN + c) + (int64_t)gy * F.p + gx;
                 if (gx + 3 < F.w) {
                     *reinterpret_cast<float4*>(d) = make_float4(v[c][0], v[c][1], v[c][2], v[c][3]);
@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) butter_decode_kerne
                 load_rgb<IT>(fd, yp, gx, gy, F.w, F.h, v[0], v[1], v[2]);
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    if (!(IT == IN_YUV && yp.linear_out)) v[c] = to_linear_fast(v[c]);
+                    if (!(IT == IN_YUV && yp.linear_out)) v[c] = to_linear_fast<IT>(v[c]);
                     iplane(ib, g, F, img, I_LIN + c)[(int64_t)gy * F.p + gx] = v[c];
                 }
             }

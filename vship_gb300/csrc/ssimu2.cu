@@ -149,7 +149,7 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
             for (int i = 0; i < 4; i++) {
 #pragma unroll
                 for (int c = 0; c < 3; c++) {
-                    const float lin = (IT == IN_YUV && yp.linear_out) ? v[c][i] : to_linear_fast(v[c][i]);
+                    const float lin = (IT == IN_YUV && yp.linear_out) ? v[c][i] : to_linear_fast<IT>(v[c][i]);
                     v[c][i] = gx + i < L.w ? lin : 0.f;  // frames converted to linear light skip x^2.4
                 }
                 float X = v[0][i], Y = v[1][i], B = v[2][i];
@@ -183,9 +183,9 @@ __device__ __forceinline__ void pyramid_tile(const FrameDesc& fd, const YuvParam
             if (gx < L.w && gy < L.h) {
                 load_rgb<IT>(fd, yp, gx, gy, L.w, L.h, v0, v1, v2);
                 if (!(IT == IN_YUV && yp.linear_out)) {  // frames converted to linear light skip x^2.4
-                    v0 = to_linear_fast(v0);
-                    v1 = to_linear_fast(v1);
-                    v2 = to_linear_fast(v2);
+                    v0 = to_linear_fast<IT>(v0);
+                    v1 = to_linear_fast<IT>(v1);
+                    v2 = to_linear_fast<IT>(v2);
                 }
                 float X = v0, Y = v1, B = v2;
                 centred_xyb(X, Y, B);
