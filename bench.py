@@ -701,8 +701,8 @@ def bench_multi(v, args, ws, rank):
     ms = [src_res.count(r) for r in range(len(MULTI_RES))]
     mp = [8 * n for n in ms]
     flags = v.MULTI_SSIMU2 | v.MULTI_BUTTERAUGLI | v.MULTI_FP16 | v.MULTI_AUTOTUNE
-    tune = os.path.join(ROOT, "gpurun_out", "multi_tune.json") if os.path.isdir(os.path.join(ROOT, "gpurun_out")) \
-        else None
+    # the autotuner's cache file: $VSHIP_MULTI_TUNE_CACHE, else one in the system temp folder
+    tune = os.environ.get("VSHIP_MULTI_TUNE_CACHE") or os.path.join(tempfile.gettempdir(), "vship_multi_tune.json")
     sc = v.MultiScorer(MULTI_RES, ms, mp, flags, 2, 203.0, tune)
     srcs = multi_descs(buf, metas, src_frame)
     cands = multi_descs(buf, metas, cand_frame)
