@@ -23,9 +23,15 @@ A step scores every pair of the workload once.
           from pinned host buffers, one handler per host thread; every call copies its planes
           host->device and reads its score back.
 
+  reference_cuda: the reference's own CUDA build (oracle/_ref/libvship_ref.so, built from
+          pkp24/Vship's sources by oracle/ref_build.py) through its stock C ABI calls on the same
+          pinned RGB48 host planes, 3 and 8 handler threads; its frame-pairs/s, this build's e2e and
+          device rates over it, and the score / norm differences on every pair.
+  error_vs_fp64: each reported form's error against the FP64 oracle on the first pairs.
+
 --impl reference runs the reference's math on the host cores instead (the reference has no CPU
-implementation and its CUDA build cannot run on this machine, so this is the FP32 CPU
-restatement in oracle/, threaded over all host cores), one bounded sample per step.
+implementation, so this is the FP32 CPU restatement in oracle/, threaded over all host cores),
+one bounded sample per step.
 
 Multi-GPU: every rank runs the full workload on its own GPU (frame pairs are independent,
 replicas only); value = pairs over all ranks / max over ranks of the timed region.
@@ -431,6 +437,129 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None, half_bands=Fal
     return sec, h2d, d2h, np.array(scores), [npairs * steps / t for t in trials]
 
 
+REF_THREADS = (3, 8)
+
+
+def run_reference_cuda(kind, ref, dst, steps, warmup):
+    """The reference's own CUDA build (oracle/_ref/libvship_ref.so, pkp24/Vship src/VshipLib.cpp
+    compiled for sm_103a) through its stock C ABI calls -- Vship_ComputeSSIMU2Uint16 /
+    Vship_ComputeButteraugliUint16 -- from the same pinned RGB48 host planes as this build's e2e,
+    one handler per host thread, at the 3 threads its documentation recommends and at 8 (this
+    build's e2e setting); the better rate is the baseline. Every call copies its planes
+    host->device, computes and returns its result, as the reference always does. Returns None when
+    the library is not built on this machine.
+
+    The reference's ABI truncates Butteraugli norms to ints, so after the timed trials one untimed
+    pass scores every pair through VshipRef_ComputeButteraugli (the same computing implementation,
+    float norms) for the parity figures."""
+    import ctypes
+    import numpy as np
+    import torch
+    from oracle import reference_cuda as R
+    if not R.available():
+        return None
+    L = R.lib()
+    npairs, _, h, w = ref.shape
+    if kind != "ssimu2" and not R.butteraugli_size_safe(w, h):
+        return None
+    href = ref.cpu().pin_memory()
+    hdst = dst.cpu().pin_memory()
+    ptrs = []
+    for t in range(npairs):
+        a = (ctypes.c_void_p * 3)(*[href[t, c].data_ptr() for c in range(3)])
+        b = (ctypes.c_void_p * 3)(*[hdst[t, c].data_ptr() for c in range(3)])
+        ptrs.append((a, b))
+    stride = w * 2
+    out = {"calls": "Vship_ComputeSSIMU2Uint16" if kind == "ssimu2" else "Vship_ComputeButteraugliUint16",
+           "input": "RGB48 planes, pinned host memory (the same buffers as e2e)", "by_threads": {}}
+    scores = [None] * npairs
+    best = 0.0
+    for nthreads in REF_THREADS:
+        handlers = []
+        for _ in range(nthreads):
+            hd = R._Handler()
+            rc = (L.Vship_SSIMU2Init(ctypes.byref(hd), w, h) if kind == "ssimu2"
+                  else L.Vship_ButteraugliInitv2(ctypes.byref(hd), w, h, 2, ctypes.c_float(203.0)))
+            R._check(rc, "reference init")
+            handlers.append(hd)
+        errors = []
+
+        def worker(k):
+            hd = handlers[k]
+            sc = ctypes.c_double()
+            bs = R._ButterScore()
+            for i in range(k, npairs, nthreads):
+                a, b = ptrs[i]
+                if kind == "ssimu2":
+                    rc = L.Vship_ComputeSSIMU2Uint16(hd, ctypes.byref(sc), ctypes.cast(a, R._PP),
+                                                     ctypes.cast(b, R._PP), stride)
+                    scores[i] = sc.value
+                else:
+                    rc = L.Vship_ComputeButteraugliUint16(hd, ctypes.byref(bs), None, 0, ctypes.cast(a, R._PP),
+                                                          ctypes.cast(b, R._PP), stride)
+                if rc:
+                    errors.append(rc)
+
+        def step():
+            th = [threading.Thread(target=worker, args=(k,)) for k in range(nthreads)]
+            [t.start() for t in th]
+            [t.join() for t in th]
+
+        for _ in range(warmup):
+            step()
+        trials = []
+        for _ in range(E2E_TRIALS):
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                step()
+            trials.append(time.perf_counter() - t0)
+        if errors:
+            R._check(errors[0], "reference compute")
+        if kind != "ssimu2":
+            norms = (ctypes.c_float * 3)()
+            hd = handlers[0]
+            for i in range(npairs):
+                a, b = ptrs[i]
+                R._check(L.VshipRef_ComputeButteraugli(hd, norms, 1, None, 0, ctypes.cast(a, R._PP),
+                                                       ctypes.cast(b, R._PP), stride, stride), "reference norms")
+                scores[i] = (float(norms[0]), float(norms[1]), float(norms[2]))
+        for hd in handlers:
+            (L.Vship_SSIMU2Free if kind == "ssimu2" else L.Vship_ButteraugliFree)(hd)
+        sec = sorted(trials)[len(trials) // 2]
+        v = npairs * steps / sec
+        out["by_threads"][str(nthreads)] = {"value": v, "trials": [round(npairs * steps / t, 1) for t in trials]}
+        best = max(best, v)
+    torch.cuda.synchronize()
+    out.update({"value": best, "unit": "frame-pairs/s", "steps": steps, "warmup": warmup, "of_trials": "median",
+                "h2d_bytes_per_step": npairs * 2 * 3 * w * h * 2,
+                "d2h_bytes_per_step": npairs * (8 if kind == "ssimu2" else 12)})
+    return out, np.array(scores, dtype=np.float64)
+
+
+def error_vs_fp64(kind, ref, dst, forms, npairs, nthreads):
+    """For each form (name -> per-pair results), the max over the first npairs of |got - FP64
+    oracle| (SSIMU2, absolute) or of the relative error of each of {Qnorm, 3-norm, inf-norm}
+    (Butteraugli). ref/dst: (pairs, 3, H, W) float32, or uint16 bits held in int16."""
+    import numpy as np
+    import oracle
+    u16 = str(ref.dtype) == "torch.int16"
+    conv = (lambda x: np.ascontiguousarray(x.cpu().numpy().view(np.uint16))) if u16 else \
+        (lambda x: np.ascontiguousarray(x.cpu().numpy()))
+    worst = {k: None for k in forms}
+    for t in range(npairs):
+        a = [conv(ref[t, c]) for c in range(3)]
+        b = [conv(dst[t, c]) for c in range(3)]
+        if kind == "ssimu2":
+            want = oracle.ssimu2(a, b, precision=64, nthreads=nthreads)
+        else:
+            want = oracle.butteraugli(a, b, precision=64, nthreads=nthreads)
+        for k, got in forms.items():
+            e = abs(float(got[t]) - want) if kind == "ssimu2" else rel_err(got[t], want)
+            w = worst[k]
+            worst[k] = e if w is None else (max(w, e) if kind == "ssimu2" else [max(x, y) for x, y in zip(w, e)])
+    return worst
+
+
 def cpu_baseline(kind, ref, dst, sample_pairs, nthreads, fp64_pairs=0):
     """The reference's math (FP32 restatement in oracle/) on the host cores for a bounded sample.
     With fp64_pairs > 0 the FP64 instantiation also scores the first pairs (untimed), the
@@ -496,6 +625,7 @@ def bench_workload(v, kind, args, ws, rank):
     """The headline form is the reference front-end's own input: 16-bit R'G'B' planes (FFVship
     converts every frame to RGB48 and calls the Uint16 entry points). Float32 R'G'B' and
     10-bit 4:2:0 (converted on the GPU) are measured beside it."""
+    import numpy as np
     import torch
     npairs = args.pairs if kind == "ssimu2" else args.butter_pairs
     chunk = args.chunk if kind == "ssimu2" else args.butter_chunk
@@ -506,10 +636,6 @@ def bench_workload(v, kind, args, ws, rank):
     # float32 R'G'B' planes
     fsec, _, _, fres = run_device(v, kind, ref, dst, args.steps, args.warmup, ws, chunk)
     fsec = max_over_ranks(fsec, ws)
-    hres = None
-    if kind != "ssimu2" and not args.skip_half_bands:
-        # the FP16-band storage form on the same float planes: its error against FP64 below
-        _, _, _, hres = run_device(v, kind, ref, dst, 1, 1, ws, chunk, half_bands=True)
     fe2e_sec, fh2d, d2h, _, ftrials = run_e2e(v, kind, ref, dst, args.e2e_steps, args.e2e_warmup, args.e2e_threads)
     fe2e_sec = max_over_ranks(fe2e_sec, ws)
     # the CPU leg runs after every GPU measurement (an all-core run before them measurably slowed
@@ -517,11 +643,11 @@ def bench_workload(v, kind, args, ws, rank):
     ns = nx = 0
     if rank == 0 and args.cpu_sample > 0:
         ns = args.cpu_sample if kind == "ssimu2" else max(1, args.cpu_sample // 4)
-        nx = args.error_pairs if kind != "ssimu2" else 0
-    ncpu = max(ns, nx)
-    ref_cpu, dst_cpu = ref[:ncpu].cpu(), dst[:ncpu].cpu()
+        nx = args.error_pairs if kind == "ssimu2" else args.butter_error_pairs
+    ref_cpu, dst_cpu = ref[:ns].cpu(), dst[:ns].cpu()
     # 16-bit R'G'B' (headline)
     ref16, dst16 = to_rgb48(ref), to_rgb48(dst)
+    ref16_cpu, dst16_cpu = ref16[:nx].cpu(), dst16[:nx].cpu()
     del ref, dst
     torch.cuda.empty_cache()
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
@@ -533,6 +659,17 @@ def bench_workload(v, kind, args, ws, rank):
     e2e_sec, h2d, d2h, host_scores, trials = run_e2e(v, kind, ref16, dst16, args.e2e_steps, args.e2e_warmup, args.e2e_threads)
     e2e_sec = max_over_ranks(e2e_sec, ws)
     e2e_value = npairs * ws * args.e2e_steps / e2e_sec
+    refc = None
+    if rank == 0 and not args.skip_reference_cuda:
+        # the reference's own CUDA build on the same pinned RGB48 frames, through its own C ABI
+        refc = run_reference_cuda(kind, ref16, dst16, args.ref_steps, args.ref_warmup)
+    worst_frames = None
+    if refc is not None and kind == "ssimu2":
+        # host copies of the pairs where the two builds differ most, for the FP64 check below
+        d_ = np.abs(dev_scores.numpy() - refc[1])
+        sub = torch.tensor([int(i) for i in np.argsort(-d_)[:args.ref_worst_pairs]], dtype=torch.long)
+        worst_frames = (ref16[sub.cuda()].cpu(), dst16[sub.cuda()].cpu())
+    barrier(ws)
     kname = "ssimu2_stats" if kind == "ssimu2" else "butter_diff"
     per_pair = ssimu2_stats_bytes(w, h) if kind == "ssimu2" else butter_diff_bytes(w, h)
     peak, peak_kind = measured_peaks()
@@ -562,8 +699,9 @@ def bench_workload(v, kind, args, ws, rank):
                      "flops_per_pair": ssimu2_stats_flops(w, h),
                      "peak_source": f"128 FP32 FMA lanes x SMs x {mhz:.0f} MHz (sampled clock)"}
     half = None
+    hres = None
     if kind != "ssimu2" and not args.skip_half_bands:
-        hsec, hprof, _, _ = run_device(v, kind, ref16, dst16, args.steps, args.warmup, ws, chunk, half_bands=True)
+        hsec, hprof, _, hres = run_device(v, kind, ref16, dst16, args.steps, args.warmup, ws, chunk, half_bands=True)
         hsec = max_over_ranks(hsec, ws)
         he2e_sec, _, _, _, htrials = run_e2e(v, kind, ref16, dst16, args.e2e_steps, args.e2e_warmup, args.e2e_threads, half_bands=True)
         he2e_sec = max_over_ranks(he2e_sec, ws)
@@ -616,20 +754,52 @@ def bench_workload(v, kind, args, ws, rank):
     }
     if half:
         res["fp16_bands"] = half
-    if ns > 0:
-        cv, csec, exact = cpu_baseline(kind, ref_cpu, dst_cpu, ns, os.cpu_count() or 1, fp64_pairs=nx)
-        cpu_res = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
-                   "sample": f"{ns} pairs of the same workload ({csec:.1f} s)"}
-        if exact:
-            # max over the checked pairs of the relative error of {Qnorm, 3-norm, inf-norm}
-            def worst(r_):
-                r = r_.numpy().reshape(-1, 3)
-                return [max(e) for e in zip(*[rel_err(r[t], exact[t]) for t in range(len(exact))])]
-            cpu_res["error_vs_fp64"] = {"pairs": len(exact), "input": "float32 R'G'B'",
-                                        "fp32_planes": worst(fres)}
+    if refc is not None:
+        rinfo, rscores = refc
+        mine = dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy().reshape(-1, 3)
+        if kind == "ssimu2":
+            diff = np.abs(mine - rscores)
+            rinfo["score_diff_max_abs"] = float(diff.max())
+            rinfo["score_diff_p99_abs"] = float(np.percentile(diff, 99))
+            rinfo["pairs_over_1e-3"] = int((diff > 1e-3).sum())
+            rinfo["tolerance"] = "1e-3 absolute"
+            if rank == 0 and args.cpu_sample > 0:
+                # the pairs where the two builds differ most, against the FP64 oracle: which of the
+                # two is off (the reference pools its per-block sums in FP32 on the host)
+                worst = [int(i) for i in np.argsort(-diff)[:args.ref_worst_pairs]]
+                if worst:
+                    wr, wd = worst_frames
+                    e = error_vs_fp64(kind, wr, wd, {"ours": mine[worst], "reference": rscores[worst]}, len(worst),
+                                      os.cpu_count() or 1)
+                    rinfo["largest_differences_vs_fp64"] = {
+                        "pairs": worst, "diff": [float(diff[i]) for i in worst],
+                        "ours_max_abs_err": e["ours"], "reference_max_abs_err": e["reference"]}
+        else:
+            rinfo["norm_diff_max_rel"] = [float(x) for x in (np.abs(mine - rscores) / np.abs(rscores)).max(axis=0)]
+            rinfo["tolerance"] = "1e-4 relative"
+        rinfo["pairs_compared"] = int(len(rscores))
+        rinfo["e2e_ratio"] = e2e_value / rinfo["value"]
+        rinfo["device_ratio"] = value / rinfo["value"]
+        rinfo["target"] = ">= 2x the reference CUDA build's frame-pairs/s"
+        res["reference_cuda"] = rinfo
+    if nx > 0:
+        nt = os.cpu_count() or 1
+        err = {"pairs": nx, "input": "RGB48 planes (the headline input)", "oracle": "FP64 oracle (oracle/)"}
+        if kind == "ssimu2":
+            forms = {"score_max_abs": dev_scores.numpy()}
+        else:
+            forms = {"fp32_planes_max_rel": dev_scores.numpy().reshape(-1, 3)}
             if hres is not None:
-                cpu_res["error_vs_fp64"]["fp16_bands"] = worst(hres)
-        res["cpu_baseline"] = cpu_res
+                forms["fp16_bands_max_rel"] = hres.numpy().reshape(-1, 3)
+            err["norms"] = "Qnorm (2), 3-norm, inf-norm"
+        if refc is not None:
+            forms["reference_cuda_" + ("score_max_abs" if kind == "ssimu2" else "max_rel")] = refc[1]
+        err.update(error_vs_fp64(kind, ref16_cpu, dst16_cpu, forms, nx, nt))
+        res["error_vs_fp64"] = err
+    if ns > 0:
+        cv, csec, _ = cpu_baseline(kind, ref_cpu, dst_cpu, ns, os.cpu_count() or 1)
+        res["cpu_baseline"] = {"value": cv, "unit": "frame-pairs/s", "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"{ns} pairs of the same workload ({csec:.1f} s)"}
     torch.cuda.empty_cache()
     return res
 
@@ -701,8 +871,10 @@ def bench_multi(v, args, ws, rank):
     ms = [src_res.count(r) for r in range(len(MULTI_RES))]
     mp = [8 * n for n in ms]
     flags = v.MULTI_SSIMU2 | v.MULTI_BUTTERAUGLI | v.MULTI_FP16 | v.MULTI_AUTOTUNE
-    # the autotuner's cache file: $VSHIP_MULTI_TUNE_CACHE, else one in the system temp folder
-    tune = os.environ.get("VSHIP_MULTI_TUNE_CACHE") or os.path.join(tempfile.gettempdir(), "vship_multi_tune.json")
+    # the autotuner's cache file: $VSHIP_MULTI_TUNE_CACHE, else one of this run and rank in the
+    # system temp folder (never shared with other jobs, nor with this job's other ranks)
+    tune = os.environ.get("VSHIP_MULTI_TUNE_CACHE") or os.path.join(
+        tempfile.gettempdir(), f"vship_multi_tune.{os.getpid()}.{rank}.json")
     sc = v.MultiScorer(MULTI_RES, ms, mp, flags, 2, 203.0, tune)
     srcs = multi_descs(buf, metas, src_frame)
     cands = multi_descs(buf, metas, cand_frame)
@@ -1041,8 +1213,9 @@ def main_ours(args):
         "yuv420p10": s2["yuv420p10"], "float32_rgb": s2["float32_rgb"], "input": s2["input"],
         "score_check": s2["score_check"],
         })
-    if "cpu_baseline" in s2:
-        out["cpu_baseline"] = s2["cpu_baseline"]
+    for k in ("reference_cuda", "error_vs_fp64", "cpu_baseline"):
+        if k in s2:
+            out[k] = s2[k]
     out["host_link"] = {"h2d_gbs": round(link, 1),
                         "note": "pinned host -> device copy, 256 MiB; e2e frac = its h2d bytes/s over this"}
     if s2:
@@ -1057,7 +1230,7 @@ def main_ours(args):
                                                    "float32_rgb", "input",
                                                    "roofline", "gpu_launches", "clocks", "kernel_share",
                                                    "pipeline_bytes_per_pair", "score_check", "fp16_bands",
-                                                   "kernel_roofline")
+                                                   "kernel_roofline", "reference_cuda", "error_vs_fp64")
                                  if k in b}
         if "cpu_baseline" in b:
             out["butteraugli_4k"]["cpu_baseline"] = b["cpu_baseline"]
@@ -1110,8 +1283,9 @@ def main_reference(args):
         "cpu_baseline": {"value": value, "unit": "frame-pairs/s", "cores": nt, "kind": "port",
                          "sample": f"{args.steps} pairs, 1 per step"},
         "e2e": {"value": value, "unit": "frame-pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference has no CPU implementation and its CUDA build cannot be built for this Arm host "
-                "from its sources here; this is its FP32 math restated in C++ (oracle/), threaded over all cores",
+        "note": "the reference has no CPU implementation (its math exists only as CUDA kernels); this is that math "
+                "restated in C++ (oracle/, FP32 instantiation), threaded over all host cores. The reference's own "
+                "CUDA build on the GPU is measured in the main run's reference_cuda block",
     }
     print(json.dumps(out), flush=True)
 
@@ -1136,8 +1310,16 @@ def main():
     ap.add_argument("--skip-multi", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
     ap.add_argument("--skip-half-bands", action="store_true", help="skip the FP16-band Butteraugli run")
-    ap.add_argument("--error-pairs", type=int, default=1,
+    ap.add_argument("--error-pairs", type=int, default=8,
+                    help="SSIMU2 pairs scored by the FP64 oracle for the headline's error")
+    ap.add_argument("--butter-error-pairs", type=int, default=4,
                     help="Butteraugli pairs scored by the FP64 oracle for the error of each storage form")
+    ap.add_argument("--skip-reference-cuda", action="store_true",
+                    help="skip the reference CUDA build's leg (reference_cuda)")
+    ap.add_argument("--ref-steps", type=int, default=2, help="timed steps per trial of the reference CUDA leg")
+    ap.add_argument("--ref-warmup", type=int, default=1)
+    ap.add_argument("--ref-worst-pairs", type=int, default=4,
+                    help="SSIMU2 pairs where the builds differ most, scored by the FP64 oracle")
     ap.add_argument("--serve-size", default=f"{W4K}x{H4K}")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-max-requests", type=int, default=400)

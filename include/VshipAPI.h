@@ -308,8 +308,10 @@ EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytesEx(int width, int height, 
  *
  * Limit: the two XYB pyramids plus per-tile sums must fit the array; 1280x720 does, larger
  * frames are refused with Vship_OutOfVRAM before anything is launched.
- * The first call on a device looks the array up and uploads that device's constant tables;
- * make it before any stream capture on that device.
+ * CUDA loads device code lazily by default, so the array's 32 MiB is committed on a device by
+ * the first call made there, which also uploads that device's constant tables. Make that first
+ * call at start-up, before fixing the memory budget and before any stream capture on that
+ * device; if the device has no room for the array, it returns Vship_OutOfVRAM.
  * All calls on one device share the array: calls whose GPU work overlaps (different streams or
  * host threads) race, so order them on one stream. */
 #define VSHIP_SSIMU2_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
@@ -410,8 +412,9 @@ EXPORTPREPROCESS Vship_Exception Vship_ServeCreate(Vship_ServeHandler* handler, 
                                                    uint64_t admission_bytes, uint64_t cache_bytes,
                                                    int max_batch_pairs, int flags, int Qnorm,
                                                    float intensity_multiplier);
-/* Format of Vship_InYuv frames (Vship_YuvFormat; matrix 2 resolves per resolution); set it
- * before the first submit. */
+/* Format of Vship_InYuv frames (Vship_YuvFormat; matrix 2 resolves per resolution). Set it before
+ * the first submit: cached source state is keyed by source, not by format, so once a request has
+ * been submitted the call is refused with Vship_BadPointer and the format stays as it was. */
 EXPORTPREPROCESS Vship_Exception Vship_ServeSetYuvFormat(Vship_ServeHandler handler, const Vship_YuvFormat* format);
 /* Vship_OutOfVRAM: the request's charge alone exceeds admission_bytes. */
 EXPORTPREPROCESS Vship_Exception Vship_ServeSubmit(Vship_ServeHandler handler, const Vship_ServeRequest* request);

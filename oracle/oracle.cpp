@@ -83,7 +83,7 @@ float half_to_float(uint16_t h) {
     return f;
 }
 
-// util/float3operations.hpp:293-314 (convertPointer<InputMemType>)
+// util/float3operations.hpp:197-218 (convertPointer<InputMemType>)
 template <typename T>
 inline T decode(const uint8_t* plane, int64_t stride, int64_t x, int64_t y, int intype) {
     const uint8_t* row = plane + y * stride;
@@ -559,7 +559,7 @@ void malta_diff(const T* l0, const T* l1, T* ac, int64_t w, int64_t h, T w_0gt1,
     });
 }
 
-// butter/simplerdiff.hpp:244-261
+// butter/simplerdiff.hpp:41-59 (L2diff_Kernel, L2diff)
 template <typename T> void l2diff(const T* a, const T* b, T* dst, int64_t n, T w) {
     if (w == (T)0) return;
     for (int64_t i = 0; i < n; i++) {
@@ -568,7 +568,8 @@ template <typename T> void l2diff(const T* a, const T* b, T* dst, int64_t n, T w
     }
 }
 
-// butter/simplerdiff.hpp:263-303 (including the extra x0.8 applied to both weights at :297-298)
+// butter/simplerdiff.hpp:61-100 (L2AsymDiff_Kernel, L2AsymDiff; including the extra x0.8 applied to
+// both weights at :94-95)
 template <typename T> void l2asym(const T* a, const T* b, T* dst, int64_t n, T w_gt, T w_lt) {
     if (w_gt == (T)0 && w_lt == (T)0) return;
     w_gt = mulD(w_gt, 0.8);
@@ -798,7 +799,7 @@ std::vector<T> butter_diffmap(std::vector<T> src1[3], std::vector<T> src2[3], in
     }
     fuzzy_erosion(blurred[0].data(), mask.data(), w, h);
     l2diff(blurred[0].data(), blurred[1].data(), ac[1].data(), n, (T)10.0f);
-    // butter/combineMasks.hpp:157-169
+    // butter/combineMasks.hpp:21-40 (computeDiffmap_Kernel, computeDiffmap)
     std::vector<T> diffmap(n);
     for (int64_t i = 0; i < n; i++) {
         T v = mask[i];
@@ -809,7 +810,7 @@ std::vector<T> butter_diffmap(std::vector<T> src1[3], std::vector<T> src2[3], in
     return diffmap;
 }
 
-// butter/main.hpp:116-195 (getmultiscalediffmap, butterprocess) and diffnorms.hpp:263-306
+// butter/main.hpp:116-195 (getmultiscalediffmap, butterprocess) and diffnorms.hpp:86-129 (diffmapscore)
 template <typename T>
 void butteraugli(const uint8_t* const* src1, const uint8_t* const* src2, int64_t stride1, int64_t stride2, int64_t w,
                  int64_t h, int intype, int qnorm, float intensity, int nthreads, double norms[3], float* distmap,
@@ -831,7 +832,7 @@ void butteraugli(const uint8_t* const* src1, const uint8_t* const* src2, int64_t
     }
     std::vector<T> dm = butter_diffmap(full[0], full[1], w, h, intensity, K, nthreads, half_bands);
     std::vector<T> dms = butter_diffmap(half[0], half[1], nw, nh, intensity, K, nthreads, half_bands);
-    // butter/downupsample.hpp:287-301 (addsupersample2X, w = 0.5)
+    // butter/downupsample.hpp:34-56 (addsupersample2X_kernel, addsupersample2X; w = 0.5)
     const T wsup = (T)0.5f;
     for (int64_t y = 0; y < h; y++)
         for (int64_t x = 0; x < w; x++) {

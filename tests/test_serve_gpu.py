@@ -136,3 +136,21 @@ def test_serve_rejects_oversized(vlib):
     srv.drain()
     assert [c[0] for c in srv.poll()] == [2] and all(0 < s <= 100 for s in out)
     srv.free()
+
+
+def test_serve_yuv_format_is_fixed_after_first_submit(vlib):
+    # cached source state is keyed by source, not by format: a format change after a submit
+    # would score later candidates against sources decoded under the old format
+    keep = []
+    pool = _pool(keep, nsrc=1)
+    srv = vlib.Server(RES, vlib.IN_YUV420P10)
+    srv.set_yuv_format(vlib.yuv_format(bits=10))  # before any submit: accepted
+    src, cands = pool[(0, 0)]
+    out = np.zeros(2)
+    srv.submit(1, 0, 0, 5, src, cands[:2], out)
+    with pytest.raises(vlib.VshipError) as e:
+        srv.set_yuv_format(vlib.yuv_format(bits=10, full_range=True))
+    assert e.value.code == vlib.BadPointer
+    srv.drain()
+    assert [c[0] for c in srv.poll()] == [1] and all(0 < s <= 100 for s in out)
+    srv.free()

@@ -19,6 +19,10 @@
 #include <fstream>
 #include <map>
 #include <sstream>
+#include <string>
+#include <thread>
+
+#include <unistd.h>
 
 namespace vship {
 
@@ -478,7 +482,8 @@ bool MultiEngine::tune_lookup(const std::string& key, MultiKnobs* k) {
     const auto m = read_tune_file(tune_path);
     const auto it = m.find(key);
     if (it == m.end()) return false;
-    k->grid_per_sm = std::min(json_int(it->second, "grid_per_sm", k->grid_per_sm), stats_blocks_per_sm);
+    // 0 means one CTA per work item; a corrupt or hand-edited entry is clamped to [0, occupancy]
+    k->grid_per_sm = std::max(0, std::min(json_int(it->second, "grid_per_sm", k->grid_per_sm), stats_blocks_per_sm));
     k->order = json_int(it->second, "order", k->order) ? 1 : 0;
     return true;
 }
@@ -489,7 +494,10 @@ void MultiEngine::tune_store(const std::string& key, const MultiKnobs& k, double
     char buf[160];
     snprintf(buf, sizeof(buf), "{\"grid_per_sm\":%d, \"order\":%d, \"ms\":%.4f}", k.grid_per_sm, k.order, ms);
     m[key] = buf;
-    const std::string tmp = tune_path + ".tmp";
+    // a temporary file of this process's own, renamed over the cache: concurrent writers (ranks of
+    // one job, other jobs sharing the file) never interleave their writes in one file
+    const std::string tmp = tune_path + ".tmp." + std::to_string((long long)getpid()) + "." +
+                            std::to_string((unsigned long long)std::hash<std::thread::id>{}(std::this_thread::get_id()));
     {
         std::ofstream f(tmp, std::ios::trunc);
         if (!f) return;

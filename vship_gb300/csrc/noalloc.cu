@@ -9,13 +9,17 @@
 // allocating library routine.
 //
 // The array is part of this library's device code: every GPU that loads that code keeps its
-// 32 MiB until the process exits. Its device address is looked up once per device with
-// cudaGetSymbolAddress (the name of the array in host code is only a host-side stand-in), on
-// the first call made on that device, which also uploads the device's constant tables. All
-// calls on one device share the array and it keeps the last call's contents; the kernels write
-// every scratch element they later read, so nothing needs clearing. Calls whose GPU work
-// overlaps -- on different streams, or from several host threads -- race on the array: order
-// them on one stream or wait between them.
+// 32 MiB until the process exits. CUDA loads a library's device code lazily by default
+// (CUDA_MODULE_LOADING=LAZY), so the 32 MiB is committed on a device by the first call made on
+// it: that call looks the array's device address up with cudaGetSymbolAddress (the name of the
+// array in host code is only a host-side stand-in), which loads the code and commits the
+// array, and uploads the device's constant tables. A caller with a fixed memory plan makes that
+// first call at start-up, before it fixes its budget and before any stream capture; if the
+// device has no room left for the array, that call returns Vship_OutOfVRAM and a later call
+// tries again. All calls on one device share the array and it keeps the last call's contents;
+// the kernels write every scratch element they later read, so nothing needs clearing. Calls
+// whose GPU work overlaps -- on different streams, or from several host threads -- race on the
+// array: order them on one stream or wait between them.
 #include "../../include/VshipAPI.h"
 
 #include "common.cuh"
@@ -42,7 +46,11 @@ int scratch_for_current_device(int dev, unsigned char** out) {
     if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) return vship::E_BAD_DEVICE_CODE;
+        if (e != cudaSuccess || !p) {
+            // Clear the failed call's error so that no later CUDA call reports it as its own.
+            cudaGetLastError();
+            return e == cudaErrorMemoryAllocation ? vship::E_OUT_OF_VRAM : vship::E_BAD_DEVICE_CODE;
+        }
         int rc = vship::ssimu2_prepare_device();
         if (rc) return rc;
         g_scratch_ptr[dev] = static_cast<unsigned char*>(p);

@@ -110,6 +110,10 @@ int Server::set_yuv_format(int bits, int ssw, int ssh, int matrix, int range, in
         if (!make_yuv_params(bits, ssw, ssh, matrix, range, loc, rh[r], &p[r], transfer, primaries))
             return E_BAD_POINTER;
     std::lock_guard<std::mutex> g(mu);
+    // The source cache is keyed by (metric, resolution, source key), not by format: state decoded
+    // under one format must never be scored against candidates of another, so the format is
+    // fixed once the first request has been submitted.
+    if (n_submitted > 0) return E_BAD_POINTER;
     for (int r = 0; r < nres; r++) yuv_r[r] = p[r];
     return E_OK;
 }
