@@ -66,7 +66,7 @@ def total_scale_pixels(w: int, h: int) -> int:
 # Algorithmic bytes of the dominant kernels, per frame pair (FP32 planes):
 #   ssimu2_stats reads both XYB pyramids once: 2 images x 3 channels x 4 B x T pixels.
 #   butter_diff reads the 20 band planes (LF vals, MF, HF, UHF of both images) once and writes
-#   4 planes (AC sum, DC sum, two mask precomputes) at each of the two scales.
+#   2 planes (AC sum, DC sum) at each of the two scales.
 def ssimu2_stats_bytes(w, h):
     return 2 * 3 * 4 * total_scale_pixels(w, h)
 
@@ -88,7 +88,7 @@ def fp32_peak_tflops(clock_mhz):
 def butter_diff_bytes(w, h):
     n = w * h
     nh = ((w - 1) // 2 + 1) * ((h - 1) // 2 + 1)
-    return 24 * 4 * (n + nh)
+    return 22 * 4 * (n + nh)
 
 
 def kernel_bytes_per_pair(kind, w, h, in_bytes):
@@ -107,8 +107,8 @@ def kernel_bytes_per_pair(kind, w, h, in_bytes):
             "butter_lf_v": 2 * 48 * ns,       # 3 blurred + 3 XYB in, D and LF vals out
             "butter_hblur_mf": 2 * 24 * ns,
             "butter_mf_v": 2 * 40 * ns,       # 3 blurred + 2 D in, 2 HF_pre + 3 MF out
-            "butter_hf": 2 * 24 * ns,         # 2 HF_pre in, HF and UHF out
-            "butter_diff": 96 * ns,           # 20 band planes in, 4 pair planes out
+            "butter_hf": 2 * 28 * ns,         # 2 HF_pre in, HF, UHF and the mask precompute out
+            "butter_diff": 88 * ns,           # 20 band planes in, 2 pair planes out
             "butter_mask_blur": 20 * ns,      # 2 mask precomputes + AC in, blurred mask + AC out
             "butter_diffmap": 16 * ns + 4 * nh}
 
@@ -140,7 +140,7 @@ def measured_peaks():
 # 3840x2160 pairs does.
 NCU_DRAM_BYTES_PER_PAIR = {
     "ssimu2_stats": (7962.84e6 + 7.55e6) / 120,
-    "butter_diff": (2933.67e6 + 568.13e6 + 11811.06e6 + 2325.37e6) / 15,
+    "butter_diff": (2488.55e6 + 250.61e6 + 9955.46e6 + 1017.72e6) / 15,
 }
 
 

@@ -99,11 +99,10 @@ enum : int {
     I_HF = 12,    // 12..13 HF (X, Y)
     I_UHF = 14,   // 14..15 UHF (X, Y)
     NIMG = 16,
+    I_PRE = 2,    // 2      the image's mask precompute (hf), in the dead TMP[2] plane
     // pair planes, inside the distorted image's dead TMP and XYB planes
     Q_SAC = 0,    // sum of AC terms            } written by diff
     Q_SDC = 1,    // sum of DC terms            }
-    Q_PRE0 = 2,   // mask precompute, image 0   }
-    Q_PRE1 = 3,   // mask precompute, image 1   }
     Q_B0 = 4,     // blurred mask of image 0 (mask_blur)
     Q_DIFF = 5    // diffmap of this scale (diffmap)
 };
@@ -589,7 +588,21 @@ __global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restri
     }
 }
 
-// HF / UHF split (separatefrequencies.hpp:117-133,189-200). grid (ceil(w/32), ceil(h/48), nimages)
+// maskinit + diffPrecompute (maskPsycho.hpp:3-40) of one image: sqrt(m + b) - sqrt(b) evaluated as
+// m / (sqrt(m + b) + sqrt(b)), the same value without the cancellation.
+__device__ __forceinline__ float mask_precompute(float hf_x, float uhf_x, float hf_y, float uhf_y) {
+    const float mul = 6.19424080439f;
+    const float bias = mul * 12.61050594197f;
+    const float xd = (uhf_x + hf_x) * 2.5f;
+    const float yd = uhf_y * 0.4f + hf_y * 0.4f;
+    const float mk = mul * sqrt_nr(xd * xd + yd * yd);
+    return div_nr(mk, sqrt_nr(mk + bias) + sqrtf(bias));
+}
+
+// HF / UHF split (separatefrequencies.hpp:117-133,189-200) and the image's mask precompute, which
+// depends on its own HF and UHF bands only (maskPsycho.hpp:3-40): computed here once per image
+// from the FP32 band values (an image shared by several pairs is not recomputed per pair).
+// grid (ceil(w/32), ceil(h/48), nimages)
 template <bool HB>
 __global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
@@ -605,6 +618,7 @@ __global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restr
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
+    float hfx[6], uhfx[6];  // the X bands, kept for the mask precompute
 #pragma unroll
     for (int c = 0; c < 2; c++) {
         const float* in = sm + c * TB_RAW;
@@ -616,23 +630,26 @@ __global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restr
 #pragma unroll
         for (int o = 0; o < 6; o++) {
             const int x = x0 + vc, y = y0 + 6 * vg + o;
+            float hf = blr[o], uhf = pre[o];
+            if (c == 0) {
+                uhf -= hf;
+                hf = remove_range(hf, 1.5f);
+                uhf = remove_range(uhf, 0.04f);
+                hfx[o] = hf;
+                uhfx[o] = uhf;
+            } else {
+                hf = maximum_clamp(hf, 28.4691806922f);
+                uhf -= hf;
+                uhf = maximum_clamp(uhf, 5.19175294647f);
+                uhf *= 2.69313763794f;
+                hf *= 2.155f;
+                hf = amplify_range(hf, 0.132f);
+            }
             if (x < S.w && y < S.h) {
-                float hf = blr[o], uhf = pre[o];
-                if (c == 0) {
-                    uhf -= hf;
-                    hf = remove_range(hf, 1.5f);
-                    uhf = remove_range(uhf, 0.04f);
-                } else {
-                    hf = maximum_clamp(hf, 28.4691806922f);
-                    uhf -= hf;
-                    uhf = maximum_clamp(uhf, 5.19175294647f);
-                    uhf *= 2.69313763794f;
-                    hf *= 2.155f;
-                    hf = amplify_range(hf, 0.132f);
-                }
                 const int64_t i = (int64_t)y * S.p + x;
                 band_store<HB>(ib, g, S, img, I_HF + c, i, hf);
                 band_store<HB>(ib, g, S, img, I_UHF + c, i, uhf);
+                if (c == 1) iplane(ib, g, S, img, I_PRE)[i] = mask_precompute(hfx[o], uhfx[o], hf, uhf);
             }
         }
     }
@@ -723,25 +740,38 @@ __device__ __forceinline__ float malta_pre(float a, float b, const MaltaMap& m) 
 constexpr int DF_TW = 32, DF_TH = 64, DF_H = 4;
 constexpr int DF_IW = DF_TW + 2 * DF_H, DF_IH = DF_TH + 2 * DF_H;  // 40 x 72
 
-// Sliding 9x9 register window down one column: rows are loaded as they are first needed and
-// die after their last pattern, so about 81 values are live at a time.
+// Sliding register window down one column. The patterns of both units reach columns
+// -2..2 at rows -4 and +4 of the window, -3..3 at rows -3 and +3 and -4..4 in between, so each
+// sample is loaded when the first output needs it and dies after the last: a row enters the
+// window with its five central columns, gains the next two a row later and the outer two a row
+// after that, and loses them in the reverse order, about 69 values live instead of 81.
+__device__ __forceinline__ constexpr int malta_reach(int dy) {
+    return (dy == 4 || dy == -4) ? 2 : (dy == 3 || dy == -3) ? 3 : 4;
+}
 template <bool HF>
-__device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r0, int c, float res[8]) {
+__device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r0, int c, float* __restrict__ acc) {
     float win[16][9];
 #pragma unroll
-    for (int r = 0; r < 16; r++) {
+    for (int o = 0; o < 8; o++) {
 #pragma unroll
-        for (int j = 0; j < 9; j++) win[r][j] = Dt[(r0 + r) * DF_IW + c + j];
-        if (r >= 8) {
-            const int o = r - 8;
-            float ret = 0.0f;
-            if (HF) {
-                MALTA_HF_BODY
-            } else {
-                MALTA_LF_BODY
+        for (int r = o; r <= o + 8; r++) {
+            const int dy = r - o - 4;
+            const int reach = malta_reach(dy);
+            // the reach this row had for the previous output (-1: not in that window)
+            const int prev = (o == 0 || r == o + 8) ? -1 : malta_reach(dy + 1);
+#pragma unroll
+            for (int j = 0; j < 9; j++) {
+                const int dx = j - 4 < 0 ? 4 - j : j - 4;
+                if (dx <= reach && dx > prev) win[r][j] = Dt[(r0 + r) * DF_IW + c + j];
             }
-            res[o] = ret;
         }
+        float ret = 0.0f;
+        if (HF) {
+            MALTA_HF_BODY
+        } else {
+            MALTA_LF_BODY
+        }
+        acc[o * 256] += ret;
     }
 }
 #undef W
@@ -755,10 +785,25 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 // With half-band storage the raw tiles are FP16 rows of DFH_P halves staged from x0 - 8 (16-byte
 // chunks of 8 halves), and the window's column c sits at half c + 4 of its row.
 constexpr int DF_RAW = DF_IH * DF_IW;
-constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW + 8 * 256) * 4;
+constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW + 2 * 8 * 256) * 4;
 constexpr int DFH_P = 56;                   // 48 staged halves + 8 of padding (7 quads per row)
 constexpr int DFH_RAWF = DF_IH * DFH_P / 2;  // one FP16 raw tile, in floats
-constexpr int kDiffSmemH = (4 * DFH_RAWF + DF_RAW + 8 * 256) * 4;
+constexpr int kDiffSmemH = (4 * DFH_RAWF + DF_RAW + 2 * 8 * 256) * 4;
+
+// L2AsymDiff's two terms for one pixel (simplerdiff.hpp:61-100), added to acc in the
+// reference's order. The two sign branches are one, on s2 mirrored to s1's side (as in
+// malta_pre): s2 + too_small == too_small - (-s2) and -s2 - too_big are the same IEEE operations;
+// outside both ranges v = 0 adds exactly nothing.
+__device__ __forceinline__ void l2asym_add(float& acc, float s1, float s2, float w_gt, float w_lt) {
+    constexpr DConst k04 = dconst(0.4);
+    const float diff = s1 - s2;
+    acc += w_gt * diff * diff;
+    const float fabs0 = fabsf(s1);
+    const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
+    const float s2m = s1 < 0 ? -s2 : s2;
+    const float v = s2m < too_small ? too_small - s2m : (s2m > too_big ? s2m - too_big : 0.0f);
+    acc += w_lt * v * v;
+}
 
 template <bool HB>
 __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
@@ -771,10 +816,12 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * DF_TW, y0 = blockIdx.y * DF_TH;
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    float* accY = Dt + DF_RAW;  // [8][256]: the Y maps' sums while the X maps run
-    float ac[8];
+    // [channel Y, X][8 outputs][256 threads]: each thread's sums, kept in shared memory rather than
+    // registers so that the Malta window has the register file to itself
+    float* accs = Dt + DF_RAW + threadIdx.x;
 #pragma unroll
-    for (int o = 0; o < 8; o++) ac[o] = 0.f;
+    for (int o = 0; o < 16; o++) accs[o * 256] = 0.f;
+    const DiffParams& P = c_dp;
     // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X. Each channel's
     // three maps are summed in that order, so the Y maps run first (m = 0, 2, 4) and the X maps
     // after (1, 3, 5): the same sums, with one channel's accumulators live at a time.
@@ -787,6 +834,12 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         else
             stage_tile_t<DF_IH, DF_IW / 4>(dst, DF_IW, (const float*)iplane(ib, g, S, img, id), S.p, S.w, S.h,
                                            x0 - DF_H, y0 - DF_H);
+    };
+    // the staged sample at this thread's output (column vc, row 8*vg + o of the tile)
+    auto center = [&](const float* tile, int o) {
+        if (HB)
+            return __half2float(reinterpret_cast<const __half*>(tile)[(8 * vg + o + DF_H) * DFH_P + vc + DF_H + 4]);
+        return tile[(8 * vg + o + DF_H) * DF_IW + vc + DF_H];
     };
     stage(sm, i0, plane_id(0));
     stage(sm + RAWF, i1, plane_id(0));
@@ -835,81 +888,50 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
                                                                malta_pre(a.z, b.z, mm), malta_pre(a.w, b.w, mm));
             }
         }
-        __syncthreads();
-        float res[8];
-        if (m < 2) malta_column<true>(Dt, 8 * vg, vc, res);
-        else malta_column<false>(Dt, 8 * vg, vc, res);
-#pragma unroll
-        for (int o = 0; o < 8; o++) ac[o] += res[o];
-        if (t == 2) {
+        // The HF and MF maps' own L2 terms (simplerdiff.hpp:41-100; channel X for odd m, Y for
+        // even), from the bands already staged here, before the barrier after which the next
+        // staging may overwrite this buffer: L2AsymDiff of HF, L2 of MF. The reference adds them
+        // after all three maps of the channel; here they join the channel's sum between maps, a
+        // different order of the same FP32 additions.
+        float* acc = accs + (m & 1) * 8 * 256;  // this map's channel
+        if (m >= 2) {
+            const int c = (m & 1) ? 0 : 1;
 #pragma unroll
             for (int o = 0; o < 8; o++) {
-                accY[o * 256 + threadIdx.x] = ac[o];
-                ac[o] = 0.f;
+                const float s1 = center(r0, o), s2 = center(r1, o);
+                float a = acc[o * 256];
+                if (m < 4) {
+                    l2asym_add(a, s1, s2, P.l2asym_gt[c], P.l2asym_lt[c]);
+                } else {
+                    const float dm = s1 - s2;
+                    a += P.wmf[c] * dm * dm;
+                }
+                acc[o * 256] = a;
             }
         }
+        __syncthreads();
+        if (m < 2) malta_column<true>(Dt, 8 * vg, vc, acc);
+        else malta_column<false>(Dt, 8 * vg, vc, acc);
     }
     const int x = x0 + vc;
     if (x >= S.w) return;
-    const float mul = 6.19424080439f;
-    const float bias = mul * 12.61050594197f;
-    const float sqb = sqrtf(bias);
-    constexpr DConst k04 = dconst(0.4);
-    const DiffParams& P = c_dp;
+    // What the staged tiles do not hold: MF of the B channel (no Malta map; L2 only) and the LF
+    // values of all three channels (the DC terms).
 #pragma unroll
     for (int o = 0; o < 8; o++) {
         const int y = y0 + 8 * vg + o;
         if (y < S.h) {
             const int64_t i = (int64_t)y * S.p + x;
-            float acc[3] = {ac[o], accY[o * 256 + threadIdx.x], 0.f};
-            float dc[3] = {0.f, 0.f, 0.f};
-            float hf[2][2], uhf[2][2], mf[2][3], lf[2][3];
-#pragma unroll
-            for (int m = 0; m < 2; m++) {
-                const int im = m ? i1 : i0;
-#pragma unroll
-                for (int c = 0; c < 2; c++) {
-                    hf[m][c] = band_load<HB>(ib, g, S, im, I_HF + c, i);
-                    uhf[m][c] = band_load<HB>(ib, g, S, im, I_UHF + c, i);
-                }
-#pragma unroll
-                for (int c = 0; c < 3; c++) {
-                    mf[m][c] = band_load<HB>(ib, g, S, im, I_MF + c, i);
-                    lf[m][c] = __ldg(iplane(ib, g, S, im, I_LFV + c) + i);
-                }
-            }
+            const float dmb = band_load<HB>(ib, g, S, i0, I_MF + 2, i) - band_load<HB>(ib, g, S, i1, I_MF + 2, i);
+            const float acc_b = P.wmf[2] * dmb * dmb;
+            float dc[3];
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                if (c < 2) {  // L2AsymDiff (simplerdiff.hpp:263-293)
-                    const float s1 = hf[0][c], s2 = hf[1][c];
-                    const float diff = s1 - s2;
-                    acc[c] += P.l2asym_gt[c] * diff * diff;
-                    const float fabs0 = fabsf(s1);
-                    const float too_small = mul_dc(fabs0, k04), too_big = fabs0;
-                    const float wl = P.l2asym_lt[c];
-                    // the two sign branches as one on s2 mirrored to s1's side (as in malta_pre):
-                    // s2 + too_small == too_small - (-s2) and -s2 - too_big are the same IEEE
-                    // operations; outside both ranges v = 0 adds exactly nothing
-                    const float s2m = s1 < 0 ? -s2 : s2;
-                    const float v = s2m < too_small ? too_small - s2m : (s2m > too_big ? s2m - too_big : 0.0f);
-                    acc[c] += wl * v * v;
-                }
-                const float dm = mf[0][c] - mf[1][c];
-                acc[c] += P.wmf[c] * dm * dm;
-                const float dl = lf[0][c] - lf[1][c];
-                dc[c] += P.wlf[c] * dl * dl;
+                const float dl = __ldg(iplane(ib, g, S, i0, I_LFV + c) + i) - __ldg(iplane(ib, g, S, i1, I_LFV + c) + i);
+                dc[c] = P.wlf[c] * dl * dl;
             }
-            iplane(ib, g, S, i1, Q_SAC)[i] = acc[0] + acc[1] + acc[2];
+            iplane(ib, g, S, i1, Q_SAC)[i] = accs[(8 + o) * 256] + accs[o * 256] + acc_b;
             iplane(ib, g, S, i1, Q_SDC)[i] = dc[0] + dc[1] + dc[2];
-            // maskinit + diffPrecompute (maskPsycho.hpp:3-40). sqrt(m + b) - sqrt(b) is evaluated
-            // as m / (sqrt(m + b) + sqrt(b)): the same value without the cancellation.
-#pragma unroll
-            for (int m = 0; m < 2; m++) {
-                const float xd = (uhf[m][0] + hf[m][0]) * 2.5f;
-                const float yd = uhf[m][1] * 0.4f + hf[m][1] * 0.4f;
-                const float mk = mul * sqrt_nr(xd * xd + yd * yd);
-                iplane(ib, g, S, i1, Q_PRE0 + m)[i] = div_nr(mk, sqrt_nr(mk + bias) + sqb);
-            }
         }
     }
 }
@@ -920,13 +942,14 @@ __global__ void __launch_bounds__(256, 6) butter_mask_blur_kernel(float* const* 
                                                                   const int2* __restrict__ pimg, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* hb = sm + 2 * TB_RAW;
-    const int i1 = pimg[blockIdx.z].y;
+    const int2 pi = pimg[blockIdx.z];
+    const int i1 = pi.y;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
     float rxy[6];
     tile_masses_r8<2>(x0, y0, S.w, S.h, rxy);
-    tile_stage_r8(sm, iplane(ib, g, S, i1, Q_PRE0), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, i1, Q_PRE1), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(ib, g, S, pi.x, I_PRE), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, i1, I_PRE), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
