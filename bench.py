@@ -1000,6 +1000,10 @@ def bench_multi(v, args, ws, rank):
         "knobs": knobs,
         "kernel_share": {k: {"launches": n, "ms": round(t, 3), "share": round(t / total_ms, 4)}
                          for k, (n, t) in sorted(prof.items(), key=lambda x: -x[1][1])} if total_ms > 0 else {},
+        "kernel_share_how": ("one more step with every launch on one stream, each bracketed by CUDA events (the "
+                             "timed steps overlap the resolutions' chains on side streams; serialised, an event pair "
+                             "times its own kernel only)"),
+        "serialised_step_ms": total_ms,
         "gpu_launches": launches * args.steps,
         "clocks": clocks,
     }

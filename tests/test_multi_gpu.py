@@ -197,15 +197,25 @@ def test_multi_autotune_cache(vlib, tmp_path):
     got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
     k = sc.knobs()
     sc.free()
-    assert got == want
+    # The tuner may pick the other stats tile shape, whose vertical pass adds the same FP32 terms
+    # in another order: the same scores to rounding, bit for bit only with the per-pair shape.
+    plain = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2)  # untuned: the per-pair shape
+    default_shape = plain.knobs()["shape"]
+    plain.free()
+    assert k["shape"] in (0, 1)
+    if k["shape"] == default_shape:
+        assert got == want
+    else:
+        assert max(abs(g - w) for g, w in zip(got, want)) <= 1e-6, (got, want)
     assert k["source"] == "tuned"
     entries = json.load(open(cache))
     assert len(entries) == 1
     (key, val), = entries.items()
     assert key.startswith("ssimu2_multi_stats|") and val["grid_per_sm"] == k["grid_per_sm"]
     sc = vlib.MultiScorer(RES, ms, mp, vlib.MULTI_SSIMU2 | vlib.MULTI_AUTOTUNE, tune_cache=cache)
-    got, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
-    assert sc.knobs()["source"] == "cache" and got == want
+    got2, _ = _run(vlib, sc, b, vlib.MULTI_SSIMU2)
+    k2 = sc.knobs()
+    assert k2["source"] == "cache" and k2["shape"] == k["shape"] and got2 == got
     sc.free()
 
 

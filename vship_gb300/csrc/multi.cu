@@ -118,9 +118,13 @@ int MultiEngine::init(int nres_, const int* widths, const int* heights, const in
     if (flags & MULTI_SSIMU2) {
         int rc = ssimu2_multi_prepare();
         if (rc) return rc;
-        rc = ssimu2_multi_stats_blocks_per_sm((flags & MULTI_FP16) != 0, &stats_blocks_per_sm);
-        if (rc) return rc;
-        stats_blocks_per_sm = std::max(1, stats_blocks_per_sm);
+        for (int sh = 0; sh < 2; sh++) {
+            rc = ssimu2_multi_stats_blocks_per_sm((flags & MULTI_FP16) != 0, sh, &stats_bps[sh]);
+            if (rc) return rc;
+            stats_bps[sh] = std::max(1, stats_bps[sh]);
+        }
+        knobs.shape = ssimu2_default_stats_shape();
+        stats_blocks_per_sm = stats_bps[knobs.shape];
         knobs.grid_per_sm = stats_blocks_per_sm;
         const size_t cand_elem = (flags & MULTI_FP16) ? 2 : 4;
         for (int r = 0; r < nres; r++) {
@@ -395,18 +399,22 @@ int MultiEngine::enqueue(int npairs, cudaStream_t st) {
     // resolution's side stream (chunks of one resolution share its workspace, so they stay in
     // order), joined back into st. Kernels with different limits (the FMA-bound stats and diff
     // kernels, the memory-heavy vertical blurs) then fill each other's gaps.
+    // With per-kernel timing on (Vship_ProfileSetEnabled), everything runs in order on st: CUDA
+    // events bracketing a kernel then time that kernel alone, not whatever overlaps it on the
+    // side streams. The timed (graph) runs keep the fork.
+    const bool serial = prof_enabled();
     VSHIP_CUDA_TRY(cudaEventRecord(ev_fork, st));
     int rc = E_OK;
     int joins = 0;
     if (flags & MULTI_SSIMU2) {
-        cudaStream_t s2 = side[kMaxRes];
+        cudaStream_t s2 = serial ? st : side[kMaxRes];
         VSHIP_CUDA_TRY(cudaStreamWaitEvent(s2, ev_fork, 0));
         const bool fp16 = (flags & MULTI_FP16) != 0;
         rc = ssimu2_multi_pyramid(s_imgs_d, s_pitems_d, n_pitems_src, geoms_d, plan_intype, false, s2);
         if (!rc) rc = ssimu2_multi_pyramid(s_imgs_d, s_pitems_d + n_pitems_src, n_pitems_cand, geoms_d, plan_intype,
                                            fp16, s2);
         const int grid = knobs.grid_per_sm > 0 ? knobs.grid_per_sm * sms : n_sitems;
-        if (!rc) rc = ssimu2_multi_stats(s_pairs_d, s_sitems_d, n_sitems, geoms_d, fp16, grid, s2);
+        if (!rc) rc = ssimu2_multi_stats(s_pairs_d, s_sitems_d, n_sitems, geoms_d, fp16, grid, knobs.shape, s2);
         if (!rc) rc = ssimu2_multi_finalize(s_pairs_d, npairs, geoms_d, s2);
         VSHIP_CUDA_TRY(cudaEventRecord(ev_join[kMaxRes], s2));
         VSHIP_CUDA_TRY(cudaStreamWaitEvent(st, ev_join[kMaxRes], 0));
@@ -416,7 +424,7 @@ int MultiEngine::enqueue(int npairs, cudaStream_t st) {
     if (flags & MULTI_BUTTERAUGLI) {
         bool used[kMaxRes] = {};
         for (const BChunk& c : b_chunks) {
-            cudaStream_t sr = side[c.res];
+            cudaStream_t sr = serial ? st : side[c.res];
             if (!used[c.res]) {
                 VSHIP_CUDA_TRY(cudaStreamWaitEvent(sr, ev_fork, 0));
                 used[c.res] = true;
@@ -426,7 +434,7 @@ int MultiEngine::enqueue(int npairs, cudaStream_t st) {
             if (rc) return rc;
         }
         for (int r = 0; r < nres; r++)
-            if (used[r]) {
+            if (used[r] && !serial) {
                 VSHIP_CUDA_TRY(cudaEventRecord(ev_join[r], side[r]));
                 VSHIP_CUDA_TRY(cudaStreamWaitEvent(st, ev_join[r], 0));
                 joins++;
@@ -483,7 +491,8 @@ bool MultiEngine::tune_lookup(const std::string& key, MultiKnobs* k) {
     const auto it = m.find(key);
     if (it == m.end()) return false;
     // 0 means one CTA per work item; a corrupt or hand-edited entry is clamped to [0, occupancy]
-    k->grid_per_sm = std::max(0, std::min(json_int(it->second, "grid_per_sm", k->grid_per_sm), stats_blocks_per_sm));
+    k->shape = json_int(it->second, "shape", k->shape) ? 1 : 0;
+    k->grid_per_sm = std::max(0, std::min(json_int(it->second, "grid_per_sm", k->grid_per_sm), stats_bps[k->shape]));
     k->order = json_int(it->second, "order", k->order) ? 1 : 0;
     return true;
 }
@@ -492,7 +501,8 @@ void MultiEngine::tune_store(const std::string& key, const MultiKnobs& k, double
     if (tune_path.empty()) return;
     auto m = read_tune_file(tune_path);
     char buf[160];
-    snprintf(buf, sizeof(buf), "{\"grid_per_sm\":%d, \"order\":%d, \"ms\":%.4f}", k.grid_per_sm, k.order, ms);
+    snprintf(buf, sizeof(buf), "{\"grid_per_sm\":%d, \"order\":%d, \"shape\":%d, \"ms\":%.4f}", k.grid_per_sm,
+             k.order, k.shape, ms);
     m[key] = buf;
     // a temporary file of this process's own, renamed over the cache: concurrent writers (ranks of
     // one job, other jobs sharing the file) never interleave their writes in one file
@@ -520,15 +530,17 @@ int MultiEngine::autotune(int npairs, cudaStream_t st) {
     VSHIP_CUDA_TRY(cudaEventCreate(&e1));
     MultiKnobs best = knobs;
     double best_ms = 1e30;
+    // every tile shape x work order x persistent grid (0 = one CTA per item)
     for (int order = 0; order < 2 && !rc; order++) {
         knobs.order = order;
         rc = upload_items(st);
-        for (int gps = 0; gps <= stats_blocks_per_sm && !rc; gps++) {
+        for (int shape = 0; shape < 2 && !rc; shape++)
+        for (int gps = 0; gps <= stats_bps[shape] && !rc; gps++) {
             const int grid = gps > 0 ? gps * sms : n_sitems;
             double ms_min = 1e30;
             for (int rep = 0; rep < 4 && !rc; rep++) {
                 cudaEventRecord(e0, st);
-                rc = ssimu2_multi_stats(s_pairs_d, s_sitems_d, n_sitems, geoms_d, fp16, grid, st);
+                rc = ssimu2_multi_stats(s_pairs_d, s_sitems_d, n_sitems, geoms_d, fp16, grid, shape, st);
                 cudaEventRecord(e1, st);
                 if (cudaEventSynchronize(e1) != cudaSuccess) rc = E_BAD_DEVICE_CODE;
                 float ms = 0.f;
@@ -539,6 +551,7 @@ int MultiEngine::autotune(int npairs, cudaStream_t st) {
                 best_ms = ms_min;
                 best.grid_per_sm = gps;
                 best.order = order;
+                best.shape = shape;
             }
         }
     }
@@ -547,6 +560,7 @@ int MultiEngine::autotune(int npairs, cudaStream_t st) {
     (void)npairs;
     if (rc) return rc;
     knobs = best;
+    stats_blocks_per_sm = stats_bps[knobs.shape];
     knobs_source = "tuned";
     tune_store(tune_key(), knobs, best_ms);
     return upload_items(st);
@@ -567,8 +581,8 @@ int MultiEngine::set_yuv_format(int bits, int ssw, int ssh, int matrix, int rang
 
 std::string MultiEngine::knobs_json() const {
     char buf[160];
-    snprintf(buf, sizeof(buf), "{\"grid_per_sm\": %d, \"order\": %d, \"source\": \"%s\"}", knobs.grid_per_sm,
-             knobs.order, knobs_source);
+    snprintf(buf, sizeof(buf), "{\"grid_per_sm\": %d, \"order\": %d, \"shape\": %d, \"source\": \"%s\"}",
+             knobs.grid_per_sm, knobs.order, knobs.shape, knobs_source);
     return buf;
 }
 
@@ -599,12 +613,14 @@ int MultiEngine::compute(int nsrc, const FrameDesc* src, const int* src_res, int
         if (rc) return rc;
         if (flags & MULTI_SSIMU2) {
             knobs = MultiKnobs{};
-            knobs.grid_per_sm = stats_blocks_per_sm;
+            knobs.shape = ssimu2_default_stats_shape();
+            knobs.grid_per_sm = stats_bps[knobs.shape];
             knobs_source = "default";
             if (tune_lookup(tune_key(), &knobs))
                 knobs_source = "cache";
             else if (flags & MULTI_AUTOTUNE)
                 tune_now = true;
+            stats_blocks_per_sm = stats_bps[knobs.shape];
             rc = upload_items(st);
             if (rc) return rc;
         }

@@ -42,6 +42,7 @@ constexpr int kMaxRes = 8;
 struct MultiKnobs {
     int grid_per_sm = 2;  // persistent stats grid = grid_per_sm x SMs (0 = one CTA per item)
     int order = 0;        // 0 = source-tile-major (a source tile's candidates back to back), 1 = pair-major
+    int shape = 0;        // stats tile shape: 0 = 48-row chunks through a ring, 1 = 64-row chunks, carried halo
 };
 
 class MultiEngine {
@@ -86,7 +87,8 @@ private:
     int2* s_sitems_d = nullptr;
     int n_pitems_src = 0, n_pitems_cand = 0, n_sitems = 0;
     size_t cap_pitems = 0, cap_sitems = 0;
-    int stats_blocks_per_sm = 1;
+    int stats_blocks_per_sm = 1;  // resident stats CTAs per SM for the current knobs' shape
+    int stats_bps[2] = {1, 1};    // ... for each tile shape
     // Butteraugli state: one image/pair engine per resolution, run over chunks
     struct BChunk {
         int res, img_off, nimg, pair_off, npairs;

@@ -51,7 +51,7 @@ int Server::create(int nres_, const int* widths, const int* heights, int intype_
     if (!rc) rc = butter_prepare_device();
     if (rc) return rc;
     int bps = 1;
-    rc = ssimu2_multi_stats_blocks_per_sm(!(flags & SERVE_FP32_CANDIDATES), &bps);
+    rc = ssimu2_multi_stats_blocks_per_sm(!(flags & SERVE_FP32_CANDIDATES), ssimu2_default_stats_shape(), &bps);
     if (rc) return rc;
     stats_grid = std::max(1, bps) * sms;
     VSHIP_CUDA_TRY(vship_malloc((void**)&sgeom_d, sizeof(Ssimu2Geom) * nres));
@@ -487,7 +487,7 @@ int Server::launch(Batch* b) {
         auto* sit = reinterpret_cast<const int2*>(dtab + t_sit);
         rc = ssimu2_multi_pyramid(imgs, pit, (int)n_pitems_src, sgeom_d, intype, false, st);
         if (!rc) rc = ssimu2_multi_pyramid(imgs, pit + n_pitems_src, (int)n_pitems_cand, sgeom_d, intype, fp16, st);
-        if (!rc) rc = ssimu2_multi_stats(pairs, sit, (int)n_sitems, sgeom_d, fp16, stats_grid, st);
+        if (!rc) rc = ssimu2_multi_stats(pairs, sit, (int)n_sitems, sgeom_d, fp16, stats_grid, ssimu2_default_stats_shape(), st);
         if (!rc) rc = ssimu2_multi_finalize(pairs, np_s2, sgeom_d, st);
     }
     for (const BGroup& G : bg) {

@@ -29,6 +29,9 @@ namespace vship {
 // ssimu2/gaussianblur.hpp:7-18 builds them.
 __constant__ float c_s2_k[17];
 __constant__ float c_s2_I[18];
+// 1 / (I[end] - I[beg]) for beg in 0..8 and end in 9..17: the inverse in-bounds mass of every
+// window a border can cut, so the renormalisation is a table load instead of a division
+__constant__ float c_s2_invm[9][9];
 __constant__ f2_t c_s2_k2[17];  // {k, k} pairs for the f32x2 FMA
 // SSIMULACRA2 feature weights (ssimu2/score.hpp:272-379), FP64.
 __constant__ double c_s2_w[108];
@@ -66,6 +69,10 @@ static int upload_constants_once() {
     }
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k, k, sizeof(k)));
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_I, I, sizeof(I)));
+    float invm[9][9];
+    for (int b = 0; b < 9; b++)
+        for (int e = 0; e < 9; e++) invm[b][e] = 1.0f / (I[9 + e] - I[b]);
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_invm, invm, sizeof(invm)));
     float k2[34];
     for (int i = 0; i < 17; i++) k2[2 * i] = k2[2 * i + 1] = k[i];
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k2, k2, sizeof(k2)));
@@ -292,7 +299,9 @@ __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
     // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
     const int beg = max(0, pos - 8) - (pos - 8);
     const int end = min(extent, pos + 9) - (pos - 8);
-    return 1.0f / (c_s2_I[end] - c_s2_I[beg]);
+    // the same IEEE quotient as 1 / (I[end] - I[beg]); positions past the edge (whose outputs are
+    // never pooled) are clamped onto the table
+    return c_s2_invm[beg][max(end - 9, 0)];
 }
 
 // FP16 delta tile: 64 rows x 48 halves, row pitch 56 halves (7 quads: conflict-free 16-byte reads)
@@ -528,7 +537,281 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
     }
 }
 
-// grid (tiles_total, npairs), dynamic smem kStatsSmem
+// ------------------------------------------------------------------------------------------
+// Second tile shape of the stats kernel: the same 32 x 192 segments, walked in 64-row chunks.
+// The horizontal pass writes a column-major buffer of 80 rows (the chunk's 64 and the 8-row
+// halos) instead of the ring, and the 16 rows a chunk shares with the next are carried over
+// (copied from buffer rows 64..79 to 0..15) rather than blurred again, so every chunk after the
+// first blurs exactly 64 new rows: one 8-row block per warp, all 8 warps busy (the ring shape
+// leaves 2 of 8 warps idle in that pass). The vertical pass gives each thread one column and 8
+// consecutive output rows; it streams the 24 buffer rows of its window once (12 16-byte loads per
+// moment pair) and scatters each into the 8 outputs it feeds. Fewer chunks and no idle warps
+// halve the barrier waits; the larger window costs registers. The batched form's autotuner
+// chooses between the two shapes per workload.
+constexpr int SC_TH = 64;
+constexpr int SC_IH = SC_TH + 2 * ST_R;  // 80 raw rows per chunk (image rows ty0 - 8 ..)
+constexpr int SC_RAW = SC_IH * ST_RP;    // one raw tile
+constexpr int SC_WIN = SC_TH / 8 + 2 * ST_R;  // 24 buffer rows per vertical window
+// column x of a buffer plane starts at float pair x * SC_HP + 8 * (x / 8); SC_HP = 82 pairs is 41
+// quads, odd, so the 16-byte loads of 8 neighbouring columns hit distinct bank quads, and the
+// 8-pair gap between column groups keeps a half-warp's 8-byte stores of two groups apart
+constexpr int SC_HP = 82;
+constexpr int SC_HPLANE = ST_TW * SC_HP + 8 * (ST_TW / 8 - 1);
+// smem: the 2 raw images, two float-pair planes {m1, m2} and {s11 + s22, s12}, the per-warp
+// pools: 74.4 KB, still three CTAs per SM
+constexpr int kStatsSmemC = (2 * SC_RAW + 4 * SC_HPLANE + 3 * 8 * 6) * 4;
+static_assert(ST_SEG % SC_TH == 0, "both shapes walk the same segments");
+
+template <bool DELTA>
+__device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, const void* __restrict__ im2v,
+                                               int64_t pe, const Ssimu2Level& L, int lt, float* __restrict__ out,
+                                               int stride) {
+    extern __shared__ __align__(16) float sm[];
+    float* raw = sm;                  // [image][80][52]
+    float* hb = sm + 2 * SC_RAW;      // [2 pair planes][32 columns of 82 rows, 8-pair gaps]
+    float* red = hb + 4 * SC_HPLANE;  // [3 channels][8 warps][6 pools]
+    const float* im2 = static_cast<const float*>(im2v);
+    const __half* im2h = static_cast<const __half*>(im2v);
+    const int tx0 = (lt % L.tiles_x) * ST_TW;
+    const int sy0 = (lt / L.tiles_x) * ST_SEG;
+    const int nchunk = (min(ST_SEG, L.h - sy0) + SC_TH - 1) / SC_TH;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool x_inside = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w;
+    // H pass: output columns 8*hg .. 8*hg+7 of 8 consecutive raw rows per warp x 4 column groups.
+    const int hg = lane >> 3, hr = lane & 7;
+    // V pass: column vc, output rows 8*vg .. 8*vg+7 of the chunk; both passes' border
+    // renormalisations (gaussianblur.hpp:63-92) applied there as one product.
+    const int vc = tid & 31, vg = tid >> 5;
+    const float rxv = s2_inv_mass(tx0 + vc, L.w);
+    const float rx_in = rxv * (1.0f / (c_s2_I[17] - c_s2_I[0]));
+    float* r1 = raw;
+    float* r2 = raw + SC_RAW;
+    f2_t* const hp1 = reinterpret_cast<f2_t*>(hb);
+    f2_t* const hp2 = reinterpret_cast<f2_t*>(hb + 2 * SC_HPLANE);
+
+#pragma unroll 1
+    for (int c = 0; c < 3; c++) {
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float shift = 0.f;
+#pragma unroll 1
+        for (int k = 0; k < nchunk; k++) {
+            const int ty0 = sy0 + k * SC_TH;
+            // the first chunk stages raw rows 0..79 (image rows ty0 - 8 ..); later chunks rows
+            // 8..79 only (rows 0..7 fed the carried rows and no output of this chunk)
+            const int rlo = k == 0 ? 0 : ST_R;
+            if (k == 0) {
+                stage_tile_t<SC_IH, 12>(r1, ST_RP, im1 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0 - ST_R, ty0 - ST_R);
+                if (DELTA)
+                    stage_tile_t<SC_IH, 6>(reinterpret_cast<__half*>(r2), ST_DP, im2h + (int64_t)c * pe, L.pitch, L.w,
+                                           L.h, tx0 - ST_R, ty0 - ST_R);
+                else
+                    stage_tile_t<SC_IH, 12>(r2, ST_RP, im2 + (int64_t)c * pe, L.pitch, L.w, L.h, tx0 - ST_R,
+                                            ty0 - ST_R);
+            } else {
+                stage_tile_t<SC_IH - ST_R, 12>(r1 + ST_R * ST_RP, ST_RP, im1 + (int64_t)c * pe, L.pitch, L.w, L.h,
+                                               tx0 - ST_R, ty0);
+                if (DELTA)
+                    stage_tile_t<SC_IH - ST_R, 6>(reinterpret_cast<__half*>(r2) + ST_R * ST_DP, ST_DP,
+                                                  im2h + (int64_t)c * pe, L.pitch, L.w, L.h, tx0 - ST_R, ty0);
+                else
+                    stage_tile_t<SC_IH - ST_R, 12>(r2 + ST_R * ST_RP, ST_RP, im2 + (int64_t)c * pe, L.pitch, L.w,
+                                                   L.h, tx0 - ST_R, ty0);
+            }
+            cp_async_commit();
+            cp_async_wait<0>();
+            __syncthreads();
+            // the per-segment shift and the border treatment of the ring shape (stats_tile)
+            if (k == 0) shift = r1[ST_R * ST_RP + ST_R];
+            if (!(x_inside && ty0 >= ST_R && ty0 + SC_TH + ST_R <= L.h)) {
+                for (int e = tid + rlo * ST_IW; e < SC_IH * ST_IW; e += 256) {
+                    const int r = e / ST_IW, col = e - r * ST_IW;
+                    const int gx = tx0 - ST_R + col, gy = ty0 - ST_R + r;
+                    if (gx < 0 || gx >= L.w || gy < 0 || gy >= L.h) {
+                        r1[r * ST_RP + col] = shift;
+                        if (!DELTA) r2[r * ST_RP + col] = shift;  // FP16 deltas arrive as zeros there
+                    }
+                }
+                __syncthreads();
+            }
+            // Horizontal pass: raw rows 0..79 of the first chunk (ten 8-row blocks; warps 0 and 1
+            // take two), rows 16..79 of later chunks (one block per warp); raw row r -> buffer row r.
+            const int nblk = k == 0 ? SC_IH / 8 : SC_TH / 8;
+            const int blk0 = k == 0 ? 0 : 2;
+#pragma unroll 1
+            for (int bi = warp; bi < nblk; bi += 8) {
+                const int rr = 8 * (blk0 + bi) + hr;
+                f2_t h1[8], h2[8];
+                const f2_t z2 = f2_pack(0.f, 0.f);
+#pragma unroll
+                for (int o = 0; o < 8; o++) {
+                    h1[o] = z2;
+                    h2[o] = z2;
+                }
+                const float* ra = r1 + rr * ST_RP + 8 * hg;
+                const float* rb = r2 + rr * ST_RP + 8 * hg;
+                float dl[24];  // DELTA: the 24 deltas of this thread's window
+                if (DELTA) {
+                    const __half* rd = reinterpret_cast<const __half*>(r2) + rr * ST_DP + 8 * hg;
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        const uint4 v4 = *reinterpret_cast<const uint4*>(rd + 8 * q);
+                        const __half2* hq = reinterpret_cast<const __half2*>(&v4);
+#pragma unroll
+                        for (int u = 0; u < 4; u++) {
+                            const float2 f = __half22float2(hq[u]);
+                            dl[8 * q + 2 * u] = f.x;
+                            dl[8 * q + 2 * u + 1] = f.y;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int j4 = 0; j4 < 6; j4++) {
+                    const float4 va = *reinterpret_cast<const float4*>(ra + 4 * j4);
+                    float4 vb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (!DELTA) vb = *reinterpret_cast<const float4*>(rb + 4 * j4);
+                    const float la[4] = {va.x, va.y, va.z, va.w};
+                    const float lb[4] = {vb.x, vb.y, vb.z, vb.w};
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const int j = 4 * j4 + u;
+                        const float a = la[u] - shift;
+                        const float b = DELTA ? a + dl[j] : lb[u] - shift;
+                        const f2_t p1 = f2_pack(a, b);
+                        const f2_t p2 = f2_pack(fmaf(a, a, b * b), a * b);
+#pragma unroll
+                        for (int o = 0; o < 8; o++) {
+                            const int i = j - o;  // tap index
+                            if (i >= 0 && i < 17) {
+                                h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
+                                h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
+                            }
+                        }
+                    }
+                }
+                f2_t* d1 = hp1 + 8 * hg * (SC_HP + 1) + rr;
+                f2_t* d2 = hp2 + 8 * hg * (SC_HP + 1) + rr;
+#pragma unroll
+                for (int o = 0; o < 8; o++) {
+                    d1[o * SC_HP] = h1[o];
+                    d2[o * SC_HP] = h2[o];
+                }
+            }
+            __syncthreads();
+            // vertical pass + maps: buffer rows 8*vg .. 8*vg+23 streamed once, each scattered into
+            // the 8 outputs it feeds
+            const bool rows_in = ty0 + 8 * vg >= ST_R && ty0 + 8 * vg + 7 + ST_R < L.h;
+            f2_t a1[8], a2[8];
+            {
+                const f2_t z2 = f2_pack(0.f, 0.f);
+#pragma unroll
+                for (int o = 0; o < 8; o++) {
+                    a1[o] = z2;
+                    a2[o] = z2;
+                }
+                const int cb = vc * SC_HP + 8 * (vc >> 3) + 8 * vg;  // even: 16-byte aligned
+                const ulonglong2* c1 = reinterpret_cast<const ulonglong2*>(hp1 + cb);
+                const ulonglong2* c2 = reinterpret_cast<const ulonglong2*>(hp2 + cb);
+#pragma unroll
+                for (int jj = 0; jj < SC_WIN / 2; jj++) {
+                    const ulonglong2 q1 = c1[jj];
+                    const ulonglong2 q2 = c2[jj];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int j = 2 * jj + h;
+                        const f2_t v1 = h ? q1.y : q1.x;
+                        const f2_t v2 = h ? q2.y : q2.x;
+#pragma unroll
+                        for (int o = 0; o < 8; o++) {
+                            const int i = j - o;
+                            if (i >= 0 && i < 17) {
+                                a1[o] = f2_fma(v1, c_s2_k2[i], a1[o]);
+                                a2[o] = f2_fma(v2, c_s2_k2[i], a2[o]);
+                            }
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                const int y = ty0 + 8 * vg + o, x = tx0 + vc;
+                if (x < L.w && y < L.h) {
+                    const float rxy = rows_in ? rx_in : rxv * s2_inv_mass(y, L.h);
+                    float m1, m2, mS, m12;
+                    f2_unpack(f2_mul(a1[o], f2_pack(rxy, rxy)), m1, m2);
+                    f2_unpack(f2_mul(a2[o], f2_pack(rxy, rxy)), mS, m12);
+                    const int so = (8 * vg + o + ST_R) * ST_RP + vc + ST_R;
+                    const float i1 = r1[so] - shift;
+                    const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(8 * vg + o + ST_R) * ST_DP +
+                                                                                                     vc + ST_R])
+                                           : r2[so] - shift;
+                    // the maps of the ring shape (stats_tile), term for term
+                    const float md = m1 - m2;
+                    const float num_m = fmaf(md, -md, 1.0f);
+                    const float hs = 0.5f * mS;
+                    const float s12 = fmaf(-m1, m2, m12);
+                    const float s11 = fmaf(-m1, m1, hs);
+                    const float s22 = fmaf(-m2, m2, hs);
+                    const float num_s = fmaf(s12, 2.0f, 0.0009f);
+                    const float denom = (s11 + s22) + 0.0009f;
+                    const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
+                    const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
+                    const float v1 = __fdividef(e2 - e1, e1 + 1.0f);
+                    const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
+                    const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
+                    acc[0] += d0;
+                    acc[1] += q0 * q0;
+                    acc[2] += d1;
+                    acc[3] += q1 * q1;
+                    acc[4] += d2;
+                    acc[5] += q2 * q2;
+                }
+            }
+            __syncthreads();  // the raw tiles and buffer rows are rewritten for the next chunk
+            if (k + 1 < nchunk) {
+                // carry buffer rows 64..79 to rows 0..15: 2 planes x 32 columns x 8 16-byte row
+                // pairs, two per thread (the next chunk's first barrier orders them before its
+                // horizontal pass writes rows 16..79)
+#pragma unroll
+                for (int q = tid; q < 2 * ST_TW * 8; q += 256) {
+                    f2_t* pl = q < ST_TW * 8 ? hp1 : hp2;
+                    const int e = q & (ST_TW * 8 - 1), x = e >> 3, rp = e & 7;
+                    ulonglong2* col = reinterpret_cast<ulonglong2*>(pl + x * SC_HP + 8 * (x >> 3));
+                    col[rp] = col[SC_TH / 2 + rp];
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 6; i++) {
+            const float v = warp_sum(acc[i]);
+            if (lane == 0) red[(c * 8 + warp) * 6 + i] = v;
+        }
+    }
+    __syncthreads();
+    if (tid < 18) {
+        const int pool = tid / 3, c = tid - pool * 3;
+        float v = 0.f;
+#pragma unroll
+        for (int w = 0; w < 8; w++) v += red[(c * 8 + w) * 6 + pool];
+        out[(int64_t)tid * stride] = v;
+    }
+}
+
+// tile shape 0: 48-row chunks through the ring (stats_tile); 1: 64-row chunks through the carry
+// buffer (stats_tile_c64). Both walk the same segments and write the same 18 sums per segment.
+template <int SHAPE, bool DELTA>
+__device__ __forceinline__ void stats_segment(const float* __restrict__ im1, const void* __restrict__ im2v,
+                                              int64_t pe, const Ssimu2Level& L, int lt, float* __restrict__ out,
+                                              int stride) {
+    if (SHAPE == 0) stats_tile<DELTA>(im1, im2v, pe, L, lt, out, stride);
+    else stats_tile_c64<DELTA>(im1, im2v, pe, L, lt, out, stride);
+}
+constexpr int stats_smem(int shape) { return shape == 0 ? kStatsSmem : kStatsSmemC; }
+// The per-pair entry points (and the no-allocation one, which must give their results bit for
+// bit) use one fixed shape, the faster at 1920x1080 on a GB300.
+constexpr int kPlainShape = 1;
+
+// grid (tiles_total, npairs), dynamic smem stats_smem(SHAPE)
+template <int SHAPE>
 __global__ void __launch_bounds__(256, 3) ssimu2_stats_kernel(const float* __restrict__ pyr,
                                                               float* __restrict__ partials, Ssimu2Geom g) {
     const int pair = blockIdx.y;
@@ -539,8 +822,8 @@ __global__ void __launch_bounds__(256, 3) ssimu2_stats_kernel(const float* __res
     const Ssimu2Level L = g.lv[s];
     const float* im1 = pyr + (int64_t)(pair * 2 + 0) * 3 * g.plane_elems + L.off;
     const float* im2 = pyr + (int64_t)(pair * 2 + 1) * 3 * g.plane_elems + L.off;
-    stats_tile<false>(im1, im2, g.plane_elems, L, t - g.tile_begin[s],
-                      partials + (int64_t)pair * 18 * g.tiles_total + t, g.tiles_total);
+    stats_segment<SHAPE, false>(im1, im2, g.plane_elems, L, t - g.tile_begin[s],
+                                partials + (int64_t)pair * 18 * g.tiles_total + t, g.tiles_total);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -605,7 +888,7 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) ssimu2_multi_pyrami
 }
 
 // persistent: CTA b takes items b, b + gridDim.x, ...; items {pair, tile}
-template <bool DELTA>
+template <bool DELTA, int SHAPE>
 __global__ void __launch_bounds__(256, 3) ssimu2_multi_stats_kernel(const Ssimu2MultiPair* __restrict__ pairs,
                                                                     const int2* __restrict__ items, int nitems,
                                                                     const Ssimu2Geom* __restrict__ geoms) {
@@ -619,8 +902,8 @@ __global__ void __launch_bounds__(256, 3) ssimu2_multi_stats_kernel(const Ssimu2
         const Ssimu2Level L = g.lv[s];
         const void* im2 = DELTA ? static_cast<const void*>(static_cast<const __half*>(P.cand) + L.off)
                                 : static_cast<const void*>(static_cast<const float*>(P.cand) + L.off);
-        stats_tile<DELTA>(P.src + L.off, im2, g.plane_elems, L, it.y - g.tile_begin[s], P.partials + it.y,
-                          g.tiles_total);
+        stats_segment<SHAPE, DELTA>(P.src + L.off, im2, g.plane_elems, L, it.y - g.tile_begin[s], P.partials + it.y,
+                                    g.tiles_total);
         __syncthreads();
     }
 }
@@ -666,7 +949,8 @@ int Ssimu2Engine::init(int64_t width, int64_t height, int max_pairs_) {
     geom = make_ssimu2_geom(w, h);
     int rc = upload_constants_once();
     if (rc) return rc;
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStatsSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel<kPlainShape>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        stats_smem(kPlainShape)));
     VSHIP_CUDA_TRY(vship_malloc((void**)&pyr, sizeof(float) * (size_t)geom.plane_elems * 3 * 2 * max_pairs));
     VSHIP_CUDA_TRY(vship_malloc((void**)&partials, sizeof(float) * (size_t)geom.tiles_total * 18 * max_pairs));
     VSHIP_CUDA_TRY(vship_malloc((void**)&scores, sizeof(double) * max_pairs));
@@ -706,7 +990,7 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
     dim3 g2((unsigned)geom.tiles_total, (unsigned)npairs);
     {
         ProfScope ps("ssimu2_stats", st);
-        ssimu2_stats_kernel<<<g2, 256, kStatsSmem, st>>>(pyr, partials, geom);
+        ssimu2_stats_kernel<kPlainShape><<<g2, 256, stats_smem(kPlainShape), st>>>(pyr, partials, geom);
     }
     {
         ProfScope ps("ssimu2_finalize", st);
@@ -722,7 +1006,8 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
 int ssimu2_prepare_device() {
     int rc = upload_constants_once();
     if (rc) return rc;
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kStatsSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel<kPlainShape>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        stats_smem(kPlainShape)));
     return E_OK;
 }
 
@@ -749,7 +1034,8 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
         case IN_YUV: ssimu2_pyramid_kernel<IN_YUV><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
         default: ssimu2_pyramid_kernel<IN_FLOAT><<<g1, 256, 0, st>>>(frames_scratch, pyr, geom, yp); break;
     }
-    ssimu2_stats_kernel<<<dim3((unsigned)geom.tiles_total, 1u), 256, kStatsSmem, st>>>(pyr, partials, geom);
+    ssimu2_stats_kernel<kPlainShape><<<dim3((unsigned)geom.tiles_total, 1u), 256, stats_smem(kPlainShape), st>>>(
+        pyr, partials, geom);
     ssimu2_finalize_kernel<<<1, 256, 0, st>>>(partials, out_score, geom);
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
@@ -761,16 +1047,28 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
 int ssimu2_multi_prepare() {
     int rc = ssimu2_prepare_device();
     if (rc) return rc;
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        kStatsSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        kStatsSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<false, 0>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, stats_smem(0)));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<true, 0>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, stats_smem(0)));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<false, 1>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, stats_smem(1)));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_multi_stats_kernel<true, 1>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, stats_smem(1)));
     return E_OK;
 }
 
-int ssimu2_multi_stats_blocks_per_sm(bool delta, int* blocks) {
-    VSHIP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        blocks, delta ? ssimu2_multi_stats_kernel<true> : ssimu2_multi_stats_kernel<false>, 256, kStatsSmem));
+int ssimu2_default_stats_shape() { return kPlainShape; }
+
+int ssimu2_multi_stats_blocks_per_sm(bool delta, int shape, int* blocks) {
+    if (shape == 0)
+        VSHIP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            blocks, delta ? ssimu2_multi_stats_kernel<true, 0> : ssimu2_multi_stats_kernel<false, 0>, 256,
+            stats_smem(0)));
+    else
+        VSHIP_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            blocks, delta ? ssimu2_multi_stats_kernel<true, 1> : ssimu2_multi_stats_kernel<false, 1>, 256,
+            stats_smem(1)));
     return E_OK;
 }
 
@@ -802,14 +1100,18 @@ int ssimu2_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items, int ni
 }
 
 int ssimu2_multi_stats(const Ssimu2MultiPair* pairs, const int2* items, int nitems, const Ssimu2Geom* geoms,
-                       bool delta, int grid, cudaStream_t st) {
+                       bool delta, int grid, int shape, cudaStream_t st) {
     if (nitems <= 0) return E_OK;
     const unsigned gr = (unsigned)std::max(1, std::min(grid, nitems));
     ProfScope ps("ssimu2_multi_stats", st);
-    if (delta)
-        ssimu2_multi_stats_kernel<true><<<gr, 256, kStatsSmem, st>>>(pairs, items, nitems, geoms);
-    else
-        ssimu2_multi_stats_kernel<false><<<gr, 256, kStatsSmem, st>>>(pairs, items, nitems, geoms);
+    const int smem = stats_smem(shape ? 1 : 0);
+    if (shape == 0) {
+        if (delta) ssimu2_multi_stats_kernel<true, 0><<<gr, 256, smem, st>>>(pairs, items, nitems, geoms);
+        else ssimu2_multi_stats_kernel<false, 0><<<gr, 256, smem, st>>>(pairs, items, nitems, geoms);
+    } else {
+        if (delta) ssimu2_multi_stats_kernel<true, 1><<<gr, 256, smem, st>>>(pairs, items, nitems, geoms);
+        else ssimu2_multi_stats_kernel<false, 1><<<gr, 256, smem, st>>>(pairs, items, nitems, geoms);
+    }
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
 }

@@ -82,13 +82,16 @@ struct Ssimu2MultiPair {
 };
 
 int ssimu2_multi_prepare();
-int ssimu2_multi_stats_blocks_per_sm(bool delta, int* blocks);
+// shape: the stats kernel's tile shape, 0 = 48-row chunks through a ring of horizontal-pass
+// rows, 1 = 64-row chunks through a carried buffer (same segments, same sums)
+int ssimu2_multi_stats_blocks_per_sm(bool delta, int shape, int* blocks);
 // items: {image, level-0 tile x, tile y, 0} in kPyrTile tiles, one CTA each. delta selects the FP16-delta store.
 int ssimu2_multi_pyramid(const Ssimu2MultiImage* imgs, const int4* items, int nitems, const Ssimu2Geom* geoms,
                          int intype, bool delta, cudaStream_t st);
 // Persistent: `grid` CTAs walk items {pair, tile} with stride grid.
 int ssimu2_multi_stats(const Ssimu2MultiPair* pairs, const int2* items, int nitems, const Ssimu2Geom* geoms,
-                       bool delta, int grid, cudaStream_t st);
+                       bool delta, int grid, int shape, cudaStream_t st);
+int ssimu2_default_stats_shape();  // the shape the per-pair entry points use
 int ssimu2_multi_finalize(const Ssimu2MultiPair* pairs, int npairs, const Ssimu2Geom* geoms, cudaStream_t st);
 
 }  // namespace vship
