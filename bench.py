@@ -274,7 +274,7 @@ def yuv_table(v, yuv, start, count):
     return v.device_frames_table(frames)
 
 
-def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands=False):
+def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands=False, fp16_deltas=False):
     """Batched device-resident throughput; returns (seconds for `steps` steps, profile dict, launches,
     results). half_bands: Butteraugli with its MF, HF and UHF bands stored as FP16."""
     import torch
@@ -284,7 +284,7 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands
     else:
         npairs, _, h, w = ref.shape
     if kind == "ssimu2":
-        eng = v.SSIMU2Batch(w, h, chunk)
+        eng = v.SSIMU2Batch(w, h, chunk, fp16_deltas=fp16_deltas)
         out = torch.zeros(npairs, dtype=torch.float64, device="cuda")
     else:
         eng = v.ButteraugliBatch(w, h, chunk, 2, 203.0, half_bands=half_bands)
@@ -699,6 +699,18 @@ def bench_workload(v, kind, args, ws, rank):
                      "flops_per_pair": ssimu2_stats_flops(w, h),
                      "peak_source": f"128 FP32 FMA lanes x SMs x {mhz:.0f} MHz (sampled clock)"}
     half = None
+    dres = None
+    if kind == "ssimu2" and not args.skip_half_bands:
+        # the distorted pyramids stored as FP16 deltas from the references' (Vship_SSIMU2Fp16Deltas)
+        dsec, dprof, _, dres = run_device(v, kind, ref16, dst16, args.steps, args.warmup, ws, chunk, fp16_deltas=True)
+        dsec = max_over_ranks(dsec, ws)
+        L = v.lib()
+        res_fp16 = {"value": npairs * ws * args.steps / dsec, "unit": "frame-pairs/s",
+                    "device_bytes_per_pair": int(L.Vship_SSIMU2DeviceBytesEx(w, h, 1, v.SSIMU2_FP16_DELTAS)),
+                    "device_bytes_per_pair_fp32": int(L.Vship_SSIMU2DeviceBytes(w, h, 1)),
+                    "kernel_ms": {k: round(t, 3) for k, (n, t) in sorted(dprof.items(), key=lambda x: -x[1][1])},
+                    "note": "distorted XYB pyramid as FP16 deltas from the reference's, all arithmetic FP32; "
+                            "error in error_vs_fp64"}
     hres = None
     if kind != "ssimu2" and not args.skip_half_bands:
         hsec, hprof, _, hres = run_device(v, kind, ref16, dst16, args.steps, args.warmup, ws, chunk, half_bands=True)
@@ -754,6 +766,8 @@ def bench_workload(v, kind, args, ws, rank):
     }
     if half:
         res["fp16_bands"] = half
+    if dres is not None:
+        res["fp16_deltas"] = res_fp16
     if refc is not None:
         rinfo, rscores = refc
         mine = dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy().reshape(-1, 3)
@@ -787,6 +801,8 @@ def bench_workload(v, kind, args, ws, rank):
         err = {"pairs": nx, "input": "RGB48 planes (the headline input)", "oracle": "FP64 oracle (oracle/)"}
         if kind == "ssimu2":
             forms = {"score_max_abs": dev_scores.numpy()}
+            if dres is not None:
+                forms["fp16_deltas_score_max_abs"] = dres.numpy()
         else:
             forms = {"fp32_planes_max_rel": dev_scores.numpy().reshape(-1, 3)}
             if hres is not None:
@@ -1217,7 +1233,7 @@ def main_ours(args):
         "yuv420p10": s2["yuv420p10"], "float32_rgb": s2["float32_rgb"], "input": s2["input"],
         "score_check": s2["score_check"],
         })
-    for k in ("reference_cuda", "error_vs_fp64", "cpu_baseline"):
+    for k in ("reference_cuda", "error_vs_fp64", "cpu_baseline", "fp16_deltas"):
         if k in s2:
             out[k] = s2[k]
     out["host_link"] = {"h2d_gbs": round(link, 1),
@@ -1313,7 +1329,8 @@ def main():
     ap.add_argument("--skip-ssimu2", action="store_true")
     ap.add_argument("--skip-multi", action="store_true")
     ap.add_argument("--skip-serving", action="store_true")
-    ap.add_argument("--skip-half-bands", action="store_true", help="skip the FP16-band Butteraugli run")
+    ap.add_argument("--skip-half-bands", action="store_true",
+                    help="skip the FP16 storage forms (Butteraugli FP16 bands, SSIMU2 FP16 deltas)")
     ap.add_argument("--error-pairs", type=int, default=8,
                     help="SSIMU2 pairs scored by the FP64 oracle for the headline's error")
     ap.add_argument("--butter-error-pairs", type=int, default=4,

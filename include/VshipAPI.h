@@ -295,6 +295,23 @@ EXPORTPREPROCESS Vship_Exception Vship_ButteraugliBatchInitEx(Vship_ButteraugliH
                                                               int max_pairs, int flags);
 EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytesEx(int width, int height, int max_pairs, int flags);
 
+/* SSIMU2 with the distorted image's XYB pyramid stored as FP16 -- no counterpart in the reference,
+ * whose pyramids are float3 arrays (src/ssimu2/main.hpp:107-151).
+ * With Vship_SSIMU2Fp16Deltas each pair's reference pyramid stays FP32 and the distorted image's
+ * is stored as half(distorted - reference), read back as reference + delta: identical samples
+ * stay identical and small distortions keep FP16's relative precision, while the pyramid bytes a
+ * pair writes and the stats kernel reads fall from 24 to 18 per pyramid element. All arithmetic
+ * stays FP32. Against the FP64 oracle the storage moves the score by about 1e-5 at 1920x1080 and
+ * up to 2e-4 at 480x270, within the 1e-3 SSIMULACRA2 tolerance; on frames of a few thousand
+ * pixels with heavy distortion it can reach 1.5e-3 (the coarsest scales hold a few pixels). Vship_SSIMU2InitEx is Vship_SSIMU2Init with flags (host-buffer
+ * Compute calls); Vship_SSIMU2BatchInitEx is Vship_SSIMU2BatchInit with flags; flags = 0 gives
+ * the FP32 pyramids of the plain functions. Other flag bits are refused (Vship_BadPointer). */
+typedef enum { Vship_SSIMU2Fp16Deltas = 1 } Vship_SSIMU2Flags;
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2InitEx(Vship_SSIMU2Handler* handler, int width, int height, int flags);
+EXPORTPREPROCESS Vship_Exception Vship_SSIMU2BatchInitEx(Vship_SSIMU2Handler* handler, int width, int height,
+                                                         int max_pairs, int flags);
+EXPORTPREPROCESS uint64_t Vship_SSIMU2DeviceBytesEx(int width, int height, int max_pairs, int flags);
+
 /* SSIMU2 for callers that cannot allocate GPU memory -- no counterpart in the reference.
  *
  * Programs that fix their GPU memory budget at start-up (real-time encoders, servers with a

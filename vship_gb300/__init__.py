@@ -29,6 +29,7 @@ EXCEPTION_NAMES = ["NoError", "OutOfVRAM", "OutOfRAM", "DifferingInputType", "No
 IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT, IN_YUV = 0, 1, 2, 3, 4
 IN_YUV420P10 = IN_YUV  # the default Y'CbCr format (10-bit 4:2:0, BT.709, limited, left siting)
 BUTTER_HALF_BANDS = 1  # Vship_ButterHalfBands: Butteraugli MF, HF and UHF bands stored as FP16
+SSIMU2_FP16_DELTAS = 1  # Vship_SSIMU2Fp16Deltas: the distorted pyramid as FP16 deltas from the reference's
 
 
 class VshipError(RuntimeError):
@@ -136,6 +137,9 @@ SIGNATURES = {
     "Vship_SSIMU2ComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
                                             ctypes.c_void_p]),
     "Vship_SSIMU2DeviceBytes": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_SSIMU2InitEx": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_SSIMU2BatchInitEx": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "Vship_SSIMU2DeviceBytesEx": (ctypes.c_uint64, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "Vship_ButteraugliBatchInit": (_E, [ctypes.POINTER(_H), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                         ctypes.c_int]),
     "Vship_ButteraugliComputeDeviceAsync": (_E, [_H, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
@@ -287,12 +291,18 @@ def _yuv_planes(frame, w, h, fmt=None):
 
 
 class SSIMU2Handler:
-    """One SSIMULACRA2 scorer for a fixed resolution (Vship_SSIMU2Init / Compute / Free)."""
+    """One SSIMULACRA2 scorer for a fixed resolution (Vship_SSIMU2Init / Compute / Free);
+    fp16_deltas=True stores the distorted image's pyramid as FP16 differences from the
+    reference's (Vship_SSIMU2InitEx with Vship_SSIMU2Fp16Deltas)."""
 
-    def __init__(self, width: int, height: int):
+    def __init__(self, width: int, height: int, fp16_deltas: bool = False):
         self.width, self.height = int(width), int(height)
         h = Handler()
-        _check(lib().Vship_SSIMU2Init(ctypes.byref(h), self.width, self.height), "Vship_SSIMU2Init")
+        if fp16_deltas:
+            _check(lib().Vship_SSIMU2InitEx(ctypes.byref(h), self.width, self.height, SSIMU2_FP16_DELTAS),
+                   "Vship_SSIMU2InitEx")
+        else:
+            _check(lib().Vship_SSIMU2Init(ctypes.byref(h), self.width, self.height), "Vship_SSIMU2Init")
         self._h = h  # only a created handler is ever freed
 
     def compute(self, reference, distorted) -> float:
@@ -429,11 +439,11 @@ class ButteraugliHandler:
 class SSIMU2Batch:
     """Batched device-resident SSIMU2 (Vship_SSIMU2BatchInit / Vship_SSIMU2ComputeDeviceAsync)."""
 
-    def __init__(self, width: int, height: int, max_pairs: int):
+    def __init__(self, width: int, height: int, max_pairs: int, fp16_deltas: bool = False):
         self.width, self.height, self.max_pairs = int(width), int(height), int(max_pairs)
         h = Handler()
-        _check(lib().Vship_SSIMU2BatchInit(ctypes.byref(h), self.width, self.height, self.max_pairs),
-               "Vship_SSIMU2BatchInit")
+        _check(lib().Vship_SSIMU2BatchInitEx(ctypes.byref(h), self.width, self.height, self.max_pairs,
+                                             SSIMU2_FP16_DELTAS if fp16_deltas else 0), "Vship_SSIMU2BatchInitEx")
         self._h = h  # only a created handler is ever freed
 
     def set_yuv_format(self, fmt: YuvFormat) -> None:

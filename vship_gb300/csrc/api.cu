@@ -466,16 +466,17 @@ Vship_Exception Vship_PinnedFree(void* ptr) {
 // ----- SSIMU2 -----------------------------------------------------------------------------
 
 static Vship_Exception ssimu2_init(Vship_SSIMU2Handler* handler, int width, int height, int max_pairs,
-                                   bool host_io) {
+                                   bool host_io, int flags = 0) {
     if (!handler) return Vship_BadPointer;
     if (width <= 0 || height <= 0 || max_pairs <= 0) return Vship_BadPointer;
+    if (flags & ~(int)Vship_SSIMU2Fp16Deltas) return Vship_BadPointer;
     int c = 0;
     int rc = check_gpu_count(&c);
     if (rc) return to_exc(rc);
     std::unique_ptr<Ssimu2Handle> h(new Ssimu2Handle());
     h->host_io = host_io;
     if (cudaGetDevice(&h->io.device) != cudaSuccess) return Vship_BadDeviceCode;
-    rc = h->eng.init(width, height, max_pairs);
+    rc = h->eng.init(width, height, max_pairs, (flags & Vship_SSIMU2Fp16Deltas) != 0);
     if (!rc && host_io) rc = h->io.init(width, height, sizeof(double));
     if (rc) return to_exc(rc);
     handler->id = g_ssimu2.put(std::move(h));
@@ -550,6 +551,19 @@ Vship_Exception Vship_SSIMU2ComputeDeviceAsync(Vship_SSIMU2Handler handler, cons
 
 uint64_t Vship_SSIMU2DeviceBytes(int width, int height, int max_pairs) {
     return (uint64_t)Ssimu2Engine::device_bytes(width, height, max_pairs);
+}
+
+Vship_Exception Vship_SSIMU2InitEx(Vship_SSIMU2Handler* handler, int width, int height, int flags) {
+    return ssimu2_init(handler, width, height, 1, true, flags);
+}
+
+Vship_Exception Vship_SSIMU2BatchInitEx(Vship_SSIMU2Handler* handler, int width, int height, int max_pairs,
+                                        int flags) {
+    return ssimu2_init(handler, width, height, max_pairs, false, flags);
+}
+
+uint64_t Vship_SSIMU2DeviceBytesEx(int width, int height, int max_pairs, int flags) {
+    return (uint64_t)Ssimu2Engine::device_bytes(width, height, max_pairs, (flags & Vship_SSIMU2Fp16Deltas) != 0);
 }
 
 // ----- Butteraugli ------------------------------------------------------------------------

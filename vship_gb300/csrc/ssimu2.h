@@ -31,24 +31,33 @@ struct Ssimu2Geom {
 Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h);
 
 // Device workspace and launch sequence for up to `max_pairs` frame pairs of one resolution.
-// Layout: pyr[pair][image][channel][plane_elems], partials[pair][tile][18], scores[pair].
+// Layout: pyr[pair][image][channel][plane_elems], partials[pair][tile][18], scores[pair]. With
+// fp16 deltas the distorted images' pyramids are stored as half(distorted - reference) in d16
+// [pair][channel][plane_elems], after the references' FP32 pyramids pyr[pair][channel][...].
 class Ssimu2Engine {
 public:
     int64_t w = 0, h = 0;
     int max_pairs = 0;
+    bool fp16 = false;
     Ssimu2Geom geom{};
     float* pyr = nullptr;
+    __half* d16 = nullptr;
     float* partials = nullptr;
     double* scores = nullptr;
 
-    int init(int64_t width, int64_t height, int max_pairs);
+    int init(int64_t width, int64_t height, int max_pairs, bool fp16_deltas = false);
     void destroy();
     // frames_dev: 2*npairs FrameDesc in device memory (pair-major: reference, distorted).
     // Scores land in out_scores (device) or in this->scores when out_scores is null.
     // yuv: the Y'CbCr format of IN_YUV frames (null: 10-bit 4:2:0 BT.709 limited, left siting).
     int launch(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st,
                const YuvParams* yuv = nullptr);
-    static size_t device_bytes(int64_t w, int64_t h, int pairs);
+    static size_t device_bytes(int64_t w, int64_t h, int pairs, bool fp16_deltas = false);
+    static size_t pyramid_bytes(const Ssimu2Geom& g, int pairs, bool fp16_deltas);
+
+private:
+    int launch_fp16(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores, cudaStream_t st,
+                    const YuvParams& yp);
 };
 
 // For callers that supply the scratch themselves (noalloc.cu): upload this device's constant
