@@ -1089,28 +1089,37 @@ __global__ void __launch_bounds__(256) butter_diffmap_kernel(float* const* __res
     }
 }
 
-// FP64 norm combine, one CTA per pair (diffnorms.hpp:263-306).
+// Norm combine, one CTA per pair (diffnorms.hpp:263-306): the per-tile sums reduced as
+// float-float sums on the FP32 pipe (eight loads in flight per thread), then the two roots in
+// FP64 by two warps at once. On this GPU a dependent FP64 operation takes about 60 cycles and
+// pow() several thousand, so the common norms take the cheaper library roots: the 3-norm cbrt,
+// a Q-norm of 2 sqrt (1 none), other Q pow.
+__device__ __forceinline__ double root_q(double x, int q) {
+    return q == 1 ? x : q == 2 ? sqrt(x) : q == 3 ? cbrt(x) : pow(x, 1.0 / (double)q);
+}
+
 __global__ void __launch_bounds__(256) butter_finalize_kernel(const float* __restrict__ partials,
                                                               double* __restrict__ norms, BGeom g, int qnorm) {
-    __shared__ double red[3][8];
+    __shared__ FSum red[2][8];
+    __shared__ float redmx[8];
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    double sq = 0.0, s3 = 0.0;
+    FSum sq{0.f, 0.f}, s3{0.f, 0.f};
     float mx = 0.f;
     const float* p = partials + (int64_t)pair * 3 * g.norm_tiles;
-    // float partial sums of 8 tiles at a time (loads issued together), combined in FP64
     for (int t0 = tid; t0 < g.norm_tiles; t0 += 256 * 8) {
-        float a = 0.f, b = 0.f;
+        float a[8], b[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             const int t = t0 + 256 * k;
-            if (t < g.norm_tiles) {
-                a += __ldg(p + t);
-                b += __ldg(p + g.norm_tiles + t);
-                mx = fmaxf(mx, __ldg(p + 2 * g.norm_tiles + t));
-            }
+            a[k] = t < g.norm_tiles ? __ldg(p + t) : 0.f;
+            b[k] = t < g.norm_tiles ? __ldg(p + g.norm_tiles + t) : 0.f;
+            if (t < g.norm_tiles) mx = fmaxf(mx, __ldg(p + 2 * g.norm_tiles + t));
         }
-        sq += (double)a;
-        s3 += (double)b;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            sq.add(a[k]);
+            s3.add(b[k]);
+        }
     }
     sq = warp_sum(sq);
     s3 = warp_sum(s3);
@@ -1118,20 +1127,19 @@ __global__ void __launch_bounds__(256) butter_finalize_kernel(const float* __res
     if (lane == 0) {
         red[0][warp] = sq;
         red[1][warp] = s3;
-        red[2][warp] = (double)mx;
+        redmx[warp] = mx;
     }
     __syncthreads();
-    if (tid == 0) {
-        double a = 0, b = 0, c = 0;
-        for (int w = 0; w < 8; w++) {
-            a += red[0][w];
-            b += red[1][w];
-            c = fmax(c, red[2][w]);
-        }
+    if (lane == 0 && warp < 2) {
+        FSum a = red[warp][0];
+        for (int w = 1; w < 8; w++) a.add(red[warp][w]);
         const double n = (double)g.s[0].w * (double)g.s[0].h;
-        norms[pair * 3 + 0] = pow(a / n, 1.0 / (double)qnorm);
-        norms[pair * 3 + 1] = pow(b / n, 1.0 / 3.0);
-        norms[pair * 3 + 2] = c;
+        norms[pair * 3 + warp] = root_q(a.value() / n, warp == 0 ? qnorm : 3);
+        if (warp == 1) {
+            float c = redmx[0];
+            for (int w = 1; w < 8; w++) c = fmaxf(c, redmx[w]);
+            norms[pair * 3 + 2] = (double)c;
+        }
     }
 }
 

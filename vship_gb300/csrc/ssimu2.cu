@@ -13,8 +13,9 @@
 //                        horizontal-pass rows, forms the SSIM / artifact / detail-loss maps and
 //                        emits 18 partial sums (6 pools x 3 channels) per CTA.
 //                        Reference: ssimu2/score.hpp:95-196, gaussianblur.hpp:24-92.
-//   3. ssimu2_finalize : FP64 combine of the partial sums, 4th roots, the 108-feature permutation,
-//                        weighted sum and score mapping (score.hpp:198-401, main.hpp:83-98).
+//   3. ssimu2_finalize : combine of the partial sums (float-float), then in FP64 the means, 4th
+//                        roots, the 108-feature permutation, weighted sum and score mapping
+//                        (score.hpp:198-401, main.hpp:83-98).
 #include "common.cuh"
 #include "ssimu2.h"
 #include "profile.h"
@@ -874,49 +875,86 @@ __global__ void __launch_bounds__(256, 3) ssimu2_stats_delta_kernel(const float*
 }
 
 // ------------------------------------------------------------------------------------------
-// Kernel 3: FP64 finalisation, one CTA per pair. The 108 (scale, pool, channel) sums are
-// reduced warp-parallel over their tiles (coalesced), then the 108 weighted features are summed
-// in parallel; only the score mapping runs on one thread (FP64 is a slow pipe on this GPU).
+// Kernel 3: finalisation, one CTA of kFinThreads per pair. The 108 (scale, pool, channel) sums
+// are reduced over their tiles by 32 warps at once (coalesced loads, four in flight per lane) as
+// float-float sums; then 108 threads form the features in FP64 (mean, 4th root, weight) and sum
+// them; only the score mapping runs on one thread. The kernel is latency-bound: on this GPU a
+// dependent FP64 operation takes about 60 cycles, an FP64 square root or reciprocal several
+// hundred and pow() several thousand, so the tile sums stay on the FP32 pipe, the means
+// multiply by inverses computed while the loads are in flight, the 4th roots use division-free
+// Newton steps and the score mapping exp2(e log2 x).
 // partials: this pair's [18][tiles_total] block.
+constexpr int kFinThreads = 1024;
+
+// x^(1/4) in FP64 arithmetic without FP64 square roots: y ~ x^(-1/4) from the FP32
+// approximations (relative error about 4e-7), two Newton steps for y^-4 = x,
+// y' = y + y (1 - x y^4) / 4 (division-free; the relative error e becomes about 2.5 e^2 per step:
+// 4e-13, then below FP64 rounding), then x^(1/4) = x y^3. Zero, NaN and values far outside
+// FP32's range take the FP64 square roots.
+__device__ __forceinline__ double root4(double x) {
+    const float xf = (float)x;
+    if (!(xf > 1e-30f && xf < 1e30f)) return sqrt(sqrt(x));
+    double y = (double)rsqrtf(sqrtf(xf));
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const double y2 = y * y;
+        y = fma(y, 0.25 * (1.0 - x * (y2 * y2)), y);
+    }
+    return (x * y) * (y * y);
+}
+
 __device__ __forceinline__ void finalize_pair(const float* __restrict__ partials, const Ssimu2Geom& g,
                                               double* __restrict__ score) {
-    __shared__ double pooled[6][18];
-    __shared__ double red[8];
+    constexpr int NW = kFinThreads / 32;
+    __shared__ FSum pooled[6][18];
+    __shared__ double inv_px[6];
+    __shared__ double red[4];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int tiles_total = g.tiles_total;
-    for (int seg = warp; seg < 108; seg += 8) {
+    // the last warp has the fewest segments: it also computes 1 / pixels per scale
+    if (warp == NW - 1 && lane < 6) inv_px[lane] = 1.0 / ((double)g.lv[lane].w * (double)g.lv[lane].h);
+    for (int seg = warp; seg < 108; seg += NW) {
         const int s = seg / 18, i = seg - 18 * (seg / 18);
         const float* p = partials + (int64_t)i * tiles_total + g.tile_begin[s];
         const int n = g.tile_begin[s + 1] - g.tile_begin[s];
-        double a = 0.0;
-        for (int t = lane; t < n; t += 32) a += (double)__ldg(p + t);
+        FSum a{0.f, 0.f};
+        for (int t0 = lane; t0 < n; t0 += 128) {
+            float v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = t0 + 32 * k < n ? __ldg(p + t0 + 32 * k) : 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; k++) a.add(v[k]);
+        }
         a = warp_sum(a);
-        if (lane == 0) pooled[s][i] = a / ((double)g.lv[s].w * (double)g.lv[s].h);
+        if (lane == 0) pooled[s][i] = a;
     }
     __syncthreads();
     // feature k = plane*36 + scale*6 + norm*3 + map (ssimu2/main.hpp:83-95); pooled index
-    // (map*2 + norm)*3 + plane; 4th root for the 4-norm (score.hpp:263-267)
-    double v = 0.0;
-    if (tid < 108) {
-        const int plane = tid / 36, sc = (tid % 36) / 6, nrm = (tid % 6) / 3, mi = tid % 3;
-        double x = pooled[sc][(mi * 2 + nrm) * 3 + plane];
-        if (nrm == 1) x = sqrt(sqrt(x));
-        v = c_s2_w[tid] * x;
+    // (map*2 + norm)*3 + plane; the mean over the scale's pixels, 4th root for the 4-norm
+    // (score.hpp:263-267)
+    if (tid < 128) {
+        double v = 0.0;
+        if (tid < 108) {
+            const int plane = tid / 36, sc = (tid % 36) / 6, nrm = (tid % 6) / 3, mi = tid % 3;
+            double x = pooled[sc][(mi * 2 + nrm) * 3 + plane].value() * inv_px[sc];
+            if (nrm == 1) x = root4(x);
+            v = c_s2_w[tid] * x;
+        }
+        v = warp_sum(v);
+        if (lane == 0) red[warp] = v;
     }
-    v = warp_sum(v);
-    if (lane == 0) red[warp] = v;
     __syncthreads();
     if (tid == 0) {
         double ssim = 0.0;
-        for (int w = 0; w < 8; w++) ssim += red[w];
+        for (int w = 0; w < 4; w++) ssim += red[w];
         ssim *= 0.9562382616834844;  // score.hpp:388-397
         ssim = (6.248496625763138e-5 * ssim * ssim) * ssim + 2.326765642916932 * ssim -
                0.020884521182843837 * ssim * ssim;
-        *score = ssim > 0.0 ? pow(ssim, 0.6276336467831387) * -10.0 + 100.0 : 100.0;
+        *score = ssim > 0.0 ? exp2(0.6276336467831387 * log2(ssim)) * -10.0 + 100.0 : 100.0;
     }
 }
 
-__global__ void __launch_bounds__(256) ssimu2_finalize_kernel(const float* __restrict__ partials,
+__global__ void __launch_bounds__(kFinThreads) ssimu2_finalize_kernel(const float* __restrict__ partials,
                                                               double* __restrict__ scores, Ssimu2Geom g) {
     finalize_pair(partials + (int64_t)blockIdx.x * 18 * g.tiles_total, g, scores + blockIdx.x);
 }
@@ -955,7 +993,7 @@ __global__ void __launch_bounds__(256, 3) ssimu2_multi_stats_kernel(const Ssimu2
     }
 }
 
-__global__ void __launch_bounds__(256) ssimu2_multi_finalize_kernel(const Ssimu2MultiPair* __restrict__ pairs,
+__global__ void __launch_bounds__(kFinThreads) ssimu2_multi_finalize_kernel(const Ssimu2MultiPair* __restrict__ pairs,
                                                                     const Ssimu2Geom* __restrict__ geoms) {
     const Ssimu2MultiPair P = pairs[blockIdx.x];
     finalize_pair(P.partials, geoms[P.geom], P.score);
@@ -1054,7 +1092,7 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
     }
     {
         ProfScope ps("ssimu2_finalize", st);
-        ssimu2_finalize_kernel<<<npairs, 256, 0, st>>>(partials, out_scores ? out_scores : scores, geom);
+        ssimu2_finalize_kernel<<<npairs, kFinThreads, 0, st>>>(partials, out_scores ? out_scores : scores, geom);
     }
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
@@ -1092,7 +1130,7 @@ int Ssimu2Engine::launch_fp16(const FrameDesc* frames_dev, int intype, int npair
     }
     {
         ProfScope ps("ssimu2_finalize", st);
-        ssimu2_finalize_kernel<<<npairs, 256, 0, st>>>(partials, out_scores ? out_scores : scores, geom);
+        ssimu2_finalize_kernel<<<npairs, kFinThreads, 0, st>>>(partials, out_scores ? out_scores : scores, geom);
     }
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
@@ -1134,7 +1172,7 @@ int ssimu2_launch_scratch(const FrameDesc& ref, const FrameDesc& dist, int intyp
     }
     ssimu2_stats_kernel<kPlainShape><<<dim3((unsigned)geom.tiles_total, 1u), 256, stats_smem(kPlainShape), st>>>(
         pyr, partials, geom);
-    ssimu2_finalize_kernel<<<1, 256, 0, st>>>(partials, out_score, geom);
+    ssimu2_finalize_kernel<<<1, kFinThreads, 0, st>>>(partials, out_score, geom);
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
 }
@@ -1217,7 +1255,7 @@ int ssimu2_multi_stats(const Ssimu2MultiPair* pairs, const int2* items, int nite
 int ssimu2_multi_finalize(const Ssimu2MultiPair* pairs, int npairs, const Ssimu2Geom* geoms, cudaStream_t st) {
     if (npairs <= 0) return E_OK;
     ProfScope ps("ssimu2_multi_finalize", st);
-    ssimu2_multi_finalize_kernel<<<(unsigned)npairs, 256, 0, st>>>(pairs, geoms);
+    ssimu2_multi_finalize_kernel<<<(unsigned)npairs, kFinThreads, 0, st>>>(pairs, geoms);
     VSHIP_CUDA_TRY(cudaGetLastError());
     return E_OK;
 }
