@@ -26,14 +26,14 @@
 namespace vship {
 
 // ------------------------------------------------------------------------------------------
-// Gaussian table (sigma 1.5, radius 8): taps and prefix integral, built on the host exactly as
-// ssimu2/gaussianblur.hpp:7-18 builds them.
-__constant__ float c_s2_k[17];
-__constant__ float c_s2_I[18];
-// 1 / (I[end] - I[beg]) for beg in 0..8 and end in 9..17: the inverse in-bounds mass of every
-// window a border can cut, so the renormalisation is a table load instead of a division
-__constant__ float c_s2_invm[9][9];
-__constant__ f2_t c_s2_k2[17];  // {k, k} pairs for the f32x2 FMA
+// Gaussian table (sigma 1.5, radius 8): taps k and prefix integral I, built on the host exactly
+// as ssimu2/gaussianblur.hpp:7-18 builds them. The stats kernels blur with the taps divided by
+// the kernel's total mass K = I[17] - I[0] ({k/K, k/K} pairs for the f32x2 FMA), so that a window
+// inside the image needs no renormalisation; a window that a border cuts (beg in 0..8 taps cut
+// on one side, end in 9..17) is multiplied by K / (I[end] - I[beg]), its inverse in-bounds mass
+// relative to K, from a table rather than by a division (exactly 1 for an uncut window).
+__constant__ f2_t c_s2_k2n[17];
+__constant__ float c_s2_invmn[9][9];
 // SSIMULACRA2 feature weights (ssimu2/score.hpp:272-379), FP64.
 __constant__ double c_s2_w[108];
 
@@ -68,15 +68,13 @@ static int upload_constants_once() {
         k[i] = (float)((double)e / std::sqrt(6.28318530718 * sigma * sigma));
         I[i + 1] = I[i] + k[i];
     }
-    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k, k, sizeof(k)));
-    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_I, I, sizeof(I)));
-    float invm[9][9];
+    const float K = I[17] - I[0];
+    float k2n[34], invmn[9][9];
+    for (int i = 0; i < 17; i++) k2n[2 * i] = k2n[2 * i + 1] = k[i] / K;
     for (int b = 0; b < 9; b++)
-        for (int e = 0; e < 9; e++) invm[b][e] = 1.0f / (I[9 + e] - I[b]);
-    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_invm, invm, sizeof(invm)));
-    float k2[34];
-    for (int i = 0; i < 17; i++) k2[2 * i] = k2[2 * i + 1] = k[i];
-    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k2, k2, sizeof(k2)));
+        for (int e = 0; e < 9; e++) invmn[b][e] = K / (I[9 + e] - I[b]);
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_k2n, k2n, sizeof(k2n)));
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_invmn, invmn, sizeof(invmn)));
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_s2_w, kSsimu2Weights, sizeof(kSsimu2Weights)));
     return E_OK;
 }
@@ -328,12 +326,54 @@ constexpr int ST_HPLANE = ST_TW * ST_HROWS + 8 * (ST_TW / 8 - 1);  // float pair
 constexpr int kStatsSmem = (2 * ST_RAW + 4 * ST_HPLANE + 3 * 8 * 6) * 4;
 
 __device__ __forceinline__ float s2_inv_mass(int pos, int extent) {
-    // in-bounds kernel mass for a 17-tap window centred on pos (reference: out / tot)
+    // in-bounds kernel mass of a 17-tap window centred on pos, inverted and relative to the
+    // whole kernel's (reference: out / tot); 1 for a window inside the image
     const int beg = max(0, pos - 8) - (pos - 8);
     const int end = min(extent, pos + 9) - (pos - 8);
-    // the same IEEE quotient as 1 / (I[end] - I[beg]); positions past the edge (whose outputs are
-    // never pooled) are clamped onto the table
-    return c_s2_invm[beg][max(end - 9, 0)];
+    // positions past the edge (whose outputs are never pooled) are clamped onto the table
+    return c_s2_invmn[beg][max(end - 9, 0)];
+}
+
+// Per-thread pooled sums of the three maps: (sum d0, sum d1) and (sum d0^4, sum d1^4) as f32x2
+// pairs, sum d2 and sum d2^4; pool index map * 2 + norm.
+struct S2Pools {
+    f2_t s01, q01;
+    float s2, q2;
+};
+__device__ __forceinline__ S2Pools s2_pools_zero() { return S2Pools{f2_pack(0.f, 0.f), f2_pack(0.f, 0.f), 0.f, 0.f}; }
+__device__ __forceinline__ void s2_pools_unpack(const S2Pools& p, float* v) {
+    f2_unpack(p.s01, v[0], v[2]);
+    f2_unpack(p.q01, v[1], v[3]);
+    v[4] = p.s2;
+    v[5] = p.q2;
+}
+
+// The SSIM, artifact and detail-loss maps of one pixel (score.hpp:141-153), pooled into P. All
+// values are on samples shifted by the segment's constant: m1 = E[a], m2 = E[b],
+// dd = E[(a - b)^2], m12 = E[a b] (blurred), i1, i2 the pixel's own samples.
+// The reference's SSIM map is max(1 - (1 - (m1 - m2)^2) (2 s12 + C2) / (s11 + s22 + C2), 0).
+// With t = dd - (m1 - m2)^2 = s11 + s22 - 2 s12 (the variance of a - b) and n = 2 s12 + C2 its
+// denominator is t + n, and the map is max((t + (m1 - m2)^2 n) / (t + n), 0): the same quantity
+// without the cancellation in 1 - num / den or in s11 + s22, and exactly 0 for identical images
+// (a - b = 0 makes dd and m1 - m2 exactly 0). The edge maps: (|I2 - m2| + 1) / (|I1 - m1| + 1) - 1
+// written as (|I2 - m2| - |I1 - m1|) / (|I1 - m1| + 1); |I - mu| is shift-invariant.
+__device__ __forceinline__ void s2_pixel_maps(float m1, float m2, float dd, float m12, float i1, float i2,
+                                              S2Pools& P) {
+    const float md = m1 - m2;
+    const float md2 = md * md;
+    const float t = dd - md2;
+    const float n = fmaf(fmaf(-m1, m2, m12), 2.0f, 0.0009f);
+    const float d0 = fmaxf(__fdividef(fmaf(md2, n, t), t + n), 0.0f);
+    const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
+    const float v = __fdividef(e2 - e1, e1 + 1.0f);
+    const float d1 = fmaxf(v, 0.0f), d2 = fmaxf(-v, 0.0f);
+    const f2_t d01 = f2_pack(d0, d1);
+    P.s01 = f2_add(P.s01, d01);
+    const f2_t q = f2_mul(d01, d01);
+    P.q01 = f2_fma(q, q, P.q01);
+    P.s2 += d2;
+    const float q2 = d2 * d2;
+    P.q2 = fmaf(q2, q2, P.q2);
 }
 
 // FP16 delta tile: 64 rows x 48 halves, row pitch 56 halves (7 quads: conflict-free 16-byte reads)
@@ -365,13 +405,12 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
     // border renormalisations (out / tot, gaussianblur.hpp:63-92) are applied here as one product.
     const int vc = tid & 31, vg = tid >> 5;
     const float rxv = s2_inv_mass(tx0 + vc, L.w);
-    const float rx_in = rxv * (1.0f / (c_s2_I[17] - c_s2_I[0]));  // rows whose window is inside
     float* r1 = raw;
     float* r2 = raw + ST_RAW;
 
 #pragma unroll 1
     for (int c = 0; c < 3; c++) {
-        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        S2Pools P = s2_pools_zero();
         float shift = 0.f;
 #pragma unroll 1
         for (int k = 0; k < nchunk; k++) {
@@ -408,8 +447,8 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
             // chunk so that the SM's four schedulers share the work evenly). Segment row
             // h = 48k + r goes to ring slot h & 63, and to slot 64 + (h & 63) as well when that is
             // below 22. The SSIM map needs the two variances only as their sum (score.hpp:147), so
-            // four moments are blurred: {a, b} and {a^2 + b^2, a*b}, each pair through the f32x2
-            // FMA with a shared weight.
+            // four moments are blurred: {a, b} and {(a - b)^2, a b} (s2_pixel_maps), each pair
+            // through the f32x2 FMA with a shared weight.
             const int rr = k == 0 ? 8 * warp + (lane & 7) : 2 * ST_R + 8 * ((warp + 2 * k) & 7) + (lane & 7);
             if (rr < ST_IH) {
                 f2_t h1[8], h2[8];
@@ -448,14 +487,15 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                         const int j = 4 * j4 + u;
                         const float a = la[u] - shift;
                         const float b = DELTA ? a + dl[j] : lb[u] - shift;
+                        const float d = DELTA ? dl[j] : la[u] - lb[u];  // b - a or a - b: squared
                         const f2_t p1 = f2_pack(a, b);
-                        const f2_t p2 = f2_pack(fmaf(a, a, b * b), a * b);
+                        const f2_t p2 = f2_pack(d * d, a * b);
 #pragma unroll
                         for (int o = 0; o < 8; o++) {
                             const int i = j - o;  // tap index
                             if (i >= 0 && i < 17) {
-                                h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
-                                h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
+                                h1[o] = f2_fma(p1, c_s2_k2n[i], h1[o]);
+                                h2[o] = f2_fma(p2, c_s2_k2n[i], h2[o]);
                             }
                         }
                     }
@@ -478,16 +518,13 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
             }
             __syncthreads();
             // vertical pass + maps (column vc, chunk rows 6*vg .. 6*vg+5): the window is ring rows
-            // s0 .. s0+21 with s0 = (48k + 6*vg) & 63, never past the mirrored slots
+            // s0 .. s0+21 with s0 = (48k + 6*vg) & 63, never past the mirrored slots. A chunk whose
+            // windows all lie inside the image needs neither renormalisation nor bounds tests.
+            const bool interior = x_inside && ty0 >= ST_R && ty0 + ST_TH + ST_R <= L.h;
             float rxy[6];
-            if (ty0 + 6 * vg >= ST_R && ty0 + 6 * vg + 5 + ST_R < L.h) {
 #pragma unroll
-                for (int o = 0; o < 6; o++) rxy[o] = rx_in;
-            } else {
-#pragma unroll
-                for (int o = 0; o < 6; o++) rxy[o] = rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
-            }
-            float m[4][6];  // mu1, mu2, E[a^2 + b^2], E[a b] (shifted)
+            for (int o = 0; o < 6; o++) rxy[o] = interior ? 1.0f : rxv * s2_inv_mass(ty0 + 6 * vg + o, L.h);
+            float m[4][6];  // mu1, mu2, E[(a - b)^2], E[a b] (shifted)
             {
                 const int s0 = (k * ST_TH + 6 * vg) & (ST_RING - 1);
                 const int cb = vc * ST_HROWS + 8 * (vc >> 3) + s0;  // even: 16-byte aligned
@@ -507,8 +544,8 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
                     for (int o = 0; o < 6; o++) {
                         f2_t a = f2_pack(0.f, 0.f);
 #pragma unroll
-                        for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], c_s2_k2[i], a);
-                        a = f2_mul(a, f2_pack(rxy[o], rxy[o]));
+                        for (int i = 0; i < 17; i++) a = f2_fma(v[o + i], c_s2_k2n[i], a);
+                        if (!interior) a = f2_mul(a, f2_pack(rxy[o], rxy[o]));
                         f2_unpack(a, m[2 * q][o], m[2 * q + 1][o]);
                     }
                 }
@@ -516,45 +553,22 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
 #pragma unroll
             for (int o = 0; o < 6; o++) {
                 const int y = ty0 + 6 * vg + o, x = tx0 + vc;
-                if (x < L.w && y < L.h) {
+                if (interior || (x < L.w && y < L.h)) {
                     const int so = (6 * vg + o + ST_R) * ST_RP + vc + ST_R;
                     const float i1 = r1[so] - shift;  // shifted samples
                     const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(6 * vg + o + ST_R) * ST_DP +
                                                                                                      vc + ST_R])
                                            : r2[so] - shift;
-                    const float m1 = m[0][o], m2 = m[1][o];  // shifted means
-                    // SSIM map (score.hpp:141-148) as max((den - num) / den, 0), the same quantity
-                    // as max(1 - num / den, 0) without the cancellation; sigma11 + sigma22 as
-                    // (S/2 - m1^2) + (S/2 - m2^2) with S = E[a^2 + b^2]. Explicit fma: identical
-                    // frames give S/2 == E[ab] exactly (a^2 + b^2 = 2ab), so num == den bitwise
-                    const float md = m1 - m2;
-                    const float num_m = fmaf(md, -md, 1.0f);
-                    const float hs = 0.5f * m[2][o];
-                    const float s12 = fmaf(-m1, m2, m[3][o]);
-                    const float s11 = fmaf(-m1, m1, hs);
-                    const float s22 = fmaf(-m2, m2, hs);
-                    const float num_s = fmaf(s12, 2.0f, 0.0009f);
-                    const float denom = (s11 + s22) + 0.0009f;
-                    const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
-                    // edge maps (score.hpp:151-153): (|I2-m2| + 1) / (|I1-m1| + 1) - 1 written as
-                    // (|I2-m2| - |I1-m1|) / (|I1-m1| + 1); |I - mu| is shift-invariant
-                    const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
-                    const float v1 = __fdividef(e2 - e1, e1 + 1.0f);
-                    const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
-                    const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
-                    acc[0] += d0;
-                    acc[1] += q0 * q0;
-                    acc[2] += d1;
-                    acc[3] += q1 * q1;
-                    acc[4] += d2;
-                    acc[5] += q2 * q2;
+                    s2_pixel_maps(m[0][o], m[1][o], m[2][o], m[3][o], i1, i2, P);
                 }
             }
             __syncthreads();  // the raw tiles and ring slots are rewritten by the next chunk
         }
+        float pv[6];
+        s2_pools_unpack(P, pv);
 #pragma unroll
         for (int i = 0; i < 6; i++) {
-            const float v = warp_sum(acc[i]);
+            const float v = warp_sum(pv[i]);
             if (lane == 0) red[(c * 8 + warp) * 6 + i] = v;
         }
     }
@@ -615,7 +629,6 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
     // renormalisations (gaussianblur.hpp:63-92) applied there as one product.
     const int vc = tid & 31, vg = tid >> 5;
     const float rxv = s2_inv_mass(tx0 + vc, L.w);
-    const float rx_in = rxv * (1.0f / (c_s2_I[17] - c_s2_I[0]));
     float* r1 = raw;
     float* r2 = raw + SC_RAW;
     f2_t* const hp1 = reinterpret_cast<f2_t*>(hb);
@@ -623,7 +636,7 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
 
 #pragma unroll 1
     for (int c = 0; c < 3; c++) {
-        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        S2Pools P = s2_pools_zero();
         float shift = 0.f;
 #pragma unroll 1
         for (int k = 0; k < nchunk; k++) {
@@ -708,14 +721,15 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
                         const int j = 4 * j4 + u;
                         const float a = la[u] - shift;
                         const float b = DELTA ? a + dl[j] : lb[u] - shift;
+                        const float d = DELTA ? dl[j] : la[u] - lb[u];  // b - a or a - b: squared
                         const f2_t p1 = f2_pack(a, b);
-                        const f2_t p2 = f2_pack(fmaf(a, a, b * b), a * b);
+                        const f2_t p2 = f2_pack(d * d, a * b);
 #pragma unroll
                         for (int o = 0; o < 8; o++) {
                             const int i = j - o;  // tap index
                             if (i >= 0 && i < 17) {
-                                h1[o] = f2_fma(p1, c_s2_k2[i], h1[o]);
-                                h2[o] = f2_fma(p2, c_s2_k2[i], h2[o]);
+                                h1[o] = f2_fma(p1, c_s2_k2n[i], h1[o]);
+                                h2[o] = f2_fma(p2, c_s2_k2n[i], h2[o]);
                             }
                         }
                     }
@@ -730,8 +744,9 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
             }
             __syncthreads();
             // vertical pass + maps: buffer rows 8*vg .. 8*vg+23 streamed once, each scattered into
-            // the 8 outputs it feeds
-            const bool rows_in = ty0 + 8 * vg >= ST_R && ty0 + 8 * vg + 7 + ST_R < L.h;
+            // the 8 outputs it feeds. A chunk whose windows all lie inside the image needs neither
+            // renormalisation nor bounds tests.
+            const bool interior = x_inside && ty0 >= ST_R && ty0 + SC_TH + ST_R <= L.h;
             f2_t a1[8], a2[8];
             {
                 const f2_t z2 = f2_pack(0.f, 0.f);
@@ -756,46 +771,42 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
                         for (int o = 0; o < 8; o++) {
                             const int i = j - o;
                             if (i >= 0 && i < 17) {
-                                a1[o] = f2_fma(v1, c_s2_k2[i], a1[o]);
-                                a2[o] = f2_fma(v2, c_s2_k2[i], a2[o]);
+                                a1[o] = f2_fma(v1, c_s2_k2n[i], a1[o]);
+                                a2[o] = f2_fma(v2, c_s2_k2n[i], a2[o]);
                             }
                         }
                     }
                 }
             }
+            if (interior) {
 #pragma unroll
-            for (int o = 0; o < 8; o++) {
-                const int y = ty0 + 8 * vg + o, x = tx0 + vc;
-                if (x < L.w && y < L.h) {
-                    const float rxy = rows_in ? rx_in : rxv * s2_inv_mass(y, L.h);
-                    float m1, m2, mS, m12;
-                    f2_unpack(f2_mul(a1[o], f2_pack(rxy, rxy)), m1, m2);
-                    f2_unpack(f2_mul(a2[o], f2_pack(rxy, rxy)), mS, m12);
+                for (int o = 0; o < 8; o++) {
+                    float m1, m2, dd, m12;
+                    f2_unpack(a1[o], m1, m2);
+                    f2_unpack(a2[o], dd, m12);
                     const int so = (8 * vg + o + ST_R) * ST_RP + vc + ST_R;
                     const float i1 = r1[so] - shift;
                     const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(8 * vg + o + ST_R) * ST_DP +
                                                                                                      vc + ST_R])
                                            : r2[so] - shift;
-                    // the maps of the ring shape (stats_tile), term for term
-                    const float md = m1 - m2;
-                    const float num_m = fmaf(md, -md, 1.0f);
-                    const float hs = 0.5f * mS;
-                    const float s12 = fmaf(-m1, m2, m12);
-                    const float s11 = fmaf(-m1, m1, hs);
-                    const float s22 = fmaf(-m2, m2, hs);
-                    const float num_s = fmaf(s12, 2.0f, 0.0009f);
-                    const float denom = (s11 + s22) + 0.0009f;
-                    const float d0 = fmaxf(__fdividef(fmaf(-num_m, num_s, denom), denom), 0.0f);
-                    const float e1 = fabsf(i1 - m1), e2 = fabsf(i2 - m2);
-                    const float v1 = __fdividef(e2 - e1, e1 + 1.0f);
-                    const float d1 = fmaxf(v1, 0.0f), d2 = fmaxf(-v1, 0.0f);
-                    const float q0 = d0 * d0, q1 = d1 * d1, q2 = d2 * d2;
-                    acc[0] += d0;
-                    acc[1] += q0 * q0;
-                    acc[2] += d1;
-                    acc[3] += q1 * q1;
-                    acc[4] += d2;
-                    acc[5] += q2 * q2;
+                    s2_pixel_maps(m1, m2, dd, m12, i1, i2, P);
+                }
+            } else {
+#pragma unroll
+                for (int o = 0; o < 8; o++) {
+                    const int y = ty0 + 8 * vg + o, x = tx0 + vc;
+                    if (x < L.w && y < L.h) {
+                        const float rxy = rxv * s2_inv_mass(y, L.h);
+                        float m1, m2, dd, m12;
+                        f2_unpack(f2_mul(a1[o], f2_pack(rxy, rxy)), m1, m2);
+                        f2_unpack(f2_mul(a2[o], f2_pack(rxy, rxy)), dd, m12);
+                        const int so = (8 * vg + o + ST_R) * ST_RP + vc + ST_R;
+                        const float i1 = r1[so] - shift;
+                        const float i2 = DELTA ? i1 + __half2float(reinterpret_cast<const __half*>(r2)[(8 * vg + o + ST_R) * ST_DP +
+                                                                                                         vc + ST_R])
+                                               : r2[so] - shift;
+                        s2_pixel_maps(m1, m2, dd, m12, i1, i2, P);
+                    }
                 }
             }
             __syncthreads();  // the raw tiles and buffer rows are rewritten for the next chunk
@@ -812,9 +823,11 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
                 }
             }
         }
+        float pv[6];
+        s2_pools_unpack(P, pv);
 #pragma unroll
         for (int i = 0; i < 6; i++) {
-            const float v = warp_sum(acc[i]);
+            const float v = warp_sum(pv[i]);
             if (lane == 0) red[(c * 8 + warp) * 6 + i] = v;
         }
     }
