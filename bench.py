@@ -105,8 +105,7 @@ def kernel_bytes_per_pair(kind, w, h, in_bytes):
             "butter_opsin": 2 * 24 * ns,      # linear RGB in, XYB out
             "butter_hblur_lf": 2 * 24 * ns,   # 3 planes in, 3 out
             "butter_lf_v": 2 * 48 * ns,       # 3 blurred + 3 XYB in, D and LF vals out
-            "butter_hblur_mf": 2 * 24 * ns,
-            "butter_mf_v": 2 * 40 * ns,       # 3 blurred + 2 D in, 2 HF_pre + 3 MF out
+            "butter_mf": 2 * 32 * ns,         # 3 D in, 2 HF_pre + 3 MF out (both passes in one)
             "butter_hf": 2 * 28 * ns,         # 2 HF_pre in, HF, UHF and the mask precompute out
             "butter_diff": 88 * ns,           # 20 band planes in, 2 pair planes out
             "butter_mask_blur": 20 * ns,      # 2 mask precomputes + AC in, blurred mask + AC out

@@ -8,8 +8,9 @@
 //                 (colors.hpp:25-91)
 //   lf_h, lf_v  : separable 43-tap blur (sigma 7.156); the vertical pass also forms D = XYB - LF
 //                 and the LF "vals" (separatefrequencies.hpp:3-12,160-203)
-//   mf_h, mf_v  : separable 19-tap blur (sigma 3.225) of D; the vertical pass forms MF with its
-//                 range operators and HF_pre = D - MF with X suppressed by Y (:37-99)
+//   mf          : separable 19-tap blur (sigma 3.225) of D, both passes in one kernel (the
+//                 horizontal pass's rows stay in shared memory); forms MF with its range operators
+//                 and HF_pre = D - MF with X suppressed by Y (:37-99)
 //   hf          : 17-tap tile blur (sigma 1.564) of HF_pre -> HF and UHF (:117-140,189-200)
 //   diff        : the six Malta maps from a register window over a smem tile of the asymmetric
 //                 diffs, the L2 / L2-asymmetric terms and the mask precompute
@@ -92,8 +93,9 @@ __device__ __forceinline__ void b_inv_mass_run(int p0, int extent, float out[N])
 // several pairs (a source scored against several candidates) is read-only after its own stage.
 enum : int {
     I_LIN = 0,    // 0..2   linear RGB; dead after opsin
-    I_TMP = 0,    // 0..2   horizontal-pass output (reuses LIN); dead after mf_v
-    I_XYB = 3,    // 3..5   XYB, then D = XYB - LF, then HF_pre (X, Y) in place; dead after hf
+    I_TMP = 0,    // 0..2   the LF horizontal pass's output (reuses LIN); dead after lf_v
+    I_XYB = 3,    // 3..5   XYB, then D = XYB - LF (in place); dead after the MF kernel
+    I_HFP = 0,    // 0..1   HF_pre (X, Y), written by the MF kernel over TMP; dead after hf
     I_LFV = 6,    // 6..8   LF vals
     I_MF = 9,     // 9..11  MF
     I_HF = 12,    // 12..13 HF (X, Y)
@@ -552,38 +554,170 @@ __device__ __forceinline__ float maximum_clamp(float v, float maxval) {
     return fmaf(v - c, kMul, c);
 }
 
-// MF vertical pass: MF with range operators, HF_pre = D - MF_raw (X, Y) with X suppressed by Y
-// written over the D planes (separatefrequencies.hpp:37-99,160-187).
-constexpr int kVMfSmem = (3 * (VB_TH + 18) * VB_TW + 2 * VB_TH * VB_TW) * 4;
+// MF band in one kernel: the separable 19-tap blur of the three D planes, then MF with the range
+// operators and HF_pre = D - MF with X suppressed by Y (separatefrequencies.hpp:37-99,160-187).
+// A CTA owns a 32-column strip of one image and walks MS_SEG rows of it in 64-row chunks. Per
+// chunk the three channels' D rows are staged (cp.async, zeros outside the image), the horizontal
+// pass writes its rows into a per-channel column-major buffer of 82 rows (the chunk's 64 and the
+// 9-row halos) and keeps the X and Y values of the output pixels, the 18 rows a chunk shares with
+// the next are carried over instead of blurred again, and the vertical pass runs the epilogue on
+// all three channels while the next chunk's rows are being staged. The horizontal pass's rows
+// never leave the SM: against a separate horizontal kernel (as the LF band still uses) this
+// saves writing and re-reading three planes and the vertical pass's re-reads of its halo rows
+// (201 -> 186 us per 3840x2160 pair). Taps, their order and the renormalisation are those of
+// butter_hblur_kernel and vblur3 with the sigma-3.225 kernel, so the values are the same bit for
+// bit as the two-pass form's. HF_pre goes to the dead TMP planes (I_HFP), not over D:
+// neighbouring CTAs still read D in their halos.
+// grid (ceil(w/32), ceil(h/MS_SEG), nimages)
+constexpr int MS_TW = 32, MS_CH = 64, MS_R = 9, MS_RA = 12;  // RA: R rounded up to a multiple of 4
+constexpr int MS_SEG = 4 * MS_CH;
+constexpr int MS_HR = MS_CH + 2 * MS_R;   // 82 rows per chunk
+constexpr int MS_IW = MS_TW + 2 * MS_RA;  // 56 staged columns, from x0 - 12
+constexpr int MS_RP = 60;                 // staged row pitch: 15 quads (conflict-free float4 rows)
+constexpr int MS_RAW = MS_HR * MS_RP;     // one channel's staged rows
+// Horizontal-pass buffer, per channel column-major: column x starts at x * 84 + 8 * (x / 8). 84
+// floats = 21 quads, odd, so the vertical pass's 16-byte loads of 8 neighbouring columns hit
+// distinct bank quads; the 8-float step between column groups spreads the horizontal pass's
+// stores of the four groups of a warp over all 32 banks.
+constexpr int MS_HP = 84;
+constexpr int MS_HPLANE = MS_TW * MS_HP + 8 * (MS_TW / 8 - 1);
+// the X and Y D values of the chunk's own pixels (rows 0..63) and of the next chunk's first 9 rows
+// (64..72), which only this chunk stages
+constexpr int MS_CTRR = MS_CH + MS_R;
+constexpr int MS_CTR = 2 * MS_CTRR * MS_TW;
+constexpr int kMfSmem = (3 * MS_RAW + 3 * MS_HPLANE + MS_CTR) * 4;
+
 template <bool HB>
-__global__ void __launch_bounds__(256) butter_mf_v_kernel(float* const* __restrict__ ib, BGeom g, int s) {
+__global__ void __launch_bounds__(256, 2) butter_mf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
-    float* ctr = sm + 3 * (VB_TH + 18) * VB_TW;
+    float* raw = sm;                          // [channel][82 staged rows][60]
+    float* hb = sm + 3 * MS_RAW;              // [channel][column-major buffer of 82 rows]
+    float* ctr = hb + 3 * MS_HPLANE;          // [X, Y][73 rows][32 columns]
     const int img = blockIdx.z;
-    float mf[3][8];
-    vblur3<3, 9>(sm, ctr, ib, g, img, s, I_TMP, I_XYB, 2, mf);
     const BScaleDev S = pick_scale(g, s);
-    const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    const int x = blockIdx.x * VB_TW + vc;
-    const int yb = blockIdx.y * VB_TH + 8 * vg;
-    if (x >= S.w) return;
-    float* d0 = iplane(ib, g, S, img, I_XYB + 0);
-    float* d1 = iplane(ib, g, S, img, I_XYB + 1);
+    const int tx0 = blockIdx.x * MS_TW, sy0 = blockIdx.y * MS_SEG;
+    const int nchunk = (min(MS_SEG, S.h - sy0) + MS_CH - 1) / MS_CH;
+    const int tid = threadIdx.x, vc = tid & 31, vg = tid >> 5;
+    // horizontal-pass tasks: output columns 8*hg .. 8*hg+7 of one staged row of one channel
+    const int hg = tid & 3;
+    float rx[8];
+    b_inv_mass_run<3, MS_R, 8>(tx0 + 8 * hg, S.w, rx);
     const float sx = 0.653020556257f, yw = 46.0f;
+    // staged row r is image row ty0 - 9 + r: a chunk's first staging takes rows 0..81, later ones
+    // rows 18..81 (the new rows; rows 0..17 of the buffer are carried, and the epilogue's own
+    // pixels are kept in ctr). The next chunk is staged as soon as this chunk's horizontal pass
+    // is done, so its loads run under the vertical pass and the epilogue.
+    auto stage = [&](int k) {
+        const int ty0 = sy0 + k * MS_CH;
 #pragma unroll
-    for (int o = 0; o < 8; o++) {
-        const int y = yb + o;
-        if (y < S.h) {
-            const int64_t i = (int64_t)y * S.p + x;
-            const int ci = (8 * vg + o) * VB_TW + vc;
-            float hx = ctr[ci] - mf[0][o];
-            const float hy = ctr[VB_TH * VB_TW + ci] - mf[1][o];
-            hx *= sx + div_nr(yw * (1.0f - sx), yw + hy * hy);
-            d0[i] = hx;
-            d1[i] = hy;
-            band_store<HB>(ib, g, S, img, I_MF + 0, i, remove_range(mf[0][o], 0.29f));
-            band_store<HB>(ib, g, S, img, I_MF + 1, i, amplify_range(mf[1][o], 0.1f));
-            band_store<HB>(ib, g, S, img, I_MF + 2, i, mf[2][o]);
+        for (int c = 0; c < 3; c++) {
+            const float* src = iplane(ib, g, S, img, I_XYB + c);
+            if (k == 0)
+                stage_tile_t<MS_HR, MS_IW / 4>(raw + c * MS_RAW, MS_RP, src, S.p, S.w, S.h, tx0 - MS_RA, ty0 - MS_R);
+            else
+                stage_tile_t<MS_CH, MS_IW / 4>(raw + c * MS_RAW + 2 * MS_R * MS_RP, MS_RP, src, S.p, S.w, S.h,
+                                               tx0 - MS_RA, ty0 + MS_R);
+        }
+        cp_async_commit();
+    };
+    stage(0);
+#pragma unroll 1
+    for (int k = 0; k < nchunk; k++) {
+        const int ty0 = sy0 + k * MS_CH;
+        cp_async_wait<0>();
+        __syncthreads();
+        // horizontal pass: buffer rows 0..81 (first chunk) or 18..81, from the staged row of the
+        // same index; the X and Y values of the output pixels (rows 9..72) go to ctr
+        const int h0 = k == 0 ? 0 : 2 * MS_R;
+        const int nrow = MS_HR - h0;
+#pragma unroll 1
+        for (int t = tid; t < 3 * nrow * 4; t += 256) {
+            const int cr = t >> 2;
+            const int c = cr / nrow, r = h0 + cr - c * nrow;
+            const float* row = raw + c * MS_RAW + r * MS_RP + 8 * hg;
+            float v[32];
+#pragma unroll
+            for (int j4 = 0; j4 < 8; j4++) {
+                const float4 q = *reinterpret_cast<const float4*>(row + 4 * j4);
+                v[4 * j4] = q.x;
+                v[4 * j4 + 1] = q.y;
+                v[4 * j4 + 2] = q.z;
+                v[4 * j4 + 3] = q.w;
+            }
+            if (c < 2 && r >= MS_R) {
+                float* cp = ctr + (c * MS_CTRR + r - MS_R) * MS_TW + 8 * hg;
+                *reinterpret_cast<float4*>(cp) = make_float4(v[MS_RA], v[MS_RA + 1], v[MS_RA + 2], v[MS_RA + 3]);
+                *reinterpret_cast<float4*>(cp + 4) = make_float4(v[MS_RA + 4], v[MS_RA + 5], v[MS_RA + 6], v[MS_RA + 7]);
+            }
+            float* d = hb + c * MS_HPLANE + 8 * hg * (MS_HP + 1) + r;
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                float a = 0.f;
+#pragma unroll
+                for (int i = 0; i < 2 * MS_R + 1; i++) a = fmaf(v[MS_RA - MS_R + o + i], c_bk[3][i], a);
+                d[o * MS_HP] = a * rx[o];
+            }
+        }
+        __syncthreads();
+        if (k + 1 < nchunk) stage(k + 1);
+        // vertical pass (column vc, rows 8*vg .. 8*vg+7 of the chunk, three channels) + epilogue
+        float ry[8];
+        b_inv_mass_run<3, MS_R, 8>(ty0 + 8 * vg, S.h, ry);
+        float mf[3][8];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float4* col = reinterpret_cast<const float4*>(hb + c * MS_HPLANE + vc * MS_HP + 8 * (vc >> 3) + 8 * vg);
+            float v[28];
+#pragma unroll
+            for (int j = 0; j < 7; j++) {
+                const float4 q = col[j];
+                v[4 * j] = q.x;
+                v[4 * j + 1] = q.y;
+                v[4 * j + 2] = q.z;
+                v[4 * j + 3] = q.w;
+            }
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                float a = 0.f;
+#pragma unroll
+                for (int i = 0; i < 2 * MS_R + 1; i++) a = fmaf(v[o + i], c_bk[3][i], a);
+                mf[c][o] = a * ry[o];
+            }
+        }
+        const int x = tx0 + vc;
+        if (x < S.w) {
+            float* h0p = iplane(ib, g, S, img, I_HFP + 0);
+            float* h1p = iplane(ib, g, S, img, I_HFP + 1);
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                const int y = ty0 + 8 * vg + o;
+                if (y < S.h) {
+                    const int64_t i = (int64_t)y * S.p + x;
+                    const int ci = (8 * vg + o) * MS_TW + vc;
+                    float hx = ctr[ci] - mf[0][o];
+                    const float hy = ctr[MS_CTRR * MS_TW + ci] - mf[1][o];
+                    hx *= sx + div_nr(yw * (1.0f - sx), yw + hy * hy);
+                    h0p[i] = hx;
+                    h1p[i] = hy;
+                    band_store<HB>(ib, g, S, img, I_MF + 0, i, remove_range(mf[0][o], 0.29f));
+                    band_store<HB>(ib, g, S, img, I_MF + 1, i, amplify_range(mf[1][o], 0.1f));
+                    band_store<HB>(ib, g, S, img, I_MF + 2, i, mf[2][o]);
+                }
+            }
+        }
+        __syncthreads();  // buffer rows and ctr are rewritten for the next chunk
+        if (k + 1 < nchunk) {
+            // carry buffer rows 64..81 to rows 0..17: 3 channels x 32 columns x 9 row pairs
+            for (int q = tid; q < 3 * MS_TW * 9; q += 256) {
+                const int c = q / (MS_TW * 9), e = q - c * (MS_TW * 9), xx = e / 9, rp = e - xx * 9;
+                float2* colp = reinterpret_cast<float2*>(hb + c * MS_HPLANE + xx * MS_HP + 8 * (xx >> 3));
+                colp[rp] = colp[MS_CH / 2 + rp];
+            }
+            // and ctr rows 64..72 (the next chunk's first 9 rows) to rows 0..8
+            for (int q = tid; q < 2 * MS_R * MS_TW; q += 256) {
+                const int c = q / (MS_R * MS_TW), e = q - c * (MS_R * MS_TW);
+                ctr[c * MS_CTRR * MS_TW + e] = ctr[(c * MS_CTRR + MS_CH) * MS_TW + e];
+            }
         }
     }
 }
@@ -613,8 +747,8 @@ __global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restr
     float rxy[6];
     tile_masses_r8<1>(x0, y0, S.w, S.h, rxy);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
-    tile_stage_r8(sm, iplane(ib, g, S, img, I_XYB), S.p, S.w, S.h, x0, y0);
-    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, img, I_XYB + 1), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm, iplane(ib, g, S, img, I_HFP), S.p, S.w, S.h, x0, y0);
+    tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, img, I_HFP + 1), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
@@ -1220,8 +1354,8 @@ int butter_prepare_device() {
     int rc = upload_butter_tables();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_v_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kVMfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmem));
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmemH));
     const DiffParams P = make_diff_params();
@@ -1340,11 +1474,11 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
             { ProfScope ps_("butter_opsin", st); butter_opsin_kernel<<<gt, 256, kTileSmem, st>>>(ib, g, s, intensity); }
             { ProfScope ps_("butter_hblur_lf", st); butter_hblur_kernel<4, 21><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
             { ProfScope ps_("butter_lf_v", st); butter_lf_v_kernel<<<gv, 256, kVLfSmem, st>>>(ib, g, s); }
-            { ProfScope ps_("butter_hblur_mf", st); butter_hblur_kernel<3, 9><<<gh, 256, 0, st>>>(ib, g, s, I_XYB, I_TMP); }
             {
-                ProfScope ps_("butter_mf_v", st);
-                if (half_bands) butter_mf_v_kernel<true><<<gv, 256, kVMfSmem, st>>>(ib, g, s);
-                else butter_mf_v_kernel<false><<<gv, 256, kVMfSmem, st>>>(ib, g, s);
+                ProfScope ps_("butter_mf", st);
+                const dim3 gmf((unsigned)ceil_div(sw, MS_TW), (unsigned)ceil_div(sh, MS_SEG), ni);
+                if (half_bands) butter_mf_kernel<true><<<gmf, 256, kMfSmem, st>>>(ib, g, s);
+                else butter_mf_kernel<false><<<gmf, 256, kMfSmem, st>>>(ib, g, s);
             }
             {
                 ProfScope ps_("butter_hf", st);

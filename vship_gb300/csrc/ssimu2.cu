@@ -747,13 +747,13 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
             // the 8 outputs it feeds. A chunk whose windows all lie inside the image needs neither
             // renormalisation nor bounds tests.
             const bool interior = x_inside && ty0 >= ST_R && ty0 + SC_TH + ST_R <= L.h;
-            f2_t a1[8], a2[8];
-            {
-                const f2_t z2 = f2_pack(0.f, 0.f);
+            // vertical pass + maps in one block per case, so that the scheduler can interleave
+            // the maps of completed outputs with the taps of the others
+            auto vpass = [&](f2_t* a1, f2_t* a2) {
 #pragma unroll
                 for (int o = 0; o < 8; o++) {
-                    a1[o] = z2;
-                    a2[o] = z2;
+                    a1[o] = f2_pack(0.f, 0.f);
+                    a2[o] = a1[o];
                 }
                 const int cb = vc * SC_HP + 8 * (vc >> 3) + 8 * vg;  // even: 16-byte aligned
                 const ulonglong2* c1 = reinterpret_cast<const ulonglong2*>(hp1 + cb);
@@ -777,8 +777,10 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
                         }
                     }
                 }
-            }
+            };
             if (interior) {
+                f2_t a1[8], a2[8];
+                vpass(a1, a2);
 #pragma unroll
                 for (int o = 0; o < 8; o++) {
                     float m1, m2, dd, m12;
@@ -792,6 +794,8 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
                     s2_pixel_maps(m1, m2, dd, m12, i1, i2, P);
                 }
             } else {
+                f2_t a1[8], a2[8];
+                vpass(a1, a2);
 #pragma unroll
                 for (int o = 0; o < 8; o++) {
                     const int y = ty0 + 8 * vg + o, x = tx0 + vc;
