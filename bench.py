@@ -306,8 +306,6 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands
         step()
     torch.cuda.synchronize()
     barrier(ws)
-    v.profile_report()  # clear
-    v.profile_enable(True)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -316,9 +314,16 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands
         step()
     e1.record(stream)
     torch.cuda.synchronize()
-    v.profile_enable(False)
     barrier(ws)
     sec = e0.elapsed_time(e1) / 1e3
+    # per-kernel breakdown: the same steps again with every launch bracketed by CUDA events (kept
+    # out of the timed region above: the events cost about 1 % there)
+    v.profile_report()  # clear
+    v.profile_enable(True)
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    v.profile_enable(False)
     prof = v.profile_report()
     launches = sum(n for n, _ in prof.values())
     result = out.cpu()

@@ -38,6 +38,7 @@ namespace vship {
 __constant__ float c_bk[5][43];
 __constant__ float c_bI[5][44];
 __constant__ float c_bInvIn[5];  // 1 / (full window mass): the renormalisation of interior outputs
+__constant__ f2_t c_bk2_t[3][17];  // the radius-8 kernels' taps (index 0..2) as {k, k} pairs
 
 static int upload_butter_tables() {
     static const double sig[5] = {1.2, 1.56416327805, 2.7, 3.22489901262, 7.15593339443};
@@ -56,6 +57,10 @@ static int upload_butter_tables() {
         }
     }
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bk, k, sizeof(k)));
+    float k2t[3][34];
+    for (int t = 0; t < 3; t++)
+        for (int i = 0; i < 17; i++) k2t[t][2 * i] = k2t[t][2 * i + 1] = k[t][i];
+    VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bk2_t, k2t, sizeof(k2t)));
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_bI, I, sizeof(I)));
     float inv[5];
     for (int t = 0; t < 5; t++) {
@@ -287,6 +292,73 @@ __device__ __forceinline__ void tile_blur_r8(const float* in, float* hb, const f
             for (int i = 0; i < 17; i++) a = fmaf(v[o + i], c_bk[KI][i], a);
             out[o] = a * rxy[o];
         }
+    }
+}
+
+// tile_blur_r8 on two planes at once, as f32x2 pairs (one instruction for both lanes, each
+// rounded as the scalar FMA, so the values are those of two tile_blur_r8 calls). hb2 holds
+// TB_TW x TB_HC {a, b} pairs, column-major (66 pairs = 33 quads per column, odd).
+template <int KI>
+__device__ __forceinline__ void tile_blur_r8_x2(const float* in0, const float* in1, float* hb2, const float rxy[6],
+                                                float out0[6], float out1[6]) {
+    const int tid = threadIdx.x;
+    {
+        const int hr = 32 * ((tid >> 5) & 1) + (tid & 31), hg = tid >> 6;
+        const float* r0 = in0 + hr * TB_IP + 8 * hg;
+        const float* r1 = in1 + hr * TB_IP + 8 * hg;
+        float v0[24], v1[24];
+#pragma unroll
+        for (int j4 = 0; j4 < 6; j4++) {
+            const float4 q0 = *reinterpret_cast<const float4*>(r0 + 4 * j4);
+            const float4 q1 = *reinterpret_cast<const float4*>(r1 + 4 * j4);
+            v0[4 * j4] = q0.x;
+            v0[4 * j4 + 1] = q0.y;
+            v0[4 * j4 + 2] = q0.z;
+            v0[4 * j4 + 3] = q0.w;
+            v1[4 * j4] = q1.x;
+            v1[4 * j4 + 1] = q1.y;
+            v1[4 * j4 + 2] = q1.z;
+            v1[4 * j4 + 3] = q1.w;
+        }
+        f2_t a[8];
+#pragma unroll
+        for (int o = 0; o < 8; o++) a[o] = f2_pack(0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 24; j++) {
+            const f2_t p = f2_pack(v0[j], v1[j]);
+#pragma unroll
+            for (int o = 0; o < 8; o++) {
+                const int i = j - o;  // tap index, ascending for each output
+                if (i >= 0 && i < 17) a[o] = f2_fma(p, c_bk2_t[KI][i], a[o]);
+            }
+        }
+        f2_t* dst = reinterpret_cast<f2_t*>(hb2) + (8 * hg) * TB_HC + hr;
+#pragma unroll
+        for (int o = 0; o < 8; o++) dst[o * TB_HC] = a[o];
+    }
+    __syncthreads();
+    {
+        const int vc = tid & 31, vg = tid >> 5;
+        const ulonglong2* col = reinterpret_cast<const ulonglong2*>(reinterpret_cast<const f2_t*>(hb2) + vc * TB_HC + 6 * vg);
+        f2_t a[6];
+#pragma unroll
+        for (int o = 0; o < 6; o++) a[o] = f2_pack(0.f, 0.f);
+#pragma unroll
+        for (int jj = 0; jj < 11; jj++) {
+            const ulonglong2 q = col[jj];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = 2 * jj + h;
+                const f2_t v = h ? q.y : q.x;
+#pragma unroll
+                for (int o = 0; o < 6; o++) {
+                    const int i = j - o;
+                    if (i >= 0 && i < 17) a[o] = f2_fma(v, c_bk2_t[KI][i], a[o]);
+                }
+            }
+        }
+#pragma unroll
+        for (int o = 0; o < 6; o++) f2_unpack(f2_mul(a[o], f2_pack(rxy[o], rxy[o])), out0[o], out1[o]);
     }
 }
 
@@ -738,9 +810,9 @@ __device__ __forceinline__ float mask_precompute(float hf_x, float uhf_x, float 
 // from the FP32 band values (an image shared by several pairs is not recomputed per pair).
 // grid (ceil(w/32), ceil(h/48), nimages)
 template <bool HB>
-__global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
+__global__ void __launch_bounds__(256, 5) butter_hf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
-    float* hb = sm + 2 * TB_RAW;
+    float* hb2 = sm + 2 * TB_RAW;
     const int img = blockIdx.z;
     const BScaleDev S = pick_scale(g, s);
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
@@ -752,39 +824,33 @@ __global__ void __launch_bounds__(256, 6) butter_hf_kernel(float* const* __restr
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
-    float hfx[6], uhfx[6];  // the X bands, kept for the mask precompute
+    float blr[2][6], pre[2][6];
+    tile_blur_r8_x2<1>(sm, sm + TB_RAW, hb2, rxy, blr[0], blr[1]);
 #pragma unroll
-    for (int c = 0; c < 2; c++) {
-        const float* in = sm + c * TB_RAW;
-        float blr[6], pre[6];
-        tile_blur_r8<1>(in, hb, rxy, blr);
+    for (int c = 0; c < 2; c++)
 #pragma unroll
-        for (int o = 0; o < 6; o++) pre[o] = in[(6 * vg + o + TB_R) * TB_IP + vc + TB_R];
-        __syncthreads();
+        for (int o = 0; o < 6; o++) pre[c][o] = sm[c * TB_RAW + (6 * vg + o + TB_R) * TB_IP + vc + TB_R];
 #pragma unroll
-        for (int o = 0; o < 6; o++) {
-            const int x = x0 + vc, y = y0 + 6 * vg + o;
-            float hf = blr[o], uhf = pre[o];
-            if (c == 0) {
-                uhf -= hf;
-                hf = remove_range(hf, 1.5f);
-                uhf = remove_range(uhf, 0.04f);
-                hfx[o] = hf;
-                uhfx[o] = uhf;
-            } else {
-                hf = maximum_clamp(hf, 28.4691806922f);
-                uhf -= hf;
-                uhf = maximum_clamp(uhf, 5.19175294647f);
-                uhf *= 2.69313763794f;
-                hf *= 2.155f;
-                hf = amplify_range(hf, 0.132f);
-            }
-            if (x < S.w && y < S.h) {
-                const int64_t i = (int64_t)y * S.p + x;
-                band_store<HB>(ib, g, S, img, I_HF + c, i, hf);
-                band_store<HB>(ib, g, S, img, I_UHF + c, i, uhf);
-                if (c == 1) iplane(ib, g, S, img, I_PRE)[i] = mask_precompute(hfx[o], uhfx[o], hf, uhf);
-            }
+    for (int o = 0; o < 6; o++) {
+        const int x = x0 + vc, y = y0 + 6 * vg + o;
+        float hfx = blr[0][o], uhfx = pre[0][o];
+        uhfx -= hfx;
+        hfx = remove_range(hfx, 1.5f);
+        uhfx = remove_range(uhfx, 0.04f);
+        float hf = blr[1][o], uhf = pre[1][o];
+        hf = maximum_clamp(hf, 28.4691806922f);
+        uhf -= hf;
+        uhf = maximum_clamp(uhf, 5.19175294647f);
+        uhf *= 2.69313763794f;
+        hf *= 2.155f;
+        hf = amplify_range(hf, 0.132f);
+        if (x < S.w && y < S.h) {
+            const int64_t i = (int64_t)y * S.p + x;
+            band_store<HB>(ib, g, S, img, I_HF + 0, i, hfx);
+            band_store<HB>(ib, g, S, img, I_UHF + 0, i, uhfx);
+            band_store<HB>(ib, g, S, img, I_HF + 1, i, hf);
+            band_store<HB>(ib, g, S, img, I_UHF + 1, i, uhf);
+            iplane(ib, g, S, img, I_PRE)[i] = mask_precompute(hfx, uhfx, hf, uhf);
         }
     }
 }
@@ -1344,6 +1410,7 @@ static DiffParams make_diff_params() {
 }
 
 constexpr int kTileSmem = (2 * TB_RAW + TB_HPL) * 4;
+constexpr int kTileSmem2 = (2 * TB_RAW + 2 * TB_HPL) * 4;  // with a pair buffer (tile_blur_r8_x2)
 
 __global__ void butter_identity_pairs_kernel(int2* pimg, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1482,8 +1549,8 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
             }
             {
                 ProfScope ps_("butter_hf", st);
-                if (half_bands) butter_hf_kernel<true><<<gt, 256, kTileSmem, st>>>(ib, g, s);
-                else butter_hf_kernel<false><<<gt, 256, kTileSmem, st>>>(ib, g, s);
+                if (half_bands) butter_hf_kernel<true><<<gt, 256, kTileSmem2, st>>>(ib, g, s);
+                else butter_hf_kernel<false><<<gt, 256, kTileSmem2, st>>>(ib, g, s);
             }
         }
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
