@@ -37,6 +37,9 @@ public:
     double* norms = nullptr;        // [pair][3]
     int2* pimg_identity = nullptr;  // (2p, 2p + 1): the paired form's pair table
     float** ibase = nullptr;        // device: base of image i = work + i * img_floats
+    // the half scale's chain runs on `side` beside the full scale's (butter_enqueue)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
     // Paired form: images 2p and 2p + 1 are pair p's reference and distorted frames.
     int init(int64_t width, int64_t height, int qnorm, float intensity, int max_pairs);
@@ -66,9 +69,13 @@ int butter_norm_tiles(int64_t w, int64_t h);
 // is image i's frame), then every pair of pimg (indices into ib) runs the pair stage. partials:
 // npairs x 3 x norm_tiles floats; norms_out: npairs x 3 doubles; distmap_out: null or npairs maps;
 // yuv: format of IN_YUV frames (null: 10-bit 4:2:0 BT.709 limited, left siting); half_bands:
-// the images' layout (butter_image_floats).
+// the images' layout (butter_image_floats). side, ev_fork, ev_join (optional): a second stream
+// and two events of the caller's; the half scale's chain then runs on side beside the full
+// scale's (the two share nothing until the full-scale diffmap adds the half-scale map), unless
+// per-kernel profiling is on.
 int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* const* ib, const FrameDesc* frames_dev,
                    int nstage, const int2* pimg, int npairs, int intype, float* partials, double* norms_out,
-                   float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr, bool half_bands = false);
+                   float* distmap_out, cudaStream_t st, const YuvParams* yuv = nullptr, bool half_bands = false,
+                   cudaStream_t side = nullptr, cudaEvent_t ev_fork = nullptr, cudaEvent_t ev_join = nullptr);
 
 }  // namespace vship
