@@ -459,17 +459,18 @@ __global__ void __launch_bounds__(256, 5) butter_opsin_kernel(float* const* __re
 }
 
 // ------------------------------------------------------------------------------------------
-// Separable horizontal pass, radius R (21 or 9): 128x16 row tiles; each thread makes 8
-// consecutive outputs of a tile. The input rows start at x0 - RA (RA = R rounded up to a multiple
-// of 4, so the cp.async chunks are 16-byte aligned) and are read back as float4 (pitch 180 = 45
-// quads: conflict-free); the thread's window starts RA - R floats into its first quad. A CTA
+// Separable horizontal pass of radius R (R = 21: the LF band's 43 taps): 128x16 row tiles; each
+// thread makes 8 consecutive outputs of a tile. The input rows start at x0 - RA (RA = R rounded
+// up to a multiple of 4, so the cp.async chunks are 16-byte aligned) and are read back as float4
+// (pitch 180 = 45 quads: conflict-free); the thread's window starts RA - R floats into its first
+// quad. A CTA
 // walks HB_NT row tiles down the column, staging tile t + 1 while it computes tile t, so the
 // global-load latency hides behind the taps of the previous tile.
 // grid (ceil(w/128), ceil(h/(16*HB_NT)), 3*nimages): z -> image = z/3, plane = src_id + z%3.
 constexpr int HB_TW = 128, HB_TH = 16, HB_P = 180, HB_NT = 4;
 
 template <int KI, int R>
-__global__ void __launch_bounds__(256, R == 9 ? 6 : 3) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s,
+__global__ void __launch_bounds__(256, 3) butter_hblur_kernel(float* const* __restrict__ ib, BGeom g, int s,
                                                               int src_id, int dst_id) {
     __shared__ __align__(16) float in[2][HB_TH * HB_P];
     constexpr int RA = (R + 3) & ~3;
