@@ -6,10 +6,11 @@
 //                        from shared memory (the pyramid is tile-local: a 2^k-aligned level-0
 //                        tile maps exactly onto its level-k tile, edge clamp included).
 //                        Reference: ssimu2/main.hpp:15-32, makeXYB.hpp:4-98, downsample.hpp:3-31.
-//   2. ssimu2_stats    : all six scales in one launch. Per 32x192 segment, in 48-row chunks,
-//                        it stages I1 and I2 (8-px halo, zero outside) in shared memory, runs the
-//                        17-tap separable Gaussian (border-renormalised) for four moments (mu1,
-//                        mu2, E[I1^2 + I2^2], E[I1 I2]) with register blocking and a ring of
+//   2. ssimu2_stats    : all six scales in one launch. Per 32-column segment (576 or 192 rows),
+//                        in 64- or 48-row chunks, it stages I1 and I2 (8-px halo, zero outside)
+//                        in shared memory, runs the 17-tap separable Gaussian (border-
+//                        renormalised) for four moments (mu1, mu2, E[(I1 - I2)^2], E[I1 I2]) with
+//                        register blocking and a carry buffer or a ring of
 //                        horizontal-pass rows, forms the SSIM / artifact / detail-loss maps and
 //                        emits 18 partial sums (6 pools x 3 channels) per CTA.
 //                        Reference: ssimu2/score.hpp:95-196, gaussianblur.hpp:24-92.
@@ -297,7 +298,7 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) ssimu2_pyramid_pair
 // Kernel 2: fused moment blur + SSIM/edge maps + per-CTA pooling, all scales in one launch.
 // grid (tiles_total, npairs), 256 threads, dynamic smem kStatsSmem, three CTAs per SM.
 //
-// Per CTA: one segment of one scale -- a 32-column strip, ST_SEG rows tall -- walked down in
+// Per CTA: one segment of one scale -- a 32-column strip, L.seg rows tall -- walked down in
 // chunks of 48 output rows. For each channel and chunk the raw I1 and I2 rows (8-px halo) are
 // staged with cp.async (bytes outside the image are zero-filled); one CTA's loads overlap the
 // arithmetic of the other CTAs on its SM. The horizontal pass reads the raw rows as float4 (row
@@ -308,7 +309,14 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) ssimu2_pyramid_pair
 // halo is blurred horizontally once per segment instead of once per chunk (64 instead of 48
 // horizontal rows per 48 output rows).
 constexpr int ST_TW = 32, ST_TH = 48, ST_R = 8;
-constexpr int ST_SEG = 4 * ST_TH;        // segment height (output rows)
+// Segment heights (output rows). Each segment's first chunk blurs the 16 halo rows above it, so
+// taller segments blur fewer rows twice: a level that still has at least kSegTallMin segments of
+// ST_SEG_TALL rows per frame uses them (1080p: 3.0 % faster stats than 192 rows throughout, 576
+// measured best among 384, 576 and 768); smaller levels keep ST_SEG rows, so that a small frame
+// still spreads over enough CTAs.
+constexpr int ST_SEG = 4 * ST_TH;
+constexpr int ST_SEG_TALL = 12 * ST_TH;
+constexpr int kSegTallMin = 24;
 constexpr int ST_IW = ST_TW + 2 * ST_R;  // 48 input columns
 constexpr int ST_IH = ST_TH + 2 * ST_R;  // 64 raw rows per chunk (image rows ty0 - 8 ..)
 constexpr int ST_RP = 52;                // raw-tile row pitch (floats; 16-byte multiple, 13 quads)
@@ -379,7 +387,7 @@ __device__ __forceinline__ void s2_pixel_maps(float m1, float m2, float dd, floa
 // FP16 delta tile: 64 rows x 48 halves, row pitch 56 halves (7 quads: conflict-free 16-byte reads)
 constexpr int ST_DP = 56;
 
-// One segment (32 columns x up to ST_SEG rows) of one scale: the four moments, the maps and 18
+// One segment (32 columns x up to L.seg rows) of one scale: the four moments, the maps and 18
 // pooled sums written to out[pool * stride] (pool = map * 2 + norm, times 3 channels). im1 / im2
 // point at the tile's scale in the channel-0 plane; DELTA: im2 holds FP16 differences against im1.
 template <bool DELTA>
@@ -392,8 +400,8 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
     const float* im2 = static_cast<const float*>(im2v);
     const __half* im2h = static_cast<const __half*>(im2v);
     const int tx0 = (lt % L.tiles_x) * ST_TW;
-    const int sy0 = (lt / L.tiles_x) * ST_SEG;
-    const int nchunk = (min(ST_SEG, L.h - sy0) + ST_TH - 1) / ST_TH;
+    const int sy0 = (lt / L.tiles_x) * L.seg;
+    const int nchunk = (min(L.seg, L.h - sy0) + ST_TH - 1) / ST_TH;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool x_inside = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w;
 
@@ -584,7 +592,7 @@ __device__ __forceinline__ void stats_tile(const float* __restrict__ im1, const 
 }
 
 // ------------------------------------------------------------------------------------------
-// Second tile shape of the stats kernel: the same 32 x 192 segments, walked in 64-row chunks.
+// Second tile shape of the stats kernel: the same 32-column segments, walked in 64-row chunks.
 // The horizontal pass writes a column-major buffer of 80 rows (the chunk's 64 and the 8-row
 // halos) instead of the ring, and the 16 rows a chunk shares with the next are carried over
 // (copied from buffer rows 64..79 to 0..15) rather than blurred again, so every chunk after the
@@ -606,7 +614,8 @@ constexpr int SC_HPLANE = ST_TW * SC_HP + 8 * (ST_TW / 8 - 1);
 // smem: the 2 raw images, two float-pair planes {m1, m2} and {s11 + s22, s12}, the per-warp
 // pools: 74.4 KB, still three CTAs per SM
 constexpr int kStatsSmemC = (2 * SC_RAW + 4 * SC_HPLANE + 3 * 8 * 6) * 4;
-static_assert(ST_SEG % SC_TH == 0, "both shapes walk the same segments");
+static_assert(ST_SEG % SC_TH == 0 && ST_SEG_TALL % SC_TH == 0 && ST_SEG_TALL % ST_TH == 0,
+              "both shapes walk the same segments");
 
 template <bool DELTA>
 __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, const void* __restrict__ im2v,
@@ -619,8 +628,8 @@ __device__ __forceinline__ void stats_tile_c64(const float* __restrict__ im1, co
     const float* im2 = static_cast<const float*>(im2v);
     const __half* im2h = static_cast<const __half*>(im2v);
     const int tx0 = (lt % L.tiles_x) * ST_TW;
-    const int sy0 = (lt / L.tiles_x) * ST_SEG;
-    const int nchunk = (min(ST_SEG, L.h - sy0) + SC_TH - 1) / SC_TH;
+    const int sy0 = (lt / L.tiles_x) * L.seg;
+    const int nchunk = (min(L.seg, L.h - sy0) + SC_TH - 1) / SC_TH;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool x_inside = tx0 >= ST_R && tx0 + ST_TW + ST_R <= L.w;
     // H pass: output columns 8*hg .. 8*hg+7 of 8 consecutive raw rows per warp x 4 column groups.
@@ -1032,7 +1041,8 @@ Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h) {
         L.off = off;
         off += round_up((int64_t)L.pitch * ch, 64);
         L.tiles_x = (int)ceil_div(cw, ST_TW);
-        L.tiles_y = (int)ceil_div(ch, ST_SEG);
+        L.seg = L.tiles_x * ceil_div(ch, ST_SEG_TALL) >= kSegTallMin ? ST_SEG_TALL : ST_SEG;
+        L.tiles_y = (int)ceil_div(ch, L.seg);
         g.tile_begin[s] = tiles;
         tiles += L.tiles_x * L.tiles_y;
         cw = half_dim(cw);

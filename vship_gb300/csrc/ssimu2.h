@@ -16,11 +16,12 @@ constexpr int kPyrTile = 32;
 struct Ssimu2Level {
     int w, h, pitch;
     int tiles_x, tiles_y;
+    int seg;      // rows per stats-kernel segment at this level (576 or 192)
     int64_t off;  // element offset of the level inside one channel plane
 };
 
 // Geometry of the 6-scale pyramid and of the stats-kernel tiling (segments of 32 columns x
-// 192 rows, one CTA each).
+// `seg` rows, one CTA each).
 struct Ssimu2Geom {
     Ssimu2Level lv[6];
     int tile_begin[7];
