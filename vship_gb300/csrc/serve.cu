@@ -57,6 +57,9 @@ int Server::create(int nres_, const int* widths, const int* heights, int intype_
     VSHIP_CUDA_TRY(vship_malloc((void**)&sgeom_d, sizeof(Ssimu2Geom) * nres));
     VSHIP_CUDA_TRY(cudaMemcpy(sgeom_d, sgeom, sizeof(Ssimu2Geom) * nres, cudaMemcpyHostToDevice));
     VSHIP_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    VSHIP_CUDA_TRY(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    VSHIP_CUDA_TRY(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    VSHIP_CUDA_TRY(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
     props.location.type = cudaMemLocationTypeDevice;
@@ -496,7 +499,7 @@ int Server::launch(Batch* b) {
                             reinterpret_cast<const FrameDesc*>(dtab + G.t_fr), G.nstage,
                             reinterpret_cast<const int2*>(dtab + G.t_pi), G.npairs, intype,
                             reinterpret_cast<float*>(block + G.part), dres + b->out_off[G.reqs[0]], nullptr, st,
-                            &yuv[G.res], (flags & SERVE_BUTTER_HALF_BANDS) != 0);
+                            &yuv[G.res], (flags & SERVE_BUTTER_HALF_BANDS) != 0, side, ev_fork, ev_join);
     }
     if (!rc && cudaMemcpyAsync(h + b->res_off, dres, res_doubles * sizeof(double), cudaMemcpyDeviceToHost, st) !=
                    cudaSuccess)
@@ -550,9 +553,13 @@ void Server::destroy() {
     if (pool) cudaMemPoolDestroy(pool);
     if (sgeom_d) cudaFree(sgeom_d);
     if (st) cudaStreamDestroy(st);
+    if (side) cudaStreamDestroy(side);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     pool = nullptr;
     sgeom_d = nullptr;
-    st = nullptr;
+    st = side = nullptr;
+    ev_fork = ev_join = nullptr;
     cudaSetDevice(dev);
 }
 

@@ -92,6 +92,9 @@ private:
     int bnorm_tiles[kMaxRes]{};
 
     cudaStream_t st = nullptr;
+    // Butteraugli's half-scale chain runs on `side` beside the full scale's (butter_enqueue)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaMemPool_t pool = nullptr;
     Admission adm;
     SourceCache<void*> cache;
