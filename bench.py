@@ -766,7 +766,10 @@ def bench_workload(v, kind, args, ws, rank):
         "gpu_launches": launches,
         "clocks": clocks,
         "score_check": {"device_vs_e2e_max_abs": float(abs(
-            (dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy()[0::3]) - host_scores).max())},
+            (dev_scores.numpy() if kind == "ssimu2" else dev_scores.numpy()[0::3]) - host_scores).max()),
+                        **({"note": "SSIMU2 launches of 16 or more pairs tile the stats kernel's pooled sums "
+                                    "in taller segments than single-pair calls: the two agree to FP32 rounding "
+                                    "of those sums, not bit for bit"} if kind == "ssimu2" else {})},
     }
     if half:
         res["fp16_bands"] = half

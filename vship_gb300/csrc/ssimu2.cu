@@ -310,10 +310,11 @@ __global__ void __launch_bounds__(256, IT == IN_YUV ? 6 : 8) ssimu2_pyramid_pair
 // horizontal rows per 48 output rows).
 constexpr int ST_TW = 32, ST_TH = 48, ST_R = 8;
 // Segment heights (output rows). Each segment's first chunk blurs the 16 halo rows above it, so
-// taller segments blur fewer rows twice: a level that still has at least kSegTallMin segments of
-// ST_SEG_TALL rows per frame uses them (1080p: 3.0 % faster stats than 192 rows throughout, 576
-// measured best among 384, 576 and 768); smaller levels keep ST_SEG rows, so that a small frame
-// still spreads over enough CTAs.
+// taller segments blur fewer rows twice. In a tall geometry (make_ssimu2_geom(w, h, true), for
+// launches of many pairs) a level that still has at least kSegTallMin segments of ST_SEG_TALL
+// rows per frame uses them (1080p: 3.0 % faster stats than 192 rows throughout, 576 measured best
+// among 384, 576 and 768); other levels, and every level of the default geometry, keep ST_SEG
+// rows, so that a small frame or a lone pair still spreads over enough CTAs.
 constexpr int ST_SEG = 4 * ST_TH;
 constexpr int ST_SEG_TALL = 12 * ST_TH;
 constexpr int kSegTallMin = 24;
@@ -1028,7 +1029,7 @@ __global__ void __launch_bounds__(kFinThreads) ssimu2_multi_finalize_kernel(cons
 // ------------------------------------------------------------------------------------------
 // Host side
 
-Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h) {
+Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h, bool tall) {
     Ssimu2Geom g{};
     int64_t off = 0;
     int tiles = 0;
@@ -1041,7 +1042,7 @@ Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h) {
         L.off = off;
         off += round_up((int64_t)L.pitch * ch, 64);
         L.tiles_x = (int)ceil_div(cw, ST_TW);
-        L.seg = L.tiles_x * ceil_div(ch, ST_SEG_TALL) >= kSegTallMin ? ST_SEG_TALL : ST_SEG;
+        L.seg = tall && L.tiles_x * ceil_div(ch, ST_SEG_TALL) >= kSegTallMin ? ST_SEG_TALL : ST_SEG;
         L.tiles_y = (int)ceil_div(ch, L.seg);
         g.tile_begin[s] = tiles;
         tiles += L.tiles_x * L.tiles_y;
@@ -1060,6 +1061,7 @@ int Ssimu2Engine::init(int64_t width, int64_t height, int max_pairs_, bool fp16_
     max_pairs = max_pairs_;
     fp16 = fp16_deltas;
     geom = make_ssimu2_geom(w, h);
+    geom_tall = make_ssimu2_geom(w, h, true);  // no more tiles than geom: the partials fit either
     int rc = upload_constants_once();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(ssimu2_stats_kernel<kPlainShape>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1101,6 +1103,7 @@ int Ssimu2Engine::launch(const FrameDesc* frames_dev, int intype, int npairs, do
     if (npairs <= 0 || npairs > max_pairs) return E_BAD_POINTER;
     const YuvParams yp = yuv ? *yuv : yuv420p10_params();
     if (fp16) return launch_fp16(frames_dev, intype, npairs, out_scores, st, yp);
+    const Ssimu2Geom& geom = npairs >= kSsimu2TallPairs ? geom_tall : this->geom;
     dim3 g1((unsigned)ceil_div(w, kPyrTile), (unsigned)ceil_div(h, kPyrTile), (unsigned)(2 * npairs));
     {
     ProfScope ps("ssimu2_pyramid", st);
@@ -1141,6 +1144,7 @@ static void launch_pyramid_pair(const FrameDesc* frames, float* ref, __half* d16
 // differences against them, then the stats kernel staging the deltas as halves.
 int Ssimu2Engine::launch_fp16(const FrameDesc* frames_dev, int intype, int npairs, double* out_scores,
                               cudaStream_t st, const YuvParams& yp) {
+    const Ssimu2Geom& geom = npairs >= kSsimu2TallPairs ? geom_tall : this->geom;
     const dim3 g1((unsigned)ceil_div(w, kPyrTile), (unsigned)ceil_div(h, kPyrTile), (unsigned)npairs);
     {
         ProfScope ps("ssimu2_pyramid", st);

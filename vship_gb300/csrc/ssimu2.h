@@ -29,9 +29,17 @@ struct Ssimu2Geom {
     int64_t plane_elems;  // elements of one channel's whole pyramid
 };
 
-Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h);
+// tall: stats segments of 576 rows on the levels that keep enough of them (ssimu2.cu); otherwise
+// 192 rows throughout. The pyramid layout is the same either way.
+Ssimu2Geom make_ssimu2_geom(int64_t w, int64_t h, bool tall = false);
 
 // Device workspace and launch sequence for up to `max_pairs` frame pairs of one resolution.
+// Launches of at least this many pairs use the tall stats segments (geom_tall): 2 % more pairs/s
+// at 1080p. Smaller launches keep 192-row segments, which spread one pair over more CTAs (a lone
+// 1080p pair takes 12 % longer with the tall ones). The two tile the pooled sums differently, so
+// scores of the two kinds of launch agree to FP32 rounding of the partial sums, not bit for bit.
+constexpr int kSsimu2TallPairs = 16;
+
 // Layout: pyr[pair][image][channel][plane_elems], partials[pair][tile][18], scores[pair]. With
 // fp16 deltas the distorted images' pyramids are stored as half(distorted - reference) in d16
 // [pair][channel][plane_elems], after the references' FP32 pyramids pyr[pair][channel][...].
@@ -40,7 +48,8 @@ public:
     int64_t w = 0, h = 0;
     int max_pairs = 0;
     bool fp16 = false;
-    Ssimu2Geom geom{};
+    Ssimu2Geom geom{};       // 192-row stats segments: launches of fewer than kSsimu2TallPairs pairs
+    Ssimu2Geom geom_tall{};  // 576-row segments where a level keeps enough of them: larger launches
     float* pyr = nullptr;
     __half* d16 = nullptr;
     float* partials = nullptr;
