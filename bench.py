@@ -25,8 +25,8 @@ A step scores every pair of the workload once.
 
   reference_cuda: the reference's own CUDA build (oracle/_ref/libvship_ref.so, built from
           pkp24/Vship's sources by oracle/ref_build.py) through its stock C ABI calls on the same
-          pinned RGB48 host planes, 3 and 8 handler threads; its frame-pairs/s, this build's e2e and
-          device rates over it, and the score / norm differences on every pair.
+          pinned RGB48 host planes, 3 and 8 handler threads; its frame-pairs/s, this library's e2e
+          and device rates over it, and the score / norm differences on every pair.
   error_vs_fp64: each reported form's error against the FP64 oracle on the first pairs.
 
 --impl reference runs the reference's math on the host cores instead (the reference has no CPU
@@ -447,9 +447,9 @@ REF_THREADS = (3, 8)
 def run_reference_cuda(kind, ref, dst, steps, warmup):
     """The reference's own CUDA build (oracle/_ref/libvship_ref.so, pkp24/Vship src/VshipLib.cpp
     compiled for sm_103a) through its stock C ABI calls -- Vship_ComputeSSIMU2Uint16 /
-    Vship_ComputeButteraugliUint16 -- from the same pinned RGB48 host planes as this build's e2e,
-    one handler per host thread, at the 3 threads its documentation recommends and at 8 (this
-    build's e2e setting); the better rate is the baseline. Every call copies its planes
+    Vship_ComputeButteraugliUint16 -- from the same pinned RGB48 host planes as this library's e2e,
+    one handler per host thread, at the 3 threads its documentation recommends and at 8 (the
+    e2e setting of this library); the better rate is the baseline. Every call copies its planes
     host->device, computes and returns its result, as the reference always does. Returns None when
     the library is not built on this machine.
 

@@ -12,7 +12,7 @@ Two sources of reference results:
 Tolerances are the ones the path is specified to: SSIMU2 within 1e-3 absolute of the reference;
 Butteraugli norms within 1e-4 relative; distortion maps within 1e-3 of the map's maximum per pixel.
 Where the reference's own FP32 result is further than the tolerance from the FP64 oracle (SSIMU2
-on frames of a few thousand pixels, whose coarsest scales hold a handful of pixels), this build
+on frames of a few thousand pixels, whose coarsest scales hold a handful of pixels), libvship
 must instead be within the tolerance of the FP64 oracle: there the reference's rounding error,
 not a difference of method, is what separates the two.
 """

@@ -359,7 +359,7 @@ const char* error_name_and_text(int e) {
         case E_DEVICE_COUNT: return "DeviceCountError: the number of GPUs could not be queried. (Advice) check the NVIDIA driver installation";
         case E_NO_DEVICE: return "NoDeviceDetected: no GPU was found. (Advice) check the NVIDIA driver and that the process can see a GPU";
         case E_BAD_DEVICE_ARG: return "BadDeviceArgument: gpu_id is negative or not smaller than the number of GPUs";
-        case E_BAD_DEVICE_CODE: return "BadDeviceCode: a GPU kernel or CUDA call failed. (Advice) this build targets sm_103a (GB300); check the GPU model";
+        case E_BAD_DEVICE_CODE: return "BadDeviceCode: a GPU kernel or CUDA call failed. (Advice) this library targets sm_103a (GB300); check the GPU model";
         case E_BAD_HANDLER: return "BadHandler: the handler was never initialised or was already freed";
         case E_BAD_POINTER: return "BadPointer: a pointer argument was NULL, a stride was smaller than a row, or the memory was not from Vship_PinnedMalloc";
         default: return "BadErrorType: unknown error";
