@@ -275,7 +275,7 @@ def yuv_table(v, yuv, start, count):
 
 def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands=False, fp16_deltas=False):
     """Batched device-resident throughput; returns (seconds for `steps` steps, profile dict, launches,
-    results). half_bands: Butteraugli with its MF, HF and UHF bands stored as FP16."""
+    results). half_bands: Butteraugli with its UHF bands stored as FP16."""
     import torch
     if yuv is not None:
         yuvt, (w, h) = yuv
@@ -729,7 +729,7 @@ def bench_workload(v, kind, args, ws, rank):
                 "device_bytes_per_pair": int(L.Vship_ButteraugliDeviceBytesEx(w, h, 1, v.BUTTER_HALF_BANDS)),
                 "device_bytes_per_pair_fp32": int(L.Vship_ButteraugliDeviceBytes(w, h, 1)),
                 "kernel_ms": {k: round(t, 3) for k, (n, t) in sorted(hprof.items(), key=lambda x: -x[1][1])},
-                "note": "MF, HF and UHF bands stored as FP16, all arithmetic FP32; error in error_vs_fp64"}
+                "note": "UHF bands stored as FP16, all arithmetic FP32; error in error_vs_fp64"}
     del ref16, dst16
     torch.cuda.empty_cache()
     # 10-bit 4:2:0 planes converted on the GPU (a quarter of the bytes of float RGB)

@@ -277,13 +277,13 @@ EXPORTPREPROCESS uint64_t Vship_ButteraugliDeviceBytes(int width, int height, in
 /* Butteraugli with FP16 band storage -- no counterpart in the reference, whose planes are all
  * FP32 (src/butter/main.hpp:141-195 allocates them per call).
  *
- * With Vship_ButterHalfBands the MF, HF and UHF frequency bands of every image, which only the
- * pair stage reads, are stored as FP16; every other plane and all arithmetic stay FP32. An image
- * then takes 12.5 instead of 16 FP32-plane equivalents per scale (a 3840x2160 pair: 1.07 instead
- * of 1.36 GB of device memory) at the same throughput, for an accuracy cost: the norms move by
- * the FP16 rounding of the bands. Against the FP64 oracle: about 2e-6 relative for the 2- and
- * 3-norm on blurred and noisy pairs (1e-7 with FP32 planes), up to 5e-5 on light block-DCT
- * distortions, and up to 3e-4 for the inf-norm, which follows one pixel.
+ * With Vship_ButterHalfBands the UHF frequency bands (X, Y) of every image, which only the pair
+ * stage reads, are stored as FP16; every other plane and all arithmetic stay FP32. An image then
+ * takes 15 instead of 16 FP32-plane equivalents per scale (a 3840x2160 pair: 1.28 instead of
+ * 1.36 GB of device memory) at the same throughput. The norms move by the FP16 rounding of those
+ * bands: against the FP64 oracle, up to about 5e-6 relative for the 2- and 3-norm and 5e-5 for
+ * the inf-norm, which follows one pixel (within 1e-4 on every frame evaluated). FP16 storage of
+ * the HF or MF bands as well would move the norms by up to 1e-3 and is not offered.
  * Vship_ButteraugliInitEx is Vship_ButteraugliInitv2 with flags (host-buffer Compute calls);
  * Vship_ButteraugliBatchInitEx is Vship_ButteraugliBatchInit with flags; flags = 0 gives the
  * FP32 planes of the plain functions. Other flag bits are refused (Vship_BadPointer). */
@@ -366,7 +366,7 @@ typedef enum {
     Vship_MultiFp16 = 4,
     Vship_MultiNoGraph = 8,
     Vship_MultiAutotune = 16,
-    Vship_MultiButterHalfBands = 32, /* Butteraugli MF, HF and UHF bands as FP16 (Vship_ButterHalfBands) */
+    Vship_MultiButterHalfBands = 32, /* Butteraugli UHF bands as FP16 (Vship_ButterHalfBands) */
 } Vship_MultiFlags;
 EXPORTPREPROCESS Vship_Exception Vship_MultiInit(Vship_MultiHandler* handler, int nres, const int* widths,
                                                  const int* heights, const int* max_sources, const int* max_pairs,
@@ -408,7 +408,7 @@ typedef struct {
 } Vship_ServeHandler;
 typedef enum { Vship_ServeSSIMU2 = 0, Vship_ServeButteraugli = 1 } Vship_ServeMetric;
 #define Vship_ServeFp32Candidates 1
-#define Vship_ServeButterHalfBands 2 /* Butteraugli MF, HF and UHF bands as FP16 (Vship_ButterHalfBands) */
+#define Vship_ServeButterHalfBands 2 /* Butteraugli UHF bands as FP16 (Vship_ButterHalfBands) */
 typedef struct {
     uint64_t request_id;
     int metric;      /* Vship_ServeMetric */

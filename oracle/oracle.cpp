@@ -727,7 +727,8 @@ void psycho_image(std::vector<T> src[3], int64_t w, int64_t h, float intensity, 
 // half_bands models FP16 storage of the frequency bands that the pair stage reads: 1 = every
 // band of both images rounded to half; 2 = reference bands exact, distorted bands stored as
 // half(distorted - reference) and read back as reference + delta; 3 = as 2 but the LF bands
-// kept exact; 4 = as 1 but the LF bands kept exact (the CUDA path's half-band storage).
+// kept exact; 4 = the UHF bands of both images rounded to half, the others exact (the CUDA
+// path's half-band storage).
 template <typename T>
 void store_bands_half(Bands<T>& b1, Bands<T>& b2, int half_bands) {
     auto each = [&](std::vector<T>& a, std::vector<T>& b) {
@@ -740,14 +741,14 @@ void store_bands_half(Bands<T>& b1, Bands<T>& b2, int half_bands) {
             }
         }
     };
-    for (int c = 0; c < 3; c++) {
-        if (half_bands != 3 && half_bands != 4) each(b1.lf[c], b2.lf[c]);
-        each(b1.mf[c], b2.mf[c]);
+    if (half_bands != 4) {
+        for (int c = 0; c < 3; c++) {
+            if (half_bands != 3) each(b1.lf[c], b2.lf[c]);
+            each(b1.mf[c], b2.mf[c]);
+        }
+        for (int c = 0; c < 2; c++) each(b1.hf[c], b2.hf[c]);
     }
-    for (int c = 0; c < 2; c++) {
-        each(b1.hf[c], b2.hf[c]);
-        each(b1.uhf[c], b2.uhf[c]);
-    }
+    for (int c = 0; c < 2; c++) each(b1.uhf[c], b2.uhf[c]);
 }
 
 template <typename T>
@@ -891,7 +892,7 @@ int oracle_butteraugli(const uint8_t* const* src1, const uint8_t* const* src2, i
     if (width <= 0 || height <= 0 || !norms3) return 1;
     // precision 16: FP32 with every band stored as half; 17: FP32 with the distorted image's
     // bands stored as half deltas against the reference's; 18: 17 with the LF bands exact;
-    // 19: 16 with the LF bands exact (MF, HF and UHF as half)
+    // 19: FP32 with the UHF bands stored as half
     if (precision == 64)
         butteraugli<double>(src1, src2, stride1, stride2, width, height, intype, qnorm, intensity, nthreads, norms3,
                             distmap);

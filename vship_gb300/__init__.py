@@ -28,7 +28,7 @@ EXCEPTION_NAMES = ["NoError", "OutOfVRAM", "OutOfRAM", "DifferingInputType", "No
 # Vship_InputType
 IN_UINT8, IN_UINT16, IN_HALF, IN_FLOAT, IN_YUV = 0, 1, 2, 3, 4
 IN_YUV420P10 = IN_YUV  # the default Y'CbCr format (10-bit 4:2:0, BT.709, limited, left siting)
-BUTTER_HALF_BANDS = 1  # Vship_ButterHalfBands: Butteraugli MF, HF and UHF bands stored as FP16
+BUTTER_HALF_BANDS = 1  # Vship_ButterHalfBands: Butteraugli UHF bands stored as FP16
 SSIMU2_FP16_DELTAS = 1  # Vship_SSIMU2Fp16Deltas: the distorted pyramid as FP16 deltas from the reference's
 
 
@@ -359,7 +359,7 @@ class SSIMU2Handler:
 
 class ButteraugliHandler:
     """One Butteraugli scorer (Vship_ButteraugliInitv2 / Compute*v3 / Free); half_bands=True stores
-    the MF, HF and UHF bands as FP16 (Vship_ButteraugliInitEx with Vship_ButterHalfBands)."""
+    the UHF bands as FP16 (Vship_ButteraugliInitEx with Vship_ButterHalfBands)."""
 
     def __init__(self, width: int, height: int, qnorm: int = 2, intensity_multiplier: float = 203.0,
                  half_bands: bool = False):

@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <vector>
 
 namespace vship {
@@ -122,7 +123,7 @@ struct BScaleDev {
 struct BGeom {
     BScaleDev s[2];  // 0 = full, 1 = half
     int64_t img_floats;
-    int half_bands;  // MF, HF and UHF stored as FP16 (hplane); the other planes stay FP32
+    int half_bands;  // UHF stored as FP16 (hplane); the other planes stay FP32
     int norm_tiles_x, norm_tiles;  // final-kernel tiling (32x32) at full scale
 };
 
@@ -130,26 +131,24 @@ struct BGeom {
 __device__ __forceinline__ float* iplane(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id) {
     return ib[img] + S.base + (int64_t)id * S.n;
 }
-// Half-band storage: the MF, HF and UHF bands, which only the pair stage reads, are kept as FP16
-// in a block after the nine FP32 planes (linear RGB / horizontal-pass scratch, XYB / D / HF_pre,
-// LF vals); plane `id` in [I_MF, I_UHF + 1] is the (id - I_MF)-th half plane of the block, with
-// the FP32 planes' element pitch.
+// Half-band storage: the UHF bands (X, Y), which only the pair stage reads, are kept as FP16 in a
+// block after the fourteen FP32 planes; plane `id` in [I_UHF, I_UHF + 1] is the (id - I_UHF)-th
+// half plane of the block, with the FP32 planes' element pitch. FP16 storage of the HF or MF bands
+// moves the norms by more than 1e-4 relative on some frames (a stored value's relative step is
+// 2^-11, and the Malta maps square differences of nearby values); of the UHF bands it does not.
 __device__ __forceinline__ __half* hplane(float* const* ib, const BScaleDev& S, int img, int id) {
-    return reinterpret_cast<__half*>(ib[img] + S.base + (int64_t)I_MF * S.n) + (int64_t)(id - I_MF) * S.n;
+    return reinterpret_cast<__half*>(ib[img] + S.base + (int64_t)I_UHF * S.n) + (int64_t)(id - I_UHF) * S.n;
 }
+// A plane is FP16 when the form stores half bands and it is a UHF plane (ids are compile-time
+// constants at every call site, so the test folds away).
+__device__ __forceinline__ constexpr bool half_plane(bool hb, int id) { return hb && id >= I_UHF; }
 template <bool HB>
 __device__ __forceinline__ void band_store(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id,
                                            int64_t i, float v) {
-    if (HB)
+    if (half_plane(HB, id))
         hplane(ib, S, img, id)[i] = __float2half_rn(v);
     else
         iplane(ib, g, S, img, id)[i] = v;
-}
-template <bool HB>
-__device__ __forceinline__ float band_load(float* const* ib, const BGeom& g, const BScaleDev& S, int img, int id,
-                                           int64_t i) {
-    if (HB) return __half2float(__ldg(hplane(ib, S, img, id) + i));
-    return __ldg(iplane(ib, g, S, img, id) + i);
 }
 // Select a scale with constant indices only, so the parameter struct is never copied to the
 // stack for a dynamic index.
@@ -662,7 +661,6 @@ constexpr int MS_CTRR = MS_CH + MS_R;
 constexpr int MS_CTR = 2 * MS_CTRR * MS_TW;
 constexpr int kMfSmem = (3 * MS_RAW + 3 * MS_HPLANE + MS_CTR) * 4;
 
-template <bool HB>
 __global__ void __launch_bounds__(256, 2) butter_mf_kernel(float* const* __restrict__ ib, BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
     float* raw = sm;                          // [channel][82 staged rows][60]
@@ -774,9 +772,10 @@ __global__ void __launch_bounds__(256, 2) butter_mf_kernel(float* const* __restr
                     hx *= sx + div_nr(yw * (1.0f - sx), yw + hy * hy);
                     h0p[i] = hx;
                     h1p[i] = hy;
-                    band_store<HB>(ib, g, S, img, I_MF + 0, i, remove_range(mf[0][o], 0.29f));
-                    band_store<HB>(ib, g, S, img, I_MF + 1, i, amplify_range(mf[1][o], 0.1f));
-                    band_store<HB>(ib, g, S, img, I_MF + 2, i, mf[2][o]);
+                    float* mfp = iplane(ib, g, S, img, I_MF);
+                    mfp[i] = remove_range(mf[0][o], 0.29f);
+                    mfp[S.n + i] = amplify_range(mf[1][o], 0.1f);
+                    mfp[2 * S.n + i] = mf[2][o];
                 }
             }
         }
@@ -985,13 +984,13 @@ __device__ __forceinline__ void malta_column(const float* __restrict__ Dt, int r
 // The six maps' raw (l0, l1) tiles are staged with cp.async, double-buffered across maps;
 // samples outside the image arrive as zeros, for which malta_pre returns exactly 0, the
 // reference's padding value (maltaDiff.hpp:549-553).
-// With half-band storage the raw tiles are FP16 rows of DFH_P halves staged from x0 - 8 (16-byte
-// chunks of 8 halves), and the window's column c sits at half c + 4 of its row.
+// With half-band storage the UHF maps' raw tiles are FP16 rows of DFH_P halves staged from x0 - 8
+// (16-byte chunks of 8 halves), in the same buffers, and the window's column c sits at half c + 4
+// of its row.
 constexpr int DF_RAW = DF_IH * DF_IW;
 constexpr int kDiffSmem = (4 * DF_RAW + DF_RAW + 2 * 8 * 256) * 4;
-constexpr int DFH_P = 56;                   // 48 staged halves + 8 of padding (7 quads per row)
-constexpr int DFH_RAWF = DF_IH * DFH_P / 2;  // one FP16 raw tile, in floats
-constexpr int kDiffSmemH = (4 * DFH_RAWF + DF_RAW + 2 * 8 * 256) * 4;
+constexpr int DFH_P = 56;  // 48 staged halves + 8 of padding (7 quads per row)
+static_assert(DF_IH * DFH_P / 2 <= DF_RAW, "an FP16 raw tile fits an FP32 tile's buffer");
 
 // L2AsymDiff's two terms for one pixel (simplerdiff.hpp:61-100), added to acc in the
 // reference's order. The two sign branches are one, on s2 mirrored to s1's side (as in
@@ -1012,7 +1011,7 @@ template <bool HB>
 __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __restrict__ ib, const int2* __restrict__ pimg,
                                                              BGeom g, int s) {
     extern __shared__ __align__(16) float sm[];
-    constexpr int RAWF = HB ? DFH_RAWF : DF_RAW;  // floats per raw tile
+    constexpr int RAWF = DF_RAW;  // floats per raw tile
     float* Dt = sm + 4 * RAWF;
     const int2 pi = pimg[blockIdx.z];
     const int i0 = pi.x, i1 = pi.y;
@@ -1025,38 +1024,34 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
 #pragma unroll
     for (int o = 0; o < 16; o++) accs[o * 256] = 0.f;
     const DiffParams& P = c_dp;
-    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X. Each channel's
-    // three maps are summed in that order, so the Y maps run first (m = 0, 2, 4) and the X maps
-    // after (1, 3, 5): the same sums, with one channel's accumulators live at a time.
-    auto map_of = [](int t) { return t < 3 ? 2 * t : 2 * (t - 3) + 1; };
+    // maltaDiff order (main.hpp:57-79): UHF Y, UHF X, HF Y, HF X, MF Y, MF X, map m = 0..5. Each
+    // channel's three maps (Y: m = 0, 2, 4; X: 1, 3, 5) are summed in that order into its own
+    // accumulators. The two UHF maps (the 9-tap Malta unit, FP16 tiles with half-band storage) run
+    // as one loop and the four HF and MF maps (the 5-tap unit, FP32 tiles) as another, so that
+    // neither loop carries the other's staging and conversion paths.
     auto plane_id = [](int m) { return (m < 2 ? I_UHF : m < 4 ? I_HF : I_MF) + 1 - (m & 1); };
-    auto stage = [&](float* dst, int img, int id) {
-        if (HB)
+    auto stage = [&](float* dst, int img, int id, auto half) {
+        if constexpr (decltype(half)::value)
             stage_tile_t<DF_IH, 6>(reinterpret_cast<__half*>(dst), DFH_P, (const __half*)hplane(ib, S, img, id), S.p,
                                    S.w, S.h, x0 - 8, y0 - DF_H);
         else
             stage_tile_t<DF_IH, DF_IW / 4>(dst, DF_IW, (const float*)iplane(ib, g, S, img, id), S.p, S.w, S.h,
                                            x0 - DF_H, y0 - DF_H);
     };
-    // the staged sample at this thread's output (column vc, row 8*vg + o of the tile)
-    auto center = [&](const float* tile, int o) {
-        if (HB)
-            return __half2float(reinterpret_cast<const __half*>(tile)[(8 * vg + o + DF_H) * DFH_P + vc + DF_H + 4]);
-        return tile[(8 * vg + o + DF_H) * DF_IW + vc + DF_H];
-    };
-    stage(sm, i0, plane_id(0));
-    stage(sm + RAWF, i1, plane_id(0));
-    cp_async_commit();
-#pragma unroll 1
-    for (int t = 0; t < 6; t++) {
-        const int m = map_of(t);
-        const float* r0 = sm + (t & 1) * 2 * RAWF;
+    // the staged sample at this thread's output (column vc, row 8*vg + o of an FP32 tile)
+    auto center = [&](const float* tile, int o) { return tile[(8 * vg + o + DF_H) * DF_IW + vc + DF_H]; };
+    // map m, whose raw tiles are staged in buffer pair m & 1; UHF: m < 2; next_half: the next
+    // map's tiles are FP16 (UHF X after UHF Y with half-band storage)
+    auto map_step = [&](int m, auto uhf, auto next_half) {
+        constexpr bool UHF = decltype(uhf)::value;
+        constexpr bool HALF = HB && UHF;
+        const float* r0 = sm + (m & 1) * 2 * RAWF;
         const float* r1 = r0 + RAWF;
-        if (t < 5) {
-            float* n0 = sm + ((t + 1) & 1) * 2 * RAWF;
-            const int id = plane_id(map_of(t + 1));
-            stage(n0, i0, id);
-            stage(n0 + RAWF, i1, id);
+        if (m < 5) {
+            float* n0 = sm + ((m + 1) & 1) * 2 * RAWF;
+            const int id = plane_id(m + 1);
+            stage(n0, i0, id, next_half);
+            stage(n0 + RAWF, i1, id, next_half);
             cp_async_commit();
             cp_async_wait<1>();
         } else {
@@ -1065,14 +1060,14 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         __syncthreads();
         const MaltaMap mm = c_dp.mm[m];
         // four neighbouring samples per thread (rows of 40 floats hold 10 whole quads): one 16-byte
-        // load per image (8 bytes of halves with FP16 bands) and one 16-byte store
+        // load per image (8 bytes of halves from an FP16 tile) and one 16-byte store
         constexpr int NQ = DF_IH * DF_IW / 4;
 #pragma unroll
         for (int k = 0; k < (NQ + 255) / 256; k++) {
             const int q = threadIdx.x + 256 * k;
             if (q < NQ) {
                 float4 a, b;
-                if (HB) {
+                if constexpr (HALF) {
                     const int r = q / (DF_IW / 4), c = 4 * (q - r * (DF_IW / 4));
                     const int hi = r * DFH_P + c + 4;  // a multiple of 4 halves: 8-byte aligned
                     const uint2 ua = *reinterpret_cast<const uint2*>(reinterpret_cast<const __half*>(r0) + hi);
@@ -1091,13 +1086,13 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
                                                                malta_pre(a.z, b.z, mm), malta_pre(a.w, b.w, mm));
             }
         }
-        // The HF and MF maps' own L2 terms (simplerdiff.hpp:41-100; channel X for odd m, Y for
-        // even), from the bands already staged here, before the barrier after which the next
-        // staging may overwrite this buffer: L2AsymDiff of HF, L2 of MF. The reference adds them
-        // after all three maps of the channel; here they join the channel's sum between maps, a
-        // different order of the same FP32 additions.
         float* acc = accs + (m & 1) * 8 * 256;  // this map's channel
-        if (m >= 2) {
+        if constexpr (!UHF) {
+            // The HF and MF maps' own L2 terms (simplerdiff.hpp:41-100; channel X for odd m, Y for
+            // even), from the bands already staged here, before the barrier after which the next
+            // staging may overwrite this buffer: L2AsymDiff of HF, L2 of MF. The reference adds
+            // them after all three maps of the channel; here they join the channel's sum between
+            // maps, a different order of the same FP32 additions.
             const int c = (m & 1) ? 0 : 1;
 #pragma unroll
             for (int o = 0; o < 8; o++) {
@@ -1113,9 +1108,21 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
             }
         }
         __syncthreads();
-        if (m < 2) malta_column<true>(Dt, 8 * vg, vc, acc);
-        else malta_column<false>(Dt, 8 * vg, vc, acc);
+        malta_column<UHF>(Dt, 8 * vg, vc, acc);
+    };
+    stage(sm, i0, plane_id(0), std::integral_constant<bool, HB>{});
+    stage(sm + RAWF, i1, plane_id(0), std::integral_constant<bool, HB>{});
+    cp_async_commit();
+    if constexpr (HB) {
+        // the UHF Y map stages FP16 tiles for UHF X, which stages FP32 tiles for HF Y
+        map_step(0, std::true_type{}, std::integral_constant<bool, HB>{});
+        map_step(1, std::true_type{}, std::false_type{});
+    } else {
+#pragma unroll 1
+        for (int m = 0; m < 2; m++) map_step(m, std::true_type{}, std::false_type{});
     }
+#pragma unroll 1
+    for (int m = 2; m < 6; m++) map_step(m, std::false_type{}, std::false_type{});
     const int x = x0 + vc;
     if (x >= S.w) return;
     // What the staged tiles do not hold: MF of the B channel (no Malta map; L2 only) and the LF
@@ -1125,7 +1132,7 @@ __global__ void __launch_bounds__(256, 3) butter_diff_kernel(float* const* __res
         const int y = y0 + 8 * vg + o;
         if (y < S.h) {
             const int64_t i = (int64_t)y * S.p + x;
-            const float dmb = band_load<HB>(ib, g, S, i0, I_MF + 2, i) - band_load<HB>(ib, g, S, i1, I_MF + 2, i);
+            const float dmb = __ldg(iplane(ib, g, S, i0, I_MF + 2) + i) - __ldg(iplane(ib, g, S, i1, I_MF + 2) + i);
             const float acc_b = P.wmf[2] * dmb * dmb;
             float dc[3];
 #pragma unroll
@@ -1361,9 +1368,9 @@ static BGeom make_bgeom(int64_t w, int64_t h, bool half_bands) {
         S.p = (int)round_up(cw, 8);
         S.n = round_up((int64_t)S.p * ch, 64);
         S.base = off;
-        // S.n is a multiple of 64, so the FP16 block (NIMG - I_MF half planes) keeps the next
+        // S.n is a multiple of 64, so the FP16 block (NIMG - I_UHF half planes) keeps the next
         // scale's base 256-byte aligned
-        off += half_bands ? S.n * I_MF + S.n * (NIMG - I_MF) / 2 : S.n * NIMG;
+        off += half_bands ? S.n * I_UHF + S.n * (NIMG - I_UHF) / 2 : S.n * NIMG;
         cw = half_dim(cw);
         ch = half_dim(ch);
     }
@@ -1424,10 +1431,9 @@ int butter_prepare_device() {
     int rc = upload_butter_tables();
     if (rc) return rc;
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_lf_v_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kVLfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmem));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_mf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kMfSmem));
     VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
-    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmemH));
+    VSHIP_CUDA_TRY(cudaFuncSetAttribute(butter_diff_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDiffSmem));
     const DiffParams P = make_diff_params();
     VSHIP_CUDA_TRY(cudaMemcpyToSymbol(c_dp, &P, sizeof(P)));
     return E_OK;
@@ -1566,8 +1572,7 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
             {
                 ProfScope ps_("butter_mf", st);
                 const dim3 gmf((unsigned)ceil_div(sw, MS_TW), (unsigned)ceil_div(sh, MS_SEG), ni);
-                if (half_bands) butter_mf_kernel<true><<<gmf, 256, kMfSmem, st>>>(ib, g, s);
-                else butter_mf_kernel<false><<<gmf, 256, kMfSmem, st>>>(ib, g, s);
+                butter_mf_kernel<<<gmf, 256, kMfSmem, st>>>(ib, g, s);
             }
             {
                 ProfScope ps_("butter_hf", st);
@@ -1578,7 +1583,7 @@ int butter_enqueue(int64_t w, int64_t h, int qnorm, float intensity, float* cons
         const dim3 gd((unsigned)ceil_div(sw, DF_TW), (unsigned)ceil_div(sh, DF_TH), np);
         {
             ProfScope ps_("butter_diff", st);
-            if (half_bands) butter_diff_kernel<true><<<gd, 256, kDiffSmemH, st>>>(ib, pimg, g, s);
+            if (half_bands) butter_diff_kernel<true><<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s);
             else butter_diff_kernel<false><<<gd, 256, kDiffSmem, st>>>(ib, pimg, g, s);
         }
         const dim3 gm((unsigned)ceil_div(sw, TB_TW), (unsigned)ceil_div(sh, TB_TH), np);

@@ -25,8 +25,8 @@ public:
     int qnorm = 2;
     float intensity = 203.f;
     int max_pairs = 0, max_images = 0;
-    // Keep the MF, HF and UHF bands as FP16 (set before init): 12.5 instead of 16 planes per
-    // image and scale; the norms move by the bands' FP16 rounding (the inf-norm by up to ~3e-4)
+    // Keep the UHF bands as FP16 (set before init): 15 instead of 16 planes per image and scale;
+    // the norms move by those bands' FP16 rounding (up to ~5e-5 relative, the inf-norm)
     bool half_bands = false;
     ButterScale sc[2]{};
     float* work = nullptr;          // all intermediate planes, [image][scale][plane]

@@ -34,7 +34,7 @@ enum : int {
     MULTI_FP16 = 4,      // candidate SSIMU2 pyramids stored as FP16 deltas
     MULTI_NO_GRAPH = 8,  // launch directly instead of replaying a CUDA graph
     MULTI_AUTOTUNE = 16,     // time the launch-knob candidates on the first call of a new layout
-    MULTI_BUTTER_HALF = 32   // Butteraugli MF, HF and UHF bands stored as FP16 (ButterEngine::half_bands)
+    MULTI_BUTTER_HALF = 32   // Butteraugli UHF bands stored as FP16 (ButterEngine::half_bands)
 };
 constexpr int kMaxRes = 8;
 

@@ -28,7 +28,7 @@ namespace vship {
 
 enum : int {
     SERVE_FP32_CANDIDATES = 1,   // keep SSIMULACRA2 candidate pyramids in FP32
-    SERVE_BUTTER_HALF_BANDS = 2  // Butteraugli MF, HF and UHF bands as FP16 (ButterEngine::half_bands)
+    SERVE_BUTTER_HALF_BANDS = 2  // Butteraugli UHF bands as FP16 (ButterEngine::half_bands)
 };
 
 struct ServeReq {
