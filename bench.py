@@ -331,7 +331,7 @@ def run_device(v, kind, ref, dst, steps, warmup, ws, chunk, yuv=None, half_bands
     return sec, prof, launches, result
 
 
-E2E_TRIALS = 3
+E2E_TRIALS = 5
 
 
 def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None, half_bands=False):
@@ -419,8 +419,8 @@ def run_e2e(v, kind, ref, dst, steps, warmup, nthreads, yuv=None, half_bands=Fal
     for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    # the host link and host memory are shared with other work on the machine: time three trials
-    # of `steps` steps and report the median (each trial's rate is kept beside it)
+    # the host link and host memory are shared with other work on the machine: time E2E_TRIALS
+    # trials of `steps` steps and report the median (each trial's rate is kept beside it)
     trials = []
     for _ in range(E2E_TRIALS):
         t0 = time.perf_counter()
