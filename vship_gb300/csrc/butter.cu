@@ -1158,17 +1158,18 @@ __global__ void __launch_bounds__(256, 6) butter_mask_blur_kernel(float* const* 
     const int x0 = blockIdx.x * TB_TW, y0 = blockIdx.y * TB_TH;
     float rxy[6];
     tile_masses_r8<2>(x0, y0, S.w, S.h, rxy);
+    // the two masks in two cp.async groups, so the second lands under the first one's blur
     tile_stage_r8(sm, iplane(ib, g, S, pi.x, I_PRE), S.p, S.w, S.h, x0, y0);
+    cp_async_commit();
     tile_stage_r8(sm + TB_RAW, iplane(ib, g, S, i1, I_PRE), S.p, S.w, S.h, x0, y0);
     cp_async_commit();
-    cp_async_wait<0>();
-    __syncthreads();
     float b[2][6];
-#pragma unroll
-    for (int m = 0; m < 2; m++) {
-        tile_blur_r8<2>(sm + m * TB_RAW, hb, rxy, b[m]);
-        __syncthreads();
-    }
+    cp_async_wait<1>();
+    __syncthreads();
+    tile_blur_r8<2>(sm, hb, rxy, b[0]);
+    cp_async_wait<0>();
+    __syncthreads();  // the second mask is staged and every thread is done with hb
+    tile_blur_r8<2>(sm + TB_RAW, hb, rxy, b[1]);
     const int vc = threadIdx.x & 31, vg = threadIdx.x >> 5;
     float* b0 = iplane(ib, g, S, i1, Q_B0);
     float* sac = iplane(ib, g, S, i1, Q_SAC);
